@@ -1,0 +1,486 @@
+// capi.cu -- extern "C" entry points of libpsfun_gb300 (see include/psfun_gb300.h).
+#include <atomic>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace psf {
+
+static cudaStream_t g_stream = nullptr;
+static bool g_stream_owned = false;
+static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+static int g_sms = 0;
+
+cudaStream_t stream() {
+  if (!g_stream) {
+    cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    g_stream_owned = true;
+  }
+  return g_stream;
+}
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+void count_launch(int n) { g_launches += n; }
+int sm_count() {
+  if (!g_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  return g_sms;
+}
+
+int DevBuf::ensure(size_t need) {
+  if (need <= bytes && ptr) return PSFUN_SUCCESS;
+  release();
+  cudaError_t e = cudaMalloc(&ptr, need);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    bytes = 0;
+    set_last_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return PSFUN_ERR_ALLOC_DEALLOC;
+  }
+  bytes = need;
+  return PSFUN_SUCCESS;
+}
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+// Fortran `character(len=20) :: s; s = val` then `select case (s)`.
+void set_fstr(char* dst, const char* src) {
+  size_t n = src ? strlen(src) : 0;
+  if (n > 20) n = 20;
+  memcpy(dst, src, n);
+  dst[n] = 0;
+}
+bool fstr_eq(const char* s, const char* lit) {
+  size_t ls = strlen(s), ll = strlen(lit);
+  while (ls > 0 && s[ls - 1] == ' ') --ls;
+  return ls == ll && strncmp(s, lit, ll) == 0;
+}
+static std::string upper_key(const char* what) {
+  std::string k(what ? what : "");
+  for (auto& ch : k) ch = (char)toupper((unsigned char)ch);
+  while (!k.empty() && k.back() == ' ') k.pop_back();
+  return k;
+}
+
+bool parse_fun(const psfun_serial* fun, FunParams* fp) {
+  fp->scaling = fun->scaling;
+  fp->padedegree = fun->padedegree;
+  fp->phiorder = fun->phiorder;
+  fp->fname = FN_INVALID;
+  fp->variant = VAR_INVALID;
+  if (fstr_eq(fun->fname, "EXP")) {
+    fp->fname = FN_EXP;
+    if (fstr_eq(fun->variant, "TAYLOR")) fp->variant = VAR_TAYLOR;
+    else if (fstr_eq(fun->variant, "SASQ")) fp->variant = VAR_SASQ;
+    else if (fstr_eq(fun->variant, "GENPADE")) fp->variant = VAR_GENPADE;
+    else if (fstr_eq(fun->variant, "CHBHES")) fp->variant = VAR_CHBHES;
+    else if (fstr_eq(fun->variant, "CHBGEN")) fp->variant = VAR_CHBGEN;
+    else if (fstr_eq(fun->variant, "CHBSYM")) fp->variant = VAR_CHBSYM;
+    else return false;  // includes the default 'EXPOKIT' (psfun_d_serial_mod.F90:387-390)
+    if (fp->variant == VAR_GENPADE && (fun->padedegree < 1 || fun->padedegree > 60)) return false;
+    return true;
+  }
+  if (fstr_eq(fun->fname, "PHI")) {
+    fp->fname = FN_PHI;
+    return fun->phiorder >= 1 && fun->padedegree >= 1 && fun->padedegree <= 60;
+  }
+  if (fstr_eq(fun->fname, "USERF")) {
+    fp->fname = FN_USERF;
+    if (fstr_eq(fun->variant, "SYM")) { fp->variant = VAR_SYM; return true; }
+    return false;
+  }
+  return false;
+}
+
+}  // namespace psf
+
+using namespace psf;
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* psfun_gpu_version(void) { return "psfun_gb300 0.1 (sm_103a)"; }
+const char* psfun_gpu_last_error(void) { return g_last_error.c_str(); }
+long long psfun_gpu_kernel_launches(void) { return g_launches.load(); }
+
+int psfun_gpu_set_stream(void* s) {
+  if (g_stream && g_stream_owned) cudaStreamDestroy(g_stream);
+  g_stream = (cudaStream_t)s;
+  g_stream_owned = false;
+  if (!s) stream();
+  return PSFUN_SUCCESS;
+}
+void* psfun_gpu_get_stream(void) { return (void*)stream(); }
+
+// ---- CSR ------------------------------------------------------------------
+int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32_t* ja, const double* val,
+                         int index_base, psfun_csr** out) {
+  if (!out) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  *out = nullptr;
+  if (n < 0 || nnz < 0 || (n > 0 && !irp) || (nnz > 0 && (!ja || !val)) || (index_base != 0 && index_base != 1)) {
+    set_last_error("invalid CSR arguments");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  if (n > 0x7ffffff0LL || nnz > 0x7ffffff0LL) {
+    set_last_error("int32 CSR index overflow");
+    return PSFUN_ERR_INVALID_MATRIX;
+  }
+  // validate + rebase to 0 (bit-exact: every index is checked, none is altered
+  // other than the constant base shift)
+  std::vector<int32_t> hirp(n + 1);
+  if (n == 0) {
+    hirp[0] = 0;
+  } else {
+    for (int64_t i = 0; i <= n; ++i) hirp[i] = irp[i] - index_base;
+    if (hirp[0] != 0 || hirp[n] != nnz) {
+      set_last_error("rowptr must start at the index base and end at nnz");
+      return PSFUN_ERR_INVALID_MATRIX;
+    }
+    for (int64_t i = 0; i < n; ++i)
+      if (hirp[i + 1] < hirp[i]) {
+        set_last_error("rowptr not monotone");
+        return PSFUN_ERR_INVALID_MATRIX;
+      }
+  }
+  std::vector<int32_t> hja(nnz);
+  for (int64_t k = 0; k < nnz; ++k) {
+    const int32_t c = ja[k] - index_base;
+    if (c < 0 || c >= n) {
+      set_last_error("column index out of range");
+      return PSFUN_ERR_INVALID_MATRIX;
+    }
+    hja[k] = c;
+  }
+  auto* a = new psfun_csr();
+  a->n = n;
+  a->nnz = nnz;
+  // tile schedule
+  std::vector<int32_t> tiles;
+  tiles.reserve(n / kTileRows + 16);
+  int64_t r = 0;
+  while (r < n) {
+    tiles.push_back((int32_t)r);
+    const int64_t start = r;
+    int64_t acc = 0;
+    while (r < n && r - start < kTileRows && acc + (hirp[r + 1] - hirp[r]) <= kTileNnz) {
+      acc += hirp[r + 1] - hirp[r];
+      ++r;
+    }
+    if (r == start) ++r;  // a row longer than a tile: its own tile
+  }
+  tiles.push_back((int32_t)n);
+  a->ntiles = (int32_t)tiles.size() - 1;
+  // norms and diagonal
+  double ninf = 0.0;
+  a->h_diag.assign(n, 0.0);
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int32_t k = hirp[i]; k < hirp[i + 1]; ++k) {
+      s += fabs(val[k]);
+      if (hja[k] == i) a->h_diag[i] += val[k];
+    }
+    if (s > ninf) ninf = s;
+  }
+  a->norm_inf = ninf;
+  cudaStream_t s = stream();
+  auto fail = [&](cudaError_t e) {
+    set_last_error(std::string("csr_create: ") + cudaGetErrorString(e));
+    psfun_gpu_csr_destroy(a);
+    return PSFUN_ERR_CUDA;
+  };
+  cudaError_t e;
+  // padded allocations so that 16-byte bulk copies never leave the buffers
+  if ((e = cudaMalloc(&a->irp, sizeof(int32_t) * (n + 1 + 8))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->ja, sizeof(int32_t) * (nnz + 16))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->val, sizeof(double) * (nnz + 8))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->tile_row, sizeof(int32_t) * tiles.size())) != cudaSuccess) return fail(e);
+  cudaMemsetAsync(a->ja, 0, sizeof(int32_t) * (nnz + 16), s);
+  cudaMemsetAsync(a->val, 0, sizeof(double) * (nnz + 8), s);
+  if ((e = cudaMemcpyAsync(a->irp, hirp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return fail(e);
+  if (nnz > 0) {
+    if ((e = cudaMemcpyAsync(a->ja, hja.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return fail(e);
+    if ((e = cudaMemcpyAsync(a->val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return fail(e);
+  }
+  if ((e = cudaMemcpyAsync(a->tile_row, tiles.data(), sizeof(int32_t) * tiles.size(), cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return fail(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(e);
+  *out = a;
+  return PSFUN_SUCCESS;
+}
+
+int psfun_gpu_csr_destroy(psfun_csr* a) {
+  if (!a) return PSFUN_SUCCESS;
+  if (a->irp) cudaFree(a->irp);
+  if (a->ja) cudaFree(a->ja);
+  if (a->val) cudaFree(a->val);
+  if (a->tile_row) cudaFree(a->tile_row);
+  if (a->diag_inv) cudaFree(a->diag_inv);
+  delete a;
+  return PSFUN_SUCCESS;
+}
+
+int psfun_gpu_csr_info(const psfun_csr* a, int64_t* n, int64_t* nnz, int64_t* ntiles, double* norm_inf) {
+  if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (n) *n = a->n;
+  if (nnz) *nnz = a->nnz;
+  if (ntiles) *ntiles = a->ntiles;
+  if (norm_inf) *norm_inf = a->norm_inf;
+  return PSFUN_SUCCESS;
+}
+
+}  // extern "C"
+
+namespace psf {
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv_axpby(CsrDev A, const double* x, double alpha, double beta,
+                                                             double* y, int* err) {
+  __shared__ SpmvSmem sm;
+  spmv_smem_init(sm);
+  EpiAxpby epi{alpha, beta, y};
+  spmv_tiles(A, x, epi, sm, err, blockIdx.x, gridDim.x);
+}
+
+int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
+  static DevBuf errbuf;
+  PSF_TRY(errbuf.ensure(sizeof(int)));
+  cudaStream_t s = stream();
+  PSF_CUDA(cudaMemsetAsync(errbuf.ptr, 0, sizeof(int), s));
+  if (a->ntiles > 0) {
+    int g = a->ntiles;
+    const int cap = sm_count() * 8;
+    if (g > cap) g = cap;
+    k_spmv_axpby<<<g, kSpmvThreads, 0, s>>>(a->dev(), x, alpha, beta, y, errbuf.as<int>());
+    count_launch();
+    PSF_CUDA(cudaGetLastError());
+  }
+  int herr = 0;
+  PSF_CUDA(cudaMemcpyAsync(&herr, errbuf.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (herr & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
+  return PSFUN_SUCCESS;
+}
+}  // namespace psf
+
+extern "C" {
+
+int psfun_gpu_csr_spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
+  if (!a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  return spmv_device(a, alpha, x, beta, y);
+}
+
+int psfun_gpu_csr_spmv(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
+  if (!a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  const size_t nb = sizeof(double) * (a->n + 1);
+  DevBuf dx, dy;
+  PSF_TRY(dx.ensure(nb));
+  if (dy.ensure(nb) != PSFUN_SUCCESS) { dx.release(); return PSFUN_ERR_ALLOC_DEALLOC; }
+  cudaStream_t s = stream();
+  int rc = PSFUN_SUCCESS;
+  if (cudaMemcpyAsync(dx.ptr, x, sizeof(double) * a->n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(dy.ptr, y, sizeof(double) * a->n, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = PSFUN_ERR_CUDA;
+  if (rc == PSFUN_SUCCESS) rc = spmv_device(a, alpha, dx.as<double>(), beta, dy.as<double>());
+  if (rc == PSFUN_SUCCESS) {
+    if (cudaMemcpyAsync(y, dy.ptr, sizeof(double) * a->n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = PSFUN_ERR_CUDA;
+  }
+  dx.release();
+  dy.release();
+  return rc;
+}
+
+// ---- serial function object -------------------------------------------------
+int psfun_gpu_serial_create(psfun_serial** out) {
+  if (!out) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  auto* f = new psfun_serial();
+  set_fstr(f->fname, "EXP");
+  set_fstr(f->variant, "EXPOKIT");
+  *out = f;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_serial_destroy(psfun_serial* fun) {
+  delete fun;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_serial_set_string(psfun_serial* fun, const char* what, const char* val) {
+  if (!fun || !val) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string k = upper_key(what);
+  if (k == "FNAME") set_fstr(fun->fname, val);
+  else if (k == "VARIANT") set_fstr(fun->variant, val);
+  else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_serial_set_real(psfun_serial* fun, const char* what, double val) {
+  if (!fun) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (upper_key(what) == "SCALING") { fun->scaling = val; return PSFUN_SUCCESS; }
+  return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+}
+int psfun_gpu_serial_set_integer(psfun_serial* fun, const char* what, int val) {
+  if (!fun) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string k = upper_key(what);
+  if (k == "PADE_DEGREE") fun->padedegree = val;
+  else if (k == "PHIORDER") fun->phiorder = val;
+  else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_serial_set_function(psfun_serial* fun, const char* what, psfun_userf val) {
+  if (!fun) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (upper_key(what) == "FPOINTER") { fun->f_ptr = val; return PSFUN_SUCCESS; }
+  return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+}
+int psfun_gpu_serial_get(const psfun_serial* fun, char* fname, char* variant, double* scaling, int* padedegree,
+                         int* phiorder) {
+  if (!fun) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (fname) strcpy(fname, fun->fname);
+  if (variant) strcpy(variant, fun->variant);
+  if (scaling) *scaling = fun->scaling;
+  if (padedegree) *padedegree = fun->padedegree;
+  if (phiorder) *phiorder = fun->phiorder;
+  return PSFUN_SUCCESS;
+}
+
+int psfun_gpu_serial_apply(psfun_serial* fun, int n, const double* a, int lda, double* y, const double* x) {
+  if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (n < 1 || lda < n) return PSFUN_ERR_FROM_SUBROUTINE;
+  DevBuf da, dx, dy;
+  PSF_TRY(da.ensure(sizeof(double) * (size_t)n * n));
+  PSF_TRY(dx.ensure(sizeof(double) * n));
+  PSF_TRY(dy.ensure(sizeof(double) * n));
+  cudaStream_t s = stream();
+  int rc = PSFUN_SUCCESS;
+  if (cudaMemcpy2DAsync(da.ptr, sizeof(double) * n, a, sizeof(double) * lda, sizeof(double) * n, n,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(dx.ptr, x, sizeof(double) * n, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = PSFUN_ERR_CUDA;
+  if (rc == PSFUN_SUCCESS) rc = serial_apply_device(fun, n, da.as<double>(), n, dy.as<double>(), dx.as<double>());
+  if (rc == PSFUN_SUCCESS) {
+    if (cudaMemcpyAsync(y, dy.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = PSFUN_ERR_CUDA;
+  }
+  da.release();
+  dx.release();
+  dy.release();
+  return rc;
+}
+
+}  // extern "C"
+
+namespace psf {
+// COO -> dense n x n on the device (psfun_d_serial_apply_sparse, :547-559)
+__global__ void k_csr_to_dense(CsrDev A, double* D) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < A.n; r += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t k = A.irp[r]; k < A.irp[r + 1]; ++k) D[r + (size_t)A.ja[k] * A.n] = A.val[k];
+}
+}  // namespace psf
+
+extern "C" {
+
+int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, const double* x) {
+  if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  const int64_t n = a->n;
+  if (n < 1 || n > 8192) return PSFUN_ERR_FROM_SUBROUTINE;
+  DevBuf da, dx, dy;
+  PSF_TRY(da.ensure(sizeof(double) * (size_t)n * n));
+  PSF_TRY(dx.ensure(sizeof(double) * n));
+  PSF_TRY(dy.ensure(sizeof(double) * n));
+  cudaStream_t s = stream();
+  int rc = PSFUN_SUCCESS;
+  cudaMemsetAsync(da.ptr, 0, sizeof(double) * (size_t)n * n, s);
+  k_csr_to_dense<<<(int)((n + 255) / 256), 256, 0, s>>>(a->dev(), da.as<double>());
+  count_launch();
+  if (cudaMemcpyAsync(dx.ptr, x, sizeof(double) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = PSFUN_ERR_CUDA;
+  if (rc == PSFUN_SUCCESS) rc = serial_apply_device(fun, (int)n, da.as<double>(), (int)n, dy.as<double>(), dx.as<double>());
+  if (rc == PSFUN_SUCCESS) {
+    if (cudaMemcpyAsync(y, dy.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = PSFUN_ERR_CUDA;
+  }
+  da.release();
+  dx.release();
+  dy.release();
+  return rc;
+}
+
+// ---- Krylov method object ------------------------------------------------------
+int psfun_gpu_krylov_create(psfun_krylov** out) {
+  if (!out) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  auto* m = new psfun_krylov();
+  set_fstr(m->kname, "ARNOLDI");
+  set_fstr(m->kmethd, "CG");
+  *out = m;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_krylov_destroy(psfun_krylov* meth) {
+  if (!meth) return PSFUN_SUCCESS;
+  meth->V.release();
+  meth->u.release();
+  meth->small.release();
+  meth->scratch.release();
+  meth->partials.release();
+  meth->ctrl.release();
+  meth->xy.release();
+  delete meth;
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char* val) {
+  if (!meth || !val) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string k = upper_key(what);
+  if (k == "KNAME") { set_fstr(meth->kname, val); return PSFUN_SUCCESS; }
+  return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+}
+int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val) {
+  if (!meth) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string k = upper_key(what);
+  if (k == "ITMAX") meth->itmax = val;
+  else if (k == "ITRACE") meth->itrace = val;
+  else if (k == "ISTOPC") meth->istopc = val;
+  else if (k == "IRST") meth->irst = val;
+  else if (k == "KEEPLAST") meth->keeplast = val;
+  else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  return PSFUN_SUCCESS;
+}
+
+int psfun_gpu_d_krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y,
+                                    const double* x, double eps, int itmax, int itrace, int istop, int* iter,
+                                    double* err, double* res, int res_cap, int* res_len) {
+  if (!meth || !fun || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  return krylov_apply_device(meth, fun, a, y, x, eps, itmax, itrace, istop, iter, err, res, res_cap, res_len);
+}
+
+int psfun_gpu_d_krylov_apply(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x,
+                             double eps, int itmax, int itrace, int istop, int* iter, double* err, double* res,
+                             int res_cap, int* res_len) {
+  if (!meth || !fun || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  const int64_t n = a->n;
+  const size_t vb = sizeof(double) * (size_t)((n + 31) & ~31LL);
+  PSF_TRY(meth->xy.ensure(2 * vb + 64));
+  double* dx = meth->xy.as<double>();
+  double* dy = reinterpret_cast<double*>(meth->xy.as<char>() + vb);
+  cudaStream_t s = stream();
+  PSF_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  const int rc = krylov_apply_device(meth, fun, a, dy, dx, eps, itmax, itrace, istop, iter, err, res, res_cap, res_len);
+  if (rc != PSFUN_SUCCESS) return rc;
+  PSF_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  return PSFUN_SUCCESS;
+}
+
+}  // extern "C"

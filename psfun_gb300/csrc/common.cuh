@@ -1,0 +1,200 @@
+// common.cuh -- device utilities shared by the psfun_gb300 kernels (sm_103a).
+//
+// FP64 is the arithmetic of the whole path.  On GB300 the FP64 pipe retires
+// about 2 DFMA per clock per SM (~0.6 TFMA/s per GPU) against ~6.7 TB/s of HBM,
+// so kernels are written to spend FP64 instructions only on the algorithm's own
+// multiply-adds: index arithmetic stays integer, scalars are folded on the host
+// or by one thread, and reductions are deterministic (fixed order) so that
+// repeated solves are bitwise reproducible.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define PSF_DEVINL __device__ __forceinline__
+
+namespace psf {
+
+// Error flags a kernel can raise in the solve's control block.
+enum : int {
+  DEVERR_NONE = 0,
+  DEVERR_TIMEOUT = 1,   // a bounded wait (mbarrier or grid barrier) gave up
+  DEVERR_SINGULAR = 2,  // dense solve met an exactly zero pivot
+  DEVERR_BADSIZE = 4,   // a dimension exceeded the workspace it was given
+  DEVERR_FUNC = 8,      // invalid function / variant selector
+};
+
+// Wall-clock limit for any spin-wait in this library (nanoseconds).
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+
+PSF_DEVINL unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+PSF_DEVINL double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+PSF_DEVINL double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum; every thread gets the result.  `red` needs blockDim/32
+// doubles of shared memory.  The summation order is fixed.
+PSF_DEVINL double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+
+PSF_DEVINL double block_max(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_max(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+
+// Sum of `count` partials in a fixed order by one block (all threads get it).
+PSF_DEVINL double block_sum_array(const volatile double* p, int count, double* red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) v += p[i];
+  return block_sum(v, red);
+}
+
+// "Last block done" reduction: every block stores its partial, the block that
+// arrives last sums all partials in index order and runs `fin(total)` with one
+// thread.  No spinning: blocks that are not last simply return.
+template <class Fin>
+PSF_DEVINL void last_block_reduce(double partial, double* partials, unsigned int* counter, double* red, Fin fin) {
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = partial;
+    __threadfence();
+    unsigned int prev = atomicAdd(counter, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    double tot = block_sum_array(partials, gridDim.x, red);
+    if (threadIdx.x == 0) {
+      *counter = 0u;
+      fin(tot);
+      __threadfence();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier for cooperative launches (all CTAs co-resident).
+// count/gen live in global memory and start at zero.  Returns false (and sets
+// *err) if the barrier did not complete within kWaitLimitNs.
+// ---------------------------------------------------------------------------
+PSF_DEVINL bool grid_barrier(unsigned int* count, volatile unsigned int* gen, int* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    unsigned int g = *gen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      *count = 0u;
+      __threadfence();
+      atomicAdd((unsigned int*)gen, 1u);
+    } else {
+      unsigned long long t0 = globaltimer_ns();
+      while (*gen == g) {
+        if (*(volatile int*)err != 0) { ok = 0; break; }
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+          atomicOr(err, DEVERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// TMA bulk copies (cp.async.bulk) with an mbarrier, bounded waits.
+// ---------------------------------------------------------------------------
+PSF_DEVINL uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+PSF_DEVINL void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+PSF_DEVINL void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+PSF_DEVINL bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for phase `parity` of the barrier; false after kWaitLimitNs.
+PSF_DEVINL bool mbar_wait(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  unsigned long long t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+  return true;
+}
+
+// 1-D bulk copy global -> shared; both addresses 16-byte aligned, bytes % 16 == 0.
+PSF_DEVINL void bulk_g2s(void* dst_smem, const void* src_gmem, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+PSF_DEVINL void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Streaming loads that should not displace reused data in L1.
+PSF_DEVINL double ld_stream(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+}  // namespace psf

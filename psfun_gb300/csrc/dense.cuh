@@ -1,0 +1,760 @@
+// dense.cuh -- the projected f(H) on the device, FP64, inside one CTA.
+//
+// Restates the dense routines behind psfun_d_serial%apply
+// (serial/psfun_d_serial_mod.F90:172-523):
+//   EXP/GENPADE  DGPADM             serial/exponential/dgpadm.f:53-168
+//   EXP/CHBHES   DNCHBV             serial/exponential/dnchbv.f:46-113
+//   EXP/CHBSYM   DSCHBV             serial/exponential/dschbv.f (ZSYSV solve)
+//   EXP/CHBGEN   DGCHBV             serial/exponential/dgchbv.f (ZGESV solve)
+//   EXP/SASQ     r8mat_expm1        serial/exponential/taylor.f90:54-103
+//   EXP/TAYLOR   r8mat_expm2        serial/exponential/taylor.f90:159-176
+//   PHI          phi_k via the augmented matrix [[sH, x e1^T],[0, J_k]]
+//   USERF/SYM    symmetric eigendecomposition (DSYEV role), f on the host
+// All matrices are column-major with a leading dimension, exactly as the
+// Fortran arrays.  Every routine is called by all threads of the block with
+// block-uniform arguments and ends with __syncthreads().  Work arrays live in
+// a global scratch buffer (L1/L2 resident at these sizes).
+#pragma once
+
+#include <cuComplex.h>
+
+#include "common.cuh"
+
+namespace psf {
+
+enum FName : int { FN_INVALID = 0, FN_EXP = 1, FN_PHI = 2, FN_USERF = 3 };
+enum Variant : int {
+  VAR_INVALID = 0,
+  VAR_TAYLOR = 1,
+  VAR_SASQ = 2,
+  VAR_GENPADE = 3,
+  VAR_CHBHES = 4,
+  VAR_CHBGEN = 5,
+  VAR_CHBSYM = 6,
+  VAR_SYM = 7
+};
+
+struct FunParams {
+  int fname;
+  int variant;
+  double scaling;
+  int padedegree;
+  int phiorder;
+};
+
+// Scratch (doubles) needed by fh_apply_cta for an m x m problem.
+__host__ __device__ inline size_t fh_scratch_doubles(int m, int phiorder) {
+  size_t M = (size_t)m + (size_t)(phiorder > 0 ? phiorder : 1) + 1;
+  size_t a = 6 * M * M + 64 * M + 512;
+  size_t b = 16 * M * M + 64 * M + 512;  // 7 complex m x m systems
+  return a > b ? a : b;
+}
+
+struct DenseSmem {
+  double red[32];
+  double dv[8];
+  int iv[8];
+  double coef[64];
+};
+
+// ---- real building blocks --------------------------------------------------
+
+// C = alpha * A * B (m x m).  alpha is folded into B(l,j) and the sum over l
+// runs in order, the operation order of the reference BLAS DGEMM.
+PSF_DEVINL void cta_gemm(int m, double alpha, const double* A, int lda, const double* B, int ldb, double* C,
+                         int ldc) {
+  const int nrb = (m + 3) >> 2;
+  for (int task = threadIdx.x; task < nrb * m; task += blockDim.x) {
+    const int j = task / nrb;
+    const int i0 = (task - j * nrb) << 2;
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    const double* a = A + i0;
+    const double* b = B + (size_t)j * ldb;
+    if (i0 + 3 < m) {
+      for (int l = 0; l < m; ++l) {
+        const double t = alpha * b[l];
+        const double* al = a + (size_t)l * lda;
+        c0 = fma(t, al[0], c0);
+        c1 = fma(t, al[1], c1);
+        c2 = fma(t, al[2], c2);
+        c3 = fma(t, al[3], c3);
+      }
+      double* c = C + i0 + (size_t)j * ldc;
+      c[0] = c0; c[1] = c1; c[2] = c2; c[3] = c3;
+    } else {
+      for (int l = 0; l < m; ++l) {
+        const double t = alpha * b[l];
+        const double* al = a + (size_t)l * lda;
+        c0 = fma(t, al[0], c0);
+        if (i0 + 1 < m) c1 = fma(t, al[1], c1);
+        if (i0 + 2 < m) c2 = fma(t, al[2], c2);
+      }
+      double* c = C + i0 + (size_t)j * ldc;
+      c[0] = c0;
+      if (i0 + 1 < m) c[1] = c1;
+      if (i0 + 2 < m) c[2] = c2;
+    }
+  }
+  __syncthreads();
+}
+
+PSF_DEVINL void cta_set_identity(int m, double d, double* A, int lda) {
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int j = t / m, i = t - j * m;
+    A[i + (size_t)j * lda] = (i == j) ? d : 0.0;
+  }
+  __syncthreads();
+}
+
+PSF_DEVINL void cta_copy(int m, const double* A, int lda, double* B, int ldb) {
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int j = t / m, i = t - j * m;
+    B[i + (size_t)j * ldb] = A[i + (size_t)j * lda];
+  }
+  __syncthreads();
+}
+
+// max_i sum_j |A(i,j)|
+PSF_DEVINL double cta_norm_inf(int m, const double* A, int lda, DenseSmem& sm) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < m; ++j) s += fabs(A[i + (size_t)j * lda]);
+    v = fmax(v, s);
+  }
+  return block_max(v, sm.red);
+}
+
+// y = A x (thread per row, sum over j in order)
+PSF_DEVINL void cta_gemv(int m, const double* A, int lda, const double* x, double* y) {
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < m; ++j) s = fma(A[i + (size_t)j * lda], x[j], s);
+    y[i] = s;
+  }
+  __syncthreads();
+}
+
+// First index of the largest |A(i,k)|, i in [k, m) (LAPACK IDAMAX rule).
+PSF_DEVINL void cta_pivot(int m, int k, const double* A, int lda, DenseSmem& sm) {
+  if (threadIdx.x < 32) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + (int)threadIdx.x; i < m; i += 32) {
+      const double v = fabs(A[i + (size_t)k * lda]);
+      if (v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (threadIdx.x == 0) { sm.iv[0] = bi; sm.dv[0] = best; }
+  }
+  __syncthreads();
+}
+
+// Solve A X = B (A m x m, B m x nrhs) by Gaussian elimination with partial
+// pivoting, B eliminated alongside (DGESV semantics).  Returns false on an
+// exactly zero pivot.
+PSF_DEVINL bool cta_gesv(int m, int nrhs, double* A, int lda, double* B, int ldb, DenseSmem& sm) {
+  for (int k = 0; k < m; ++k) {
+    cta_pivot(m, k, A, lda, sm);
+    const int p = sm.iv[0];
+    if (sm.dv[0] == 0.0) { __syncthreads(); return false; }
+    if (p != k) {
+      for (int j = threadIdx.x; j < m + nrhs; j += blockDim.x) {
+        double* a = (j < m) ? A + (size_t)j * lda : B + (size_t)(j - m) * ldb;
+        const double t = a[k]; a[k] = a[p]; a[p] = t;
+      }
+      __syncthreads();
+    }
+    const double piv = A[k + (size_t)k * lda];
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)k * lda] /= piv;
+    __syncthreads();
+    const int rows = m - k - 1;
+    if (rows > 0) {
+      const int cols = rows + nrhs;
+      for (int t = threadIdx.x; t < rows * cols; t += blockDim.x) {
+        const int jj = t / rows, i = k + 1 + (t - jj * rows);
+        const double l = A[i + (size_t)k * lda];
+        if (jj < rows) {
+          const int j = k + 1 + jj;
+          A[i + (size_t)j * lda] = fma(-l, A[k + (size_t)j * lda], A[i + (size_t)j * lda]);
+        } else {
+          const int j = jj - rows;
+          B[i + (size_t)j * ldb] = fma(-l, B[k + (size_t)j * ldb], B[i + (size_t)j * ldb]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < nrhs; j += blockDim.x) {
+    double* b = B + (size_t)j * ldb;
+    for (int i = m - 1; i >= 0; --i) {
+      double t = b[i];
+      for (int l = i + 1; l < m; ++l) t = fma(-A[i + (size_t)l * lda], b[l], t);
+      b[i] = t / A[i + (size_t)i * lda];
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// r8mat_fss (r8lib.f90:12806): row-normalising elimination used by SASQ.
+PSF_DEVINL bool cta_fss(int n, double* a, int nb, double* b, DenseSmem& sm) {
+  for (int jcol = 0; jcol < n; ++jcol) {
+    cta_pivot(n, jcol, a, n, sm);
+    const int ip = sm.iv[0];
+    if (sm.dv[0] == 0.0) { __syncthreads(); return false; }
+    if (ip != jcol) {
+      for (int j = threadIdx.x; j < n + nb; j += blockDim.x) {
+        double* c = (j < n) ? a + (size_t)j * n : b + (size_t)(j - n) * n;
+        const double t = c[jcol]; c[jcol] = c[ip]; c[ip] = t;
+      }
+      __syncthreads();
+    }
+    const double d = a[jcol + (size_t)jcol * n];
+    __syncthreads();
+    // a(jcol, jcol+1:n) /= d ; b(jcol, 1:nb) /= d
+    for (int j = threadIdx.x; j < (n - jcol - 1) + nb; j += blockDim.x) {
+      if (j < n - jcol - 1) a[jcol + (size_t)(jcol + 1 + j) * n] /= d;
+      else b[jcol + (size_t)(j - (n - jcol - 1)) * n] /= d;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) a[jcol + (size_t)jcol * n] = 1.0;
+    const int rows = n - jcol - 1;
+    const int cols = (n - jcol - 1) + nb;
+    for (int t = threadIdx.x; t < rows * cols; t += blockDim.x) {
+      const int jj = t / rows, i = jcol + 1 + (t - jj * rows);
+      const double temp = -a[i + (size_t)jcol * n];
+      if (temp == 0.0) continue;
+      if (jj < n - jcol - 1) {
+        const int j = jcol + 1 + jj;
+        a[i + (size_t)j * n] = fma(temp, a[jcol + (size_t)j * n], a[i + (size_t)j * n]);
+      } else {
+        const int j = jj - (n - jcol - 1);
+        b[i + (size_t)j * n] = fma(temp, b[jcol + (size_t)j * n], b[i + (size_t)j * n]);
+      }
+    }
+    __syncthreads();
+    for (int i = jcol + 1 + threadIdx.x; i < n; i += blockDim.x) a[i + (size_t)jcol * n] = 0.0;
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    double* bj = b + (size_t)j * n;
+    for (int jcol = n - 1; jcol >= 1; --jcol)
+      for (int i = 0; i < jcol; ++i) bj[i] = fma(-a[i + (size_t)jcol * n], bj[jcol], bj[i]);
+  }
+  __syncthreads();
+  return true;
+}
+
+// ---- DGPADM -----------------------------------------------------------------
+// expH = exp(t H), m x m, leading dimension m.  Returns 0, or DEVERR_* flags.
+PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, double* expH, double* scratch,
+                          DenseSmem& sm) {
+  if (m < 1 || ideg < 1 || ideg > 60) return DEVERR_BADSIZE;
+  const size_t mm = (size_t)m * m;
+  double* h2 = scratch;
+  double* slot0 = scratch + mm;
+  double* slot1 = scratch + 2 * mm;
+  double* slot2 = scratch + 3 * mm;
+  double hnorm = fabs(t * cta_norm_inf(m, H, ldh, sm));
+  if (hnorm == 0.0) return DEVERR_SINGULAR;  // reference: stop 'null H'
+  int ns = (int)(log(hnorm) / log(2.0)) + 2;
+  if (ns < 0) ns = 0;
+  const double scale = ldexp(t, -ns);
+  const double scale2 = scale * scale;
+  if (threadIdx.x == 0) {
+    sm.coef[0] = 1.0;
+    for (int k = 1; k <= ideg; ++k)
+      sm.coef[k] = (sm.coef[k - 1] * (double)(ideg + 1 - k)) / (double)(k * (2 * ideg + 1 - k));
+  }
+  __syncthreads();
+  cta_gemm(m, scale2, H, ldh, H, ldh, h2, m);
+  double* p = slot0;
+  double* q = slot1;
+  double* fr = slot2;
+  cta_set_identity(m, sm.coef[ideg - 1], p, m);
+  cta_set_identity(m, sm.coef[ideg], q, m);
+  int iodd = 1;
+  for (int k = ideg - 1; k > 0; --k) {
+    double* used = iodd ? q : p;
+    cta_gemm(m, 1.0, used, m, h2, m, fr, m);
+    for (int j = threadIdx.x; j < m; j += blockDim.x) fr[j + (size_t)j * m] += sm.coef[k - 1];
+    __syncthreads();
+    if (iodd) q = fr; else p = fr;
+    fr = used;
+    iodd = 1 - iodd;
+  }
+  if (iodd == 1) {
+    cta_gemm(m, scale, q, m, H, ldh, fr, m);
+    double* tmp = q; q = fr; fr = tmp;
+  } else {
+    cta_gemm(m, scale, p, m, H, ldh, fr, m);
+    double* tmp = p; p = fr; fr = tmp;
+  }
+  for (size_t e = threadIdx.x; e < mm; e += blockDim.x) q[e] -= p[e];
+  __syncthreads();
+  if (!cta_gesv(m, m, q, m, p, m, sm)) return DEVERR_SINGULAR;
+  for (size_t e = threadIdx.x; e < mm; e += blockDim.x) p[e] *= 2.0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += blockDim.x) p[j + (size_t)j * m] += 1.0;
+  __syncthreads();
+  double* res = p;
+  if (ns == 0 && iodd == 1) {
+    for (size_t e = threadIdx.x; e < mm; e += blockDim.x) p[e] = -p[e];
+    __syncthreads();
+  } else {
+    double* get = p;
+    double* put = q;
+    for (int k = 0; k < ns; ++k) {
+      cta_gemm(m, 1.0, get, m, get, m, put, m);
+      double* tmp = get; get = put; put = tmp;
+    }
+    res = get;
+  }
+  cta_copy(m, res, m, expH, m);
+  return 0;
+}
+
+// ---- SASQ / TAYLOR ----------------------------------------------------------
+PSF_DEVINL int cta_expm_sasq(int n, const double* a, double* e, double* scratch, DenseSmem& sm) {
+  const size_t nn = (size_t)n * n;
+  double* a2 = scratch;
+  double* x = scratch + nn;
+  double* d = scratch + 2 * nn;
+  double* tmp = scratch + 3 * nn;
+  cta_copy(n, a, n, a2, n);
+  const double anorm = cta_norm_inf(n, a2, n, sm);
+  int s = 0;
+  if (anorm != 0.0) {
+    const int ee = (int)(log(anorm) / log(2.0)) + 1;
+    s = ee + 1 > 0 ? ee + 1 : 0;
+  }
+  const double sc = ldexp(1.0, s);
+  for (size_t k = threadIdx.x; k < nn; k += blockDim.x) a2[k] /= sc;
+  __syncthreads();
+  cta_copy(n, a2, n, x, n);
+  double c = 0.5;
+  const int q = 6;
+  for (size_t k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int j = (int)(k / n), i = (int)(k - (size_t)j * n);
+    e[k] = (i == j ? 1.0 : 0.0) + c * a2[k];
+    d[k] = (i == j ? 1.0 : 0.0) - c * a2[k];
+  }
+  __syncthreads();
+  int p = 1;
+  for (int k = 2; k <= q; ++k) {
+    c = c * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
+    cta_gemm(n, 1.0, a2, n, x, n, tmp, n);
+    cta_copy(n, tmp, n, x, n);
+    for (size_t l = threadIdx.x; l < nn; l += blockDim.x) {
+      e[l] = e[l] + c * x[l];
+      d[l] = p ? d[l] + c * x[l] : d[l] - c * x[l];
+    }
+    __syncthreads();
+    p = !p;
+  }
+  if (!cta_fss(n, d, n, e, sm)) return DEVERR_SINGULAR;
+  for (int k = 0; k < s; ++k) {
+    cta_gemm(n, 1.0, e, n, e, n, tmp, n);
+    cta_copy(n, tmp, n, e, n);
+  }
+  return 0;
+}
+
+PSF_DEVINL int cta_expm_taylor(int n, const double* a, double* e, double* scratch, DenseSmem& sm) {
+  const size_t nn = (size_t)n * n;
+  double* f = scratch;
+  double* tmp = scratch + nn;
+  for (size_t k = threadIdx.x; k < nn; k += blockDim.x) e[k] = 0.0;
+  cta_set_identity(n, 1.0, f, n);
+  int k = 1;
+  for (int guard = 0; guard < 100000; ++guard) {
+    int sig = 0;
+    for (size_t l = threadIdx.x; l < nn; l += blockDim.x) {
+      const double r = e[l];
+      const double t = r + f[l];
+      const double tol = 2.220446049250313e-16 * fabs(r);
+      if (tol < fabs(r - t)) sig = 1;
+    }
+    if (!__syncthreads_or(sig)) break;
+    for (size_t l = threadIdx.x; l < nn; l += blockDim.x) e[l] += f[l];
+    __syncthreads();
+    cta_gemm(n, 1.0, a, n, f, n, tmp, n);
+    for (size_t l = threadIdx.x; l < nn; l += blockDim.x) f[l] = tmp[l] / (double)k;
+    __syncthreads();
+    k = k + 1;
+  }
+  return 0;
+}
+
+// ---- CRAM(14,14) --------------------------------------------------------------
+// Published coefficients of the partial-fraction form of the (14,14) uniform
+// rational Chebyshev approximation to exp(-x) on [0, inf), as tabulated at
+// serial/exponential/dnchbv.f:54-69.
+__constant__ double kCramAlpha0 = 0.183216998528140087e-11;
+__constant__ double kCramAlpha[7][2] = {
+    {0.557503973136501826e+02, -0.204295038779771857e+03}, {-0.938666838877006739e+02, 0.912874896775456363e+02},
+    {0.469965415550370835e+02, -0.116167609985818103e+02}, {-0.961424200626061065e+01, -0.264195613880262669e+01},
+    {0.752722063978321642e+00, 0.670367365566377770e+00},  {-0.188781253158648576e-01, -0.343696176445802414e-01},
+    {0.143086431411801849e-03, 0.287221133228814096e-03}};
+__constant__ double kCramTheta[7][2] = {
+    {-0.562314417475317895e+01, 0.119406921611247440e+01}, {-0.508934679728216110e+01, 0.358882439228376881e+01},
+    {-0.399337136365302569e+01, 0.600483209099604664e+01}, {-0.226978543095856366e+01, 0.846173881758693369e+01},
+    {0.208756929753827868e+00, 0.109912615662209418e+02},  {0.370327340957595652e+01, 0.136563731924991884e+02},
+    {0.889777151877331107e+01, 0.166309842834712071e+02}};
+
+typedef cuDoubleComplex zc;
+PSF_DEVINL zc zmk(double r, double i) { return make_cuDoubleComplex(r, i); }
+PSF_DEVINL zc zadd(zc a, zc b) { return cuCadd(a, b); }
+PSF_DEVINL zc zsub(zc a, zc b) { return cuCsub(a, b); }
+PSF_DEVINL zc zmul(zc a, zc b) { return cuCmul(a, b); }
+PSF_DEVINL zc zdiv(zc a, zc b) { return cuCdiv(a, b); }
+PSF_DEVINL double zabs(zc a) { return hypot(cuCreal(a), cuCimag(a)); }
+
+// Accumulate y = alpha0 * x + sum_p Re(alpha_p * sol_p) (dnchbv.f:73-113).
+PSF_DEVINL void cram_accumulate(int m, const double* x, const zc* sols, double* y) {
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    double acc = x[j] * kCramAlpha0;
+    for (int p = 0; p < 7; ++p) {
+      const zc a = zmk(kCramAlpha[p][0], kCramAlpha[p][1]);
+      acc = acc + cuCreal(zmul(a, sols[(size_t)p * m + j]));
+    }
+    y[j] = acc;
+  }
+  __syncthreads();
+}
+
+// CHBHES: one warp per pole, Hessenberg elimination with adjacent-row pivoting.
+PSF_DEVINL void cta_cram_hessenberg(int m, double t, const double* H, int ldh, const double* x, double* y,
+                                    double* scratch) {
+  zc* sols = (zc*)scratch;                      // 7 * m
+  zc* work = (zc*)(scratch + 2 * 7 * (size_t)m);  // 7 * m * m
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  for (int p = warp; p < 7; p += nwarps) {
+    zc* wh = work + (size_t)p * m * m;
+    zc* wy = sols + (size_t)p * m;
+    const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
+    for (int j = 0; j < m; ++j) {
+      const int ilim = (j + 2 < m) ? j + 2 : m;
+      for (int i = lane; i < m; i += 32) {
+        zc v = zmk(0.0, 0.0);
+        if (i < ilim) v = zmk(-t * H[i + (size_t)j * ldh], 0.0);
+        if (i == j) v = zsub(v, theta);
+        wh[i + (size_t)j * m] = v;
+      }
+    }
+    for (int j = lane; j < m; j += 32) wy[j] = zmk(x[j], 0.0);
+    __syncwarp();
+    for (int i = 0; i < m - 1; ++i) {
+      const bool swp = zabs(wh[i + (size_t)i * m]) < zabs(wh[i + 1 + (size_t)i * m]);
+      if (swp) {
+        for (int j = i + lane; j < m; j += 32) {
+          const zc a = wh[i + (size_t)j * m];
+          wh[i + (size_t)j * m] = wh[i + 1 + (size_t)j * m];
+          wh[i + 1 + (size_t)j * m] = a;
+        }
+        if (lane == 0) { const zc a = wy[i]; wy[i] = wy[i + 1]; wy[i + 1] = a; }
+      }
+      __syncwarp();
+      const zc tmpc = zdiv(wh[i + 1 + (size_t)i * m], wh[i + (size_t)i * m]);
+      for (int j = i + 1 + lane; j < m; j += 32)
+        wh[i + 1 + (size_t)j * m] = zsub(wh[i + 1 + (size_t)j * m], zmul(tmpc, wh[i + (size_t)j * m]));
+      if (lane == 0) wy[i + 1] = zsub(wy[i + 1], zmul(tmpc, wy[i]));
+      __syncwarp();
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      zc part = zmk(0.0, 0.0);
+      for (int j = i + 1 + lane; j < m; j += 32) part = zadd(part, zmul(wh[i + (size_t)j * m], wy[j]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        part.x += __shfl_xor_sync(0xffffffffu, part.x, o);
+        part.y += __shfl_xor_sync(0xffffffffu, part.y, o);
+      }
+      if (lane == 0) wy[i] = zdiv(zsub(wy[i], part), wh[i + (size_t)i * m]);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  cram_accumulate(m, x, sols, y);
+}
+
+// CHBSYM / CHBGEN on a general matrix: one warp per pole, complex GEPP.
+PSF_DEVINL bool cta_cram_full(int m, double t, const double* H, int ldh, const double* x, double* y,
+                              double* scratch) {
+  zc* sols = (zc*)scratch;
+  zc* work = (zc*)(scratch + 2 * 7 * (size_t)m);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  int bad = 0;
+  for (int p = warp; p < 7; p += nwarps) {
+    zc* a = work + (size_t)p * m * m;
+    zc* b = sols + (size_t)p * m;
+    const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
+    for (int j = 0; j < m; ++j)
+      for (int i = lane; i < m; i += 32) {
+        zc v = zmk(-t * H[i + (size_t)j * ldh], 0.0);
+        if (i == j) v = zsub(v, theta);
+        a[i + (size_t)j * m] = v;
+      }
+    for (int j = lane; j < m; j += 32) b[j] = zmk(x[j], 0.0);
+    __syncwarp();
+    for (int k = 0; k < m && !bad; ++k) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + lane; i < m; i += 32) {
+        const double v = zabs(a[i + (size_t)k * m]);
+        if (v > best) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (best == 0.0) { bad = 1; break; }
+      if (bi != k) {
+        for (int j = lane; j < m; j += 32) {
+          const zc tt = a[k + (size_t)j * m]; a[k + (size_t)j * m] = a[bi + (size_t)j * m]; a[bi + (size_t)j * m] = tt;
+        }
+        if (lane == 0) { const zc tt = b[k]; b[k] = b[bi]; b[bi] = tt; }
+        __syncwarp();
+      }
+      const zc piv = a[k + (size_t)k * m];
+      for (int i = k + 1 + lane; i < m; i += 32) {
+        const zc l = zdiv(a[i + (size_t)k * m], piv);
+        for (int j = k + 1; j < m; ++j) a[i + (size_t)j * m] = zsub(a[i + (size_t)j * m], zmul(l, a[k + (size_t)j * m]));
+        b[i] = zsub(b[i], zmul(l, b[k]));
+      }
+      __syncwarp();
+    }
+    if (!bad) {
+      for (int i = m - 1; i >= 0; --i) {
+        zc part = zmk(0.0, 0.0);
+        for (int j = i + 1 + lane; j < m; j += 32) part = zadd(part, zmul(a[i + (size_t)j * m], b[j]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          part.x += __shfl_xor_sync(0xffffffffu, part.x, o);
+          part.y += __shfl_xor_sync(0xffffffffu, part.y, o);
+        }
+        if (lane == 0) b[i] = zdiv(zsub(b[i], part), a[i + (size_t)i * m]);
+        __syncwarp();
+      }
+    }
+  }
+  if (__syncthreads_or(bad)) return false;
+  cram_accumulate(m, x, sols, y);
+  return true;
+}
+
+// CHB* on a symmetric tridiagonal matrix (the Lanczos T): banded GEPP, one
+// thread per pole.  Same pivots and eliminations as the full GEPP restricted
+// to the nonzeros (a row swap fills one extra super-diagonal).
+PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, const double* x, double* y,
+                                 double* scratch) {
+  zc* sols = (zc*)scratch;                      // 7*m
+  zc* band = (zc*)(scratch + 2 * 7 * (size_t)m);  // 7 * 4 * m : d, du, du2, dl
+  int bad = 0;
+  if (threadIdx.x < 7) {
+    const int p = threadIdx.x;
+    const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
+    zc* d = band + (size_t)p * 4 * m;
+    zc* du = d + m;
+    zc* du2 = du + m;
+    zc* dl = du2 + m;
+    zc* b = sols + (size_t)p * m;
+    for (int i = 0; i < m; ++i) {
+      d[i] = zsub(zmk(-t * H[i + (size_t)i * ldh], 0.0), theta);
+      du[i] = (i + 1 < m) ? zmk(-t * H[i + (size_t)(i + 1) * ldh], 0.0) : zmk(0.0, 0.0);
+      dl[i] = (i + 1 < m) ? zmk(-t * H[i + 1 + (size_t)i * ldh], 0.0) : zmk(0.0, 0.0);
+      du2[i] = zmk(0.0, 0.0);
+      b[i] = zmk(x[i], 0.0);
+    }
+    for (int k = 0; k < m - 1 && !bad; ++k) {
+      if (zabs(d[k]) < zabs(dl[k])) {  // swap rows k, k+1 (first max rule)
+        zc tt;
+        tt = d[k]; d[k] = dl[k]; dl[k] = tt;
+        tt = du[k]; du[k] = d[k + 1]; d[k + 1] = tt;
+        if (k + 1 < m - 1) { tt = du2[k]; du2[k] = du[k + 1]; du[k + 1] = tt; }
+        tt = b[k]; b[k] = b[k + 1]; b[k + 1] = tt;
+      }
+      if (zabs(d[k]) == 0.0) { bad = 1; break; }
+      const zc l = zdiv(dl[k], d[k]);
+      d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
+      if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
+      b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+    }
+    if (!bad && zabs(d[m - 1]) == 0.0) bad = 1;
+    if (!bad) {
+      for (int i = m - 1; i >= 0; --i) {
+        zc s = b[i];
+        if (i + 1 < m) s = zsub(s, zmul(du[i], b[i + 1]));
+        if (i + 2 < m) s = zsub(s, zmul(du2[i], b[i + 2]));
+        b[i] = zdiv(s, d[i]);
+      }
+    }
+  }
+  if (__syncthreads_or(bad)) return false;
+  cram_accumulate(m, x, sols, y);
+  return true;
+}
+
+// ---- symmetric eigendecomposition (parallel cyclic Jacobi) -----------------
+// A (upper triangle read) -> eigenvalues w, eigenvectors V (columns).
+PSF_DEVINL void cta_sym_eig(int m, const double* A, int lda, double* w, double* V, double* scratch,
+                            DenseSmem& sm) {
+  double* S = scratch;  // m x m working copy
+  int* pairs = (int*)(scratch + (size_t)m * m);
+  double* cs = scratch + (size_t)m * m + m + 2;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int j = t / m, i = t - j * m;
+    S[t] = (i <= j) ? A[i + (size_t)j * lda] : A[j + (size_t)i * lda];
+    V[t] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int mm = (m + 1) & ~1;
+  const int np = mm / 2;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+      const int j = t / m, i = t - j * m;
+      const double x2 = S[t] * S[t];
+      tot += x2;
+      if (i != j) off += x2;
+    }
+    off = block_sum(off, sm.red);
+    tot = block_sum(tot, sm.red);
+    if (off == 0.0 || off <= 1e-32 * tot) break;
+    for (int round = 0; round < mm - 1; ++round) {
+      for (int k = threadIdx.x; k < np; k += blockDim.x) {
+        int p, q;
+        if (k == 0) { p = 0; q = (round % (mm - 1)) + 1; }
+        else {
+          p = ((k + round) % (mm - 1)) + 1;
+          q = ((mm - 1 - k + round) % (mm - 1)) + 1;
+        }
+        if (p > q) { const int tt = p; p = q; q = tt; }
+        double c = 1.0, s = 0.0;
+        if (q < m) {
+          const double apq = S[p + (size_t)q * m];
+          if (apq != 0.0) {
+            const double app = S[p + (size_t)p * m], aqq = S[q + (size_t)q * m];
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(tt * tt + 1.0);
+            s = tt * c;
+          }
+        }
+        pairs[2 * k] = p;
+        pairs[2 * k + 1] = q;
+        cs[2 * k] = c;
+        cs[2 * k + 1] = s;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < np * m; t += blockDim.x) {  // columns: S <- S J, V <- V J
+        const int k = t / m, i = t - k * m;
+        const int p = pairs[2 * k], q = pairs[2 * k + 1];
+        if (q >= m) continue;
+        const double c = cs[2 * k], s = cs[2 * k + 1];
+        if (s == 0.0) continue;
+        const double sp = S[i + (size_t)p * m], sq = S[i + (size_t)q * m];
+        S[i + (size_t)p * m] = c * sp - s * sq;
+        S[i + (size_t)q * m] = s * sp + c * sq;
+        const double vp = V[i + (size_t)p * m], vq = V[i + (size_t)q * m];
+        V[i + (size_t)p * m] = c * vp - s * vq;
+        V[i + (size_t)q * m] = s * vp + c * vq;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < np * m; t += blockDim.x) {  // rows: S <- J^T S
+        const int k = t / m, j = t - k * m;
+        const int p = pairs[2 * k], q = pairs[2 * k + 1];
+        if (q >= m) continue;
+        const double c = cs[2 * k], s = cs[2 * k + 1];
+        if (s == 0.0) continue;
+        const double sp = S[p + (size_t)j * m], sq = S[q + (size_t)j * m];
+        S[p + (size_t)j * m] = c * sp - s * sq;
+        S[q + (size_t)j * m] = s * sp + c * sq;
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = S[i + (size_t)i * m];
+  __syncthreads();
+}
+
+// ---- dispatcher -------------------------------------------------------------
+// y = f(fp.scaling * H) x for the function/variant in fp, H m x m (ldh).
+// `tridiag` tells that H is symmetric tridiagonal (Lanczos).  x and y must not
+// alias scratch.  USERF is not handled here (its f lives on the host).
+// Returns 0 or DEVERR_* flags.
+PSF_DEVINL int fh_apply_cta(const FunParams& fp, int m, const double* H, int ldh, const double* x, double* y,
+                            double* scratch, bool tridiag, DenseSmem& sm) {
+  if (m < 1) return DEVERR_BADSIZE;
+  const size_t mm = (size_t)m * m;
+  if (fp.fname == FN_EXP) {
+    switch (fp.variant) {
+      case VAR_GENPADE: {
+        double* E = scratch + 4 * mm;
+        const int rc = cta_dgpadm(fp.padedegree, m, fp.scaling, H, ldh, E, scratch, sm);
+        if (rc) return rc;
+        cta_gemv(m, E, m, x, y);
+        return 0;
+      }
+      case VAR_SASQ:
+      case VAR_TAYLOR: {
+        double* SA = scratch + 5 * mm;
+        double* E = scratch + 4 * mm;
+        for (size_t t = threadIdx.x; t < mm; t += blockDim.x) {
+          const int j = (int)(t / m), i = (int)(t - (size_t)j * m);
+          SA[t] = fp.scaling * H[i + (size_t)j * ldh];
+        }
+        __syncthreads();
+        const int rc = (fp.variant == VAR_SASQ) ? cta_expm_sasq(m, SA, E, scratch, sm)
+                                                : cta_expm_taylor(m, SA, E, scratch, sm);
+        if (rc) return rc;
+        cta_gemv(m, E, m, x, y);
+        return 0;
+      }
+      case VAR_CHBHES:
+        cta_cram_hessenberg(m, fp.scaling, H, ldh, x, y, scratch);
+        return 0;
+      case VAR_CHBGEN:
+      case VAR_CHBSYM: {
+        const bool ok = tridiag ? cta_cram_tridiag(m, fp.scaling, H, ldh, x, y, scratch)
+                                : cta_cram_full(m, fp.scaling, H, ldh, x, y, scratch);
+        return ok ? 0 : DEVERR_SINGULAR;
+      }
+      default:
+        return DEVERR_FUNC;
+    }
+  } else if (fp.fname == FN_PHI) {
+    const int k = fp.phiorder;
+    if (k < 1) return DEVERR_FUNC;
+    const int M = m + k;
+    const size_t MM = (size_t)M * M;
+    double* aug = scratch + 5 * MM;
+    double* E = scratch + 4 * MM;
+    for (size_t t = threadIdx.x; t < MM; t += blockDim.x) {
+      const int j = (int)(t / M), i = (int)(t - (size_t)j * M);
+      double v = 0.0;
+      if (i < m && j < m) v = fp.scaling * H[i + (size_t)j * ldh];
+      else if (i < m && j == m) v = x[i];
+      else if (i >= m && j == i + 1) v = 1.0;
+      aug[t] = v;
+    }
+    __syncthreads();
+    const int rc = cta_dgpadm(fp.padedegree, M, 1.0, aug, M, E, scratch, sm);
+    if (rc) return rc;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) y[i] = E[i + (size_t)(M - 1) * M];
+    __syncthreads();
+    return 0;
+  }
+  return DEVERR_FUNC;
+}
+
+}  // namespace psf

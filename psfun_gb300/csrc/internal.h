@@ -1,0 +1,124 @@
+// internal.h -- host-side handle types and helpers of libpsfun_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/psfun_gb300.h"
+#include "dense.cuh"
+#include "spmv.cuh"
+
+namespace psf {
+
+// Library-wide state.
+cudaStream_t stream();
+void set_last_error(const std::string& msg);
+void count_launch(int n = 1);
+int sm_count();
+
+// CUDA call -> status code, recording the message.
+#define PSF_CUDA(call)                                                          \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      ::psf::set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+      return PSFUN_ERR_CUDA;                                                    \
+    }                                                                           \
+  } while (0)
+
+#define PSF_TRY(expr)        \
+  do {                               \
+    int rc_ = (expr);                \
+    if (rc_ != PSFUN_SUCCESS) return rc_; \
+  } while (0)
+
+// Device buffer that grows on demand (never shrinks until freed).
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need);
+  void release();
+  template <class T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Control block of one Krylov solve, in device memory.
+struct KCtrl {
+  int done;       // stop enqueued work
+  int conv;       // estimate below eps
+  int breakdown;  // Lanczos |beta| < 1e-16 / Arnoldi h(i,i-1) == 0
+  int itx;        // iterations (reference `itx`)
+  int yk_len;
+  int nterms;
+  int err;        // DEVERR_* flags
+  int info;       // PSBLAS-style status
+  unsigned bar_count;
+  unsigned bar_gen;
+  unsigned red_counter;
+  unsigned red_counter2;
+  double beta0;   // rs(1) = ||x||
+  double errnum;
+  double errden;
+  double c1, c2;  // Lanczos update coefficients
+  double derr;
+};
+
+}  // namespace psf
+
+struct psfun_csr {
+  int64_t n = 0, nnz = 0;
+  int32_t* irp = nullptr;
+  int32_t* ja = nullptr;
+  double* val = nullptr;
+  int32_t* tile_row = nullptr;
+  int32_t ntiles = 0;
+  double norm_inf = 0.0;
+  double* diag_inv = nullptr;  // Jacobi preconditioner (lazy)
+  std::vector<double> h_diag;  // diagonal of A (host copy, for DIAG)
+  psf::CsrDev dev() const {
+    psf::CsrDev d;
+    d.n = n; d.nnz = nnz; d.irp = irp; d.ja = ja; d.val = val; d.tile_row = tile_row; d.ntiles = ntiles;
+    return d;
+  }
+};
+
+struct psfun_serial {
+  char fname[21];
+  char variant[21];
+  double scaling = 1.0;
+  int padedegree = 6;
+  int phiorder = 1;
+  psfun_userf f_ptr = nullptr;
+};
+
+struct psfun_krylov {
+  char kname[21];
+  char kmethd[21];
+  double tau = 0.0;
+  int itmax = 200, itrace = 0, istopc = 1, irst = 10;
+  int keeplast = 0;
+  // cached workspace (never per call)
+  psf::DevBuf V, u, small, scratch, partials, ctrl, xy;
+  int64_t ldv = 0;
+  int nl_cap = 0;
+};
+
+namespace psf {
+// Parses fname / variant with the reference's case-sensitive, blank-padded
+// comparison.  Returns false if the pair is not a valid selector.
+bool parse_fun(const psfun_serial* fun, FunParams* fp);
+bool fstr_eq(const char* s, const char* lit);
+void set_fstr(char* dst, const char* src);  // Fortran character(len=20) assignment
+
+int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x, double eps,
+                        int itmax, int itrace, int istop, int* iter, double* err, double* res, int res_cap,
+                        int* res_len);
+int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev, const double* x_dev);
+int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
+              int istop, int* iter, double* err);
+int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
+                      const double* x, double* y, double eps, int itmax, int* iter, double* err);
+int userf_eval(psfun_userf f, double scaling, const double* w_dev, double* fv_dev, int m);
+}  // namespace psf

@@ -1,0 +1,948 @@
+// krylov.cu -- Arnoldi and Lanczos f(A)x on one GB300.
+//
+// Restates psfun_d_arnoldi (krylov/polynomial/psfun_d_arnoldi.f90:98-343) and
+// psfun_d_lanczos (krylov/polynomial/psfun_d_lanczos.f90:97-391) with the
+// control flow, stopping rule and outputs of the reference.  Device layout:
+//
+//   V    (nl+1) basis slots of ldv doubles (ldv = n rounded up to 32, so every
+//        slot starts on a 256-byte boundary).  Slot k holds W_k, the basis
+//        vector before normalisation; its scale s_k = 1/||W_k|| is kept apart
+//        and folded into the scalars that use it, so no pass over HBM is spent
+//        on normalising (v_k = s_k W_k).
+//   H    (nl+1)^2 column-major, the reference's h / t array.
+//   ctrl one KCtrl block: iteration count, flags, reduction counters.
+//
+// Per Lanczos step two kernels: SpMV with the fused dot (alpha), then the
+// three-term update with the fused norm (beta).  Per Arnoldi step: the SpMV,
+// then one cooperative kernel that runs modified Gram-Schmidt in one pass over
+// the basis: each CTA keeps its rows of w, and per basis vector performs the
+// update of the previous coefficient and the dot of the next one in a single
+// sweep, separated by a bounded grid barrier.  Scalars are finalised on the
+// device, so no host round trip sits inside the loop; the per-step error
+// estimate (istop = 1) is a one-CTA kernel in the same stream.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace psf {
+
+struct KState {
+  int64_t n, ldv;
+  int nl, ldh;
+  double* V;
+  double* u;
+  double* H;
+  double* s;
+  double* rs;
+  double* yk;
+  double* e1;
+  double* coef;
+  double* partials;
+  KCtrl* ctrl;
+  double* fscratch;
+  double* ework;  // USERF: eigenvalues / f values / eigenvectors
+  volatile int* host_flag;  // mapped: [0] done, [1] last finished step
+};
+
+#define HAT(st, i, j) (st).H[((i)-1) + (size_t)((j)-1) * (st).ldh]
+#define WAT(st, k) ((st).V + (size_t)((k)-1) * (st).ldv)
+
+constexpr int kVecThreads = 256;
+constexpr int kDenseThreads = 256;
+constexpr int kMgsThreads = 1024;
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// W_1 = x ; beta0 = ||x|| ; s_1 = 1/beta0  (psfun_d_arnoldi.f90:183-197)
+__global__ void __launch_bounds__(kVecThreads) k_init(KState st, const double* __restrict__ x) {
+  __shared__ double red[32];
+  double* w1 = WAT(st, 1);
+  double acc = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < st.n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[r];
+    w1[r] = v;
+    acc = fma(v, v, acc);
+  }
+  acc = block_sum(acc, red);
+  KCtrl* c = st.ctrl;
+  last_block_reduce(acc, st.partials, &c->red_counter, red, [&](double tot) {
+    const double b = sqrt(tot);
+    c->beta0 = b;
+    st.rs[0] = b;
+    if (b == 0.0) {
+      c->done = 1;
+      c->itx = 0;
+    } else {
+      st.s[1] = 1.0 / b;
+    }
+  });
+}
+
+// Lanczos: u = A v_i and alpha_i = u . v_i   (psfun_d_lanczos.f90:198-204, :239-246)
+__global__ void __launch_bounds__(kSpmvThreads) k_lz_spmv(KState st, CsrDev A, int i) {
+  __shared__ SpmvSmem sm;
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  if (c->breakdown) {  // |beta_i| < 1e-16 found by the previous update: exit at the top of iteration i
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      c->done = 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+    return;
+  }
+  spmv_smem_init(sm);
+  const double sc = st.s[i];
+  const double* wi = WAT(st, i);
+  EpiScaleDot epi{sc, st.u, wi, 0.0};
+  spmv_tiles(A, wi, epi, sm, &c->err, blockIdx.x, gridDim.x);
+  const double acc = block_sum(epi.acc, sm.red);
+  last_block_reduce(acc, st.partials, &c->red_counter, sm.red, [&](double tot) {
+    const double alpha = sc * tot;
+    HAT(st, i, i) = alpha;
+    c->c1 = alpha * sc;
+    c->c2 = (i >= 2) ? HAT(st, i - 1, i) * st.s[i - 1] : 0.0;
+    if (i >= 2) c->itx = i - 1;
+  });
+}
+
+// Lanczos: w = u - alpha_i v_i - beta_i v_{i-1}, beta_{i+1} = ||w||
+// (psfun_d_lanczos.f90:212, :221-230, :254-266)
+__global__ void __launch_bounds__(kVecThreads) k_lz_update(KState st, int i) {
+  __shared__ double red[32];
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  const double c1 = c->c1, c2 = c->c2;
+  const double* __restrict__ u = st.u;
+  const double* __restrict__ wi = WAT(st, i);
+  const double* __restrict__ wm = (i >= 2) ? WAT(st, i - 1) : wi;
+  double* __restrict__ wo = WAT(st, i + 1);
+  double acc = 0.0;
+  const int64_t npair = st.n >> 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npair; p += stride) {
+    const double2 uu = reinterpret_cast<const double2*>(u)[p];
+    const double2 a = reinterpret_cast<const double2*>(wi)[p];
+    const double2 b = reinterpret_cast<const double2*>(wm)[p];
+    double2 w;
+    w.x = fma(-c2, b.x, fma(-c1, a.x, uu.x));
+    w.y = fma(-c2, b.y, fma(-c1, a.y, uu.y));
+    reinterpret_cast<double2*>(wo)[p] = w;
+    acc = fma(w.x, w.x, acc);
+    acc = fma(w.y, w.y, acc);
+  }
+  if ((st.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int64_t r = st.n - 1;
+    const double w = fma(-c2, wm[r], fma(-c1, wi[r], u[r]));
+    wo[r] = w;
+    acc = fma(w, w, acc);
+  }
+  acc = block_sum(acc, red);
+  last_block_reduce(acc, st.partials, &c->red_counter, red, [&](double tot) {
+    const double b = sqrt(tot);
+    HAT(st, i, i + 1) = b;
+    HAT(st, i + 1, i) = b;
+    st.s[i + 1] = 1.0 / b;
+    if (i + 1 <= st.nl && fabs(b) < 1e-16) {  // checked at the top of iteration i+1
+      c->breakdown = 1;
+      c->itx = i;
+    }
+    if (st.host_flag) st.host_flag[1] = i;
+  });
+}
+
+// Arnoldi: w = scaling * A v_{i-1} into slot i   (psfun_d_arnoldi.f90:202)
+__global__ void __launch_bounds__(kSpmvThreads) k_ar_spmv(KState st, CsrDev A, int i, double scaling) {
+  __shared__ SpmvSmem sm;
+  KCtrl* c = st.ctrl;
+  if (c->done || c->breakdown) return;
+  spmv_smem_init(sm);
+  EpiAxpby epi{scaling * st.s[i - 1], 0.0, WAT(st, i)};
+  spmv_tiles(A, WAT(st, i - 1), epi, sm, &c->err, blockIdx.x, gridDim.x);
+}
+
+// Arnoldi: modified Gram-Schmidt of slot i against slots 1..i-1, one pass over
+// the basis (psfun_d_arnoldi.f90:210-217).  Cooperative launch.
+__global__ void __launch_bounds__(kMgsThreads) k_ar_mgs(KState st, int i) {
+  __shared__ double red[32];
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  if (c->breakdown) {  // the previous step found h(i-1,i-2) == 0 (istop = 2)
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->done = 1;
+    return;
+  }
+  const int G = gridDim.x;
+  const int b = blockIdx.x;
+  int64_t chunk = (st.n + G - 1) / G;
+  chunk = (chunk + 1) & ~(int64_t)1;
+  const int64_t r0 = (int64_t)b * chunk;
+  const int64_t r1 = (r0 + chunk < st.n) ? r0 + chunk : st.n;
+  double* __restrict__ w = WAT(st, i);
+  double* part = st.partials;
+  // dot with v_1
+  {
+    const double* __restrict__ wk = WAT(st, 1);
+    double acc = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) acc = fma(wk[r], w[r], acc);
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) part[b] = acc;
+  }
+  if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+  for (int k = 1; k <= i - 1; ++k) {
+    const double tot = block_sum_array(part + (size_t)((k - 1) & 1) * G, G, red);
+    const double h = st.s[k] * tot;  // h(k,i-1) = v_k . w
+    if (b == 0 && threadIdx.x == 0) HAT(st, k, i - 1) = h;
+    const double cc = h * st.s[k];
+    const double* __restrict__ wk = WAT(st, k);
+    double acc = 0.0;
+    if (k + 1 <= i - 1) {
+      const double* __restrict__ wn = WAT(st, k + 1);
+      for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const double v = fma(-cc, wk[r], w[r]);
+        w[r] = v;
+        acc = fma(wn[r], v, acc);
+      }
+    } else {
+      for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const double v = fma(-cc, wk[r], w[r]);
+        w[r] = v;
+        acc = fma(v, v, acc);
+      }
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) part[(size_t)(k & 1) * G + b] = acc;
+    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+  }
+  const double tot = block_sum_array(part + (size_t)((i - 1) & 1) * G, G, red);
+  if (b == 0 && threadIdx.x == 0) {
+    const double beta = sqrt(tot);
+    HAT(st, i, i - 1) = beta;
+    st.s[i] = 1.0 / beta;
+    c->itx = i - 1;
+    if (beta == 0.0) c->breakdown = 1;
+    if (st.host_flag) st.host_flag[1] = i;
+  }
+}
+
+// A posteriori estimate of iteration i (psfun_d_arnoldi.f90:222-276,
+// psfun_d_lanczos.f90:271-324): yk = f(H(1:i-1,1:i-1)) e1,
+// rs(i) = beta0 * h(i,i-1) * |yk(i-1)| / ||yk||; stop when rs(i) < eps.
+__device__ void estimate_tail(KState& st, int i, double eps, double* red) {
+  KCtrl* c = st.ctrl;
+  const int m = i - 1;
+  double ss = 0.0;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) ss = fma(st.yk[j], st.yk[j], ss);
+  ss = block_sum(ss, red);
+  if (threadIdx.x == 0) {
+    const double errnum = c->beta0 * HAT(st, i, i - 1) * fabs(st.yk[m - 1]);
+    const double errden = sqrt(ss);
+    const double r = errnum / errden;
+    st.rs[i - 1] = r;
+    c->errnum = errnum;
+    c->errden = errden;
+    if (r < eps) {
+      c->done = 1;
+      c->conv = 1;
+      c->yk_len = m;
+      c->itx = i - 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams fp, int i, double eps, int tridiag) {
+  __shared__ DenseSmem sm;
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  const int m = i - 1;
+  const int rc = fh_apply_cta(fp, m, st.H, st.ldh, st.e1, st.yk, st.fscratch, tridiag != 0, sm);
+  if (rc) {
+    if (threadIdx.x == 0) {
+      atomicOr(&c->err, rc);
+      c->info = PSFUN_ERR_FROM_SUBROUTINE_NON;
+      c->done = 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+    return;
+  }
+  estimate_tail(st, i, eps, sm.red);
+}
+
+// USERF estimate tail: yk was produced by the host-assisted path.
+__global__ void k_estimate_tail(KState st, int i, double eps) {
+  __shared__ double red[32];
+  if (st.ctrl->done) return;
+  estimate_tail(st, i, eps, red);
+}
+
+// Final f(H) e1 when no estimate converged, and the assembly coefficients
+// (psfun_d_arnoldi.f90:282-329, psfun_d_lanczos.f90:330-377).
+// mode: 0 = compute f on the device, 1 = yk already computed (USERF).
+__device__ int final_dim(const KCtrl* c, int arnoldi) {
+  return (arnoldi && c->breakdown) ? c->itx : c->itx - 1;
+}
+
+__global__ void __launch_bounds__(kDenseThreads) k_final(KState st, FunParams fp, int tridiag, int keeplast,
+                                                         int arnoldi, int mode) {
+  __shared__ DenseSmem sm;
+  KCtrl* c = st.ctrl;
+  if (c->info != 0) return;
+  if (c->beta0 == 0.0) {
+    if (threadIdx.x == 0) { c->nterms = 0; c->itx = 0; c->derr = 0.0; }
+    return;
+  }
+  const int conv = c->conv;
+  const int itx = c->itx;
+  int yk_len;
+  if (!conv) {
+    const int m = final_dim(c, arnoldi);
+    if (m < 1) {
+      if (threadIdx.x == 0) c->info = PSFUN_ERR_FROM_SUBROUTINE_NON;
+      return;
+    }
+    if (mode == 0) {
+      const int rc = fh_apply_cta(fp, m, st.H, st.ldh, st.e1, st.yk, st.fscratch, tridiag != 0, sm);
+      if (rc) {
+        if (threadIdx.x == 0) { atomicOr(&c->err, rc); c->info = PSFUN_ERR_FROM_SUBROUTINE_NON; }
+        return;
+      }
+    }
+    yk_len = m;
+  } else {
+    yk_len = c->yk_len;
+  }
+  int nterms = (conv && !keeplast) ? (itx - 1 > 1 ? itx - 1 : 1) : yk_len;
+  if (nterms > yk_len) nterms = yk_len;
+  for (int j = threadIdx.x; j < nterms; j += blockDim.x) st.coef[j] = c->beta0 * st.yk[j] * st.s[j + 1];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c->yk_len = yk_len;
+    c->nterms = nterms;
+    c->derr = (c->errden > 0.0) ? c->errnum / c->errden : c->errnum;
+  }
+}
+
+// y = sum_j coef_j W_j  (the assembly y = rs(1) * sum yk(j) v(j))
+__global__ void __launch_bounds__(kVecThreads) k_recombine(KState st, double* __restrict__ y) {
+  const KCtrl* c = st.ctrl;
+  const int nterms = (c->info == 0) ? c->nterms : 0;
+  const double* __restrict__ coef = st.coef;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < st.n; r += stride) {
+    double acc = 0.0;
+    const double* v = st.V + r;
+    int j = 0;
+    for (; j + 4 <= nterms; j += 4) {
+      const double a0 = v[(size_t)j * st.ldv], a1 = v[(size_t)(j + 1) * st.ldv];
+      const double a2 = v[(size_t)(j + 2) * st.ldv], a3 = v[(size_t)(j + 3) * st.ldv];
+      acc = fma(coef[j], a0, acc);
+      acc = fma(coef[j + 1], a1, acc);
+      acc = fma(coef[j + 2], a2, acc);
+      acc = fma(coef[j + 3], a3, acc);
+    }
+    for (; j < nterms; ++j) acc = fma(coef[j], v[(size_t)j * st.ldv], acc);
+    y[r] = acc;
+  }
+}
+
+// ---- USERF/SYM: eigendecomposition on the device, f(lambda) on the host ----
+__global__ void __launch_bounds__(kDenseThreads) k_symeig(int m, const double* H, int ldh, double* w, double* V,
+                                                          double* work) {
+  __shared__ DenseSmem sm;
+  cta_sym_eig(m, H, ldh, w, V, work, sm);
+}
+
+// y = V diag(fv) V^T x  (psfun_d_serial_mod.F90:473-477)
+__global__ void __launch_bounds__(kDenseThreads) k_userf_apply(int m, const double* V, const double* fv,
+                                                               const double* x, double* y, double* t) {
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s = fma(V[k + (size_t)i * m], x[k], s);
+    t[i] = fv[i] * s;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s = fma(V[i + (size_t)k * m], t[k], s);
+    y[i] = s;
+  }
+}
+
+// y = f(scaling*H) x with the host callback.  `work` holds >= 4 m^2 + 4 m doubles.
+static int userf_apply(psfun_userf f, double scaling, int m, const double* H, int ldh, const double* x, double* y,
+                       double* work) {
+  double* w = work;
+  double* fv = work + m;
+  double* t = work + 2 * m;
+  double* V = work + 3 * m;
+  double* scr = V + (size_t)m * m;
+  cudaStream_t s = stream();
+  k_symeig<<<1, kDenseThreads, 0, s>>>(m, H, ldh, w, V, scr);
+  count_launch();
+  PSF_CUDA(cudaGetLastError());
+  std::vector<double> hw(m), hf(m);
+  PSF_CUDA(cudaMemcpyAsync(hw.data(), w, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < m; ++i) hf[i] = f(scaling * hw[i], 0);
+  PSF_CUDA(cudaMemcpyAsync(fv, hf.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  k_userf_apply<<<1, kDenseThreads, 0, s>>>(m, V, fv, x, y, t);
+  count_launch();
+  PSF_CUDA(cudaGetLastError());
+  PSF_CUDA(cudaStreamSynchronize(s));
+  return PSFUN_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+
+static int upper_trim(const char* s, char* out, int cap) {
+  int n = 0;
+  for (; s[n] && n < cap - 1; ++n) out[n] = (char)toupper((unsigned char)s[n]);
+  while (n > 0 && out[n - 1] == ' ') --n;
+  out[n] = 0;
+  return n;
+}
+
+static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder) {
+  const int64_t ldv = (n + 31) & ~(int64_t)31;
+  if (meth->ldv != ldv || meth->nl_cap < nl) {
+    meth->V.release();
+    meth->u.release();
+    meth->ldv = ldv;
+    meth->nl_cap = nl;
+  }
+  const size_t vbytes = sizeof(double) * (size_t)(nl + 1) * ldv;
+  if (meth->V.bytes < vbytes) {
+    PSF_TRY(meth->V.ensure(vbytes));
+    PSF_CUDA(cudaMemsetAsync(meth->V.ptr, 0, vbytes, stream()));
+  }
+  if (meth->u.bytes < sizeof(double) * ldv) {
+    PSF_TRY(meth->u.ensure(sizeof(double) * ldv));
+    PSF_CUDA(cudaMemsetAsync(meth->u.ptr, 0, sizeof(double) * ldv, stream()));
+  }
+  const size_t ldh = (size_t)nl + 1;
+  const size_t small = ldh * ldh + 6 * (ldh + 2) + 64;
+  PSF_TRY(meth->small.ensure(sizeof(double) * small));
+  const size_t fs = fh_scratch_doubles(nl + 1, phiorder) + 4 * ldh * ldh + 8 * ldh;
+  PSF_TRY(meth->scratch.ensure(sizeof(double) * fs));
+  PSF_TRY(meth->partials.ensure(sizeof(double) * 2 * 4096));
+  PSF_TRY(meth->ctrl.ensure(sizeof(KCtrl) + 64));
+  return PSFUN_SUCCESS;
+}
+
+static int grid_for(int64_t items, int threads, int per_sm) {
+  int64_t g = (items + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * per_sm;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+static int mgs_grid() {
+  static int g = 0;
+  if (g == 0) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ar_mgs, kMgsThreads, 0);
+    if (per < 1) per = 1;
+    g = sm_count() * std::min(per, 1);
+  }
+  return g;
+}
+
+int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x, double eps,
+                        int itmax, int itrace, int istop, int* iter, double* err, double* res, int res_cap,
+                        int* res_len) {
+  (void)itrace;
+  char kn[32];
+  upper_trim(meth->kname, kn, sizeof kn);
+  int arnoldi;
+  if (!strcmp(kn, "ARNOLDI")) arnoldi = 1;
+  else if (!strcmp(kn, "LANCZOS")) arnoldi = 0;
+  else {
+    set_last_error(std::string("kname not available: ") + kn);
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;  // psfun_d_krylov_mod.F90:265-266
+  }
+  if (istop < 1 || istop > 2) return PSFUN_ERR_INVALID_ISTOP;
+  if (!x || !y || !a) return PSFUN_ERR_INVALID_VECT_STATE;
+  const int nl = itmax;
+  FunParams fp;
+  if (!parse_fun(fun, &fp)) {
+    set_last_error("invalid function name / variant");
+    return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  }
+  if (nl < 2) {
+    set_last_error("itmax < 2 leaves an empty projected matrix");
+    return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  }
+  const bool userf = (fp.fname == FN_USERF);
+  if (userf && !fun->f_ptr) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  const int64_t n = a->n;
+  PSF_TRY(ensure_workspace(meth, n, nl, fp.phiorder));
+  cudaStream_t s = stream();
+
+  // The Krylov space carries the scaling (Arnoldi) or ignores it (Lanczos);
+  // f(H) is always evaluated with scaling 1 (psfun_d_arnoldi.f90:173-174,
+  // psfun_d_lanczos.f90:172-173).
+  const double scaling = fun->scaling;
+  FunParams fpk = fp;
+  fpk.scaling = 1.0;
+
+  KState st;
+  st.n = n;
+  st.ldv = meth->ldv;
+  st.nl = nl;
+  st.ldh = nl + 1;
+  st.V = meth->V.as<double>();
+  st.u = meth->u.as<double>();
+  double* sm = meth->small.as<double>();
+  const size_t ldh = (size_t)nl + 1;
+  st.H = sm;
+  st.s = sm + ldh * ldh;
+  st.rs = st.s + (ldh + 2);
+  st.yk = st.rs + (ldh + 2);
+  st.e1 = st.yk + (ldh + 2);
+  st.coef = st.e1 + (ldh + 2);
+  st.partials = meth->partials.as<double>();
+  st.ctrl = meth->ctrl.as<KCtrl>();
+  st.fscratch = meth->scratch.as<double>();
+  st.ework = st.fscratch + fh_scratch_doubles(nl + 1, fp.phiorder);
+  st.host_flag = nullptr;
+
+  // reset the solve state
+  PSF_CUDA(cudaMemsetAsync(sm, 0, meth->small.bytes, s));
+  KCtrl h0;
+  memset(&h0, 0, sizeof h0);
+  h0.errnum = 0.0;
+  h0.errden = 1.0;
+  PSF_CUDA(cudaMemcpyAsync(st.ctrl, &h0, sizeof h0, cudaMemcpyHostToDevice, s));
+  const double one = 1.0;
+  PSF_CUDA(cudaMemcpyAsync(st.e1, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+
+  // host-visible progress flag for early termination of the enqueue loop
+  static volatile int* hflag = nullptr;
+  static int* dflag = nullptr;
+  if (!hflag) {
+    int* p = nullptr;
+    PSF_CUDA(cudaHostAlloc((void**)&p, 4 * sizeof(int), cudaHostAllocMapped));
+    hflag = p;
+    PSF_CUDA(cudaHostGetDevicePointer((void**)&dflag, p, 0));
+  }
+  hflag[0] = 0;
+  hflag[1] = 0;
+  st.host_flag = dflag;
+
+  const CsrDev A = a->dev();
+  const int gv = grid_for(n, kVecThreads, 8);
+  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 8);
+  const int gm = mgs_grid();
+  const int tridiag = arnoldi ? 0 : 1;
+
+  k_init<<<gv, kVecThreads, 0, s>>>(st, x);
+  count_launch();
+  if (!arnoldi) {
+    k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, 1);
+    k_lz_update<<<gv, kVecThreads, 0, s>>>(st, 1);
+    count_launch(2);
+  }
+  PSF_CUDA(cudaGetLastError());
+  const int max_ahead = 24;
+  for (int i = 2; i <= nl; ++i) {
+    if (istop == 1 && hflag[0]) break;
+    if (arnoldi) {
+      k_ar_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i, scaling);
+      void* args[] = {(void*)&st, (void*)&i};
+      PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
+      count_launch(2);
+    } else {
+      k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i);
+      k_lz_update<<<gv, kVecThreads, 0, s>>>(st, i);
+      count_launch(2);
+    }
+    if (istop == 1) {
+      if (userf) {
+        // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
+        PSF_CUDA(cudaStreamSynchronize(s));
+        KCtrl hc;
+        PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
+        if (hc.done) break;
+        PSF_TRY(userf_apply(fun->f_ptr, 1.0, i - 1, st.H, st.ldh, st.e1, st.yk, st.ework));
+        k_estimate_tail<<<1, kDenseThreads, 0, s>>>(st, i, eps);
+        count_launch();
+      } else {
+        k_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, tridiag);
+        count_launch();
+      }
+    }
+    PSF_CUDA(cudaGetLastError());
+    // keep at most max_ahead steps queued ahead of the device
+    if (istop == 1 && !userf) {
+      for (long spin = 0; i - hflag[1] > max_ahead && !hflag[0]; ++spin) {
+        if (cudaStreamQuery(s) == cudaSuccess) break;
+        if (spin > 200000000L) break;
+      }
+    }
+  }
+  if (userf) {
+    PSF_CUDA(cudaStreamSynchronize(s));
+    KCtrl hc;
+    PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
+    if (hc.info == 0 && hc.beta0 != 0.0 && !hc.conv) {
+      const int m = (arnoldi && hc.breakdown) ? hc.itx : hc.itx - 1;
+      if (m >= 1) PSF_TRY(userf_apply(fun->f_ptr, 1.0, m, st.H, st.ldh, st.e1, st.yk, st.ework));
+    }
+    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, 1);
+  } else {
+    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, 0);
+  }
+  k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
+  count_launch(2);
+  PSF_CUDA(cudaGetLastError());
+
+  KCtrl hc;
+  PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
+  std::vector<double> hrs(nl + 1);
+  PSF_CUDA(cudaMemcpyAsync(hrs.data(), st.rs, sizeof(double) * (nl + 1), cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (hc.err & DEVERR_TIMEOUT) {
+    set_last_error("device-side wait timed out");
+    return PSFUN_ERR_DEVICE_TIMEOUT;
+  }
+  if (hc.info != 0) return hc.info;
+  if (iter) *iter = hc.itx;
+  if (err) *err = hc.derr;
+  if (res) {
+    const int cnt = std::min(hc.itx + 1, res_cap);
+    for (int l = 0; l < cnt; ++l) res[l] = (l < hc.itx) ? hrs[l] : hc.derr;
+    if (res_len) *res_len = cnt;
+  } else if (res_len) {
+    *res_len = 0;
+  }
+  return PSFUN_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// serial apply: y = f(scaling*a) x for a dense matrix on the device
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kDenseThreads) k_serial_apply(FunParams fp, int n, const double* a, int lda,
+                                                                const double* x, double* y, double* scratch,
+                                                                int* status) {
+  __shared__ DenseSmem sm;
+  const int rc = fh_apply_cta(fp, n, a, lda, x, y, scratch, false, sm);
+  if (threadIdx.x == 0) *status = rc;
+}
+
+int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev, const double* x_dev) {
+  FunParams fp;
+  if (n < 1) return PSFUN_ERR_FROM_SUBROUTINE;
+  if (!parse_fun(fun, &fp)) return PSFUN_ERR_FROM_SUBROUTINE;
+  cudaStream_t s = stream();
+  const size_t fs = fh_scratch_doubles(n, fp.phiorder) + 4 * (size_t)n * n + 8 * (size_t)n;
+  DevBuf scr;
+  PSF_TRY(scr.ensure(sizeof(double) * fs + 64));
+  int rc = PSFUN_SUCCESS;
+  if (fp.fname == FN_USERF) {
+    if (!fun->f_ptr) { scr.release(); return PSFUN_ERR_FROM_SUBROUTINE; }
+    rc = userf_apply(fun->f_ptr, fun->scaling, n, a_dev, lda, x_dev, y_dev, scr.as<double>());
+  } else {
+    int* dstat = reinterpret_cast<int*>(scr.as<char>() + sizeof(double) * fs);
+    k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr.as<double>(), dstat);
+    count_launch();
+    int hs = 0;
+    cudaError_t e = cudaMemcpyAsync(&hs, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      set_last_error(cudaGetErrorString(e));
+      rc = PSFUN_ERR_CUDA;
+    } else if (hs != 0) {
+      rc = PSFUN_ERR_FROM_SUBROUTINE;
+    }
+  }
+  scr.release();
+  return rc;
+}
+
+
+// ===========================================================================
+// Rational quadrature sum  y = eta * A * Im( sum_j c_j (xi_j I + sign A)^{-1} x )
+// for the poles xi_j, weights c_j, eta and sign of a psfun_z_quadrature
+// (quadratures/psfun_z_quadrature_mod.F90:42-55, filled by hhtmethod1,
+// quadratures/psfun_z_quadrules_mod.f90:40-85; the reference provides no
+// routine that forms the sum).  With HHT's sign = -1 the systems are
+// (xi_j I - A) u_j = x.
+//
+// All N shifted systems share one Lanczos basis of A (multi-shift FOM/CG):
+// each step costs one SpMV plus the three-term update, independent of N.
+// After step i the relative residual of shift j is beta_{i+1} |phi_i(xi_j)|,
+// phi_i the last entry of (xi_j I + sign T_i)^{-1} e_1, updated in O(1) per
+// shift through the LDL^T recurrence of the shifted tridiagonal.  At exit the
+// N tridiagonal systems are solved exactly (banded complex GEPP), the
+// combination g = Im(sum_j c_j z_j) is formed in the small space, and the
+// leading A is applied through the Lanczos relation A V_m = V_{m+1} Tbar_m, so
+// y = eta V_{m+1} (Tbar_m g) is one recombination pass over the basis.
+// ===========================================================================
+struct MsParams {
+  int N;
+  const double* xi;  // 2N
+  const double* c;   // 2N
+  double sign, eta, eps;
+  double* d;      // 2N: LDL pivots of the last step
+  double* phi;    // 2N
+  double* resid;  // N
+};
+
+__global__ void k_ms_monitor(KState st, MsParams mp, int i) {
+  __shared__ double red[32];
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  const double alpha = HAT(st, i, i);
+  const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
+  const double bnext = HAT(st, i + 1, i);
+  double worst = 0.0;
+  for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
+    const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
+    const zc a = zadd(xi, zmk(mp.sign * alpha, 0.0));
+    zc d, phi;
+    if (i == 1) {
+      d = a;
+      phi = zdiv(zmk(1.0, 0.0), d);
+    } else {
+      const zc dprev = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
+      const zc phiprev = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
+      const double b = mp.sign * bi;
+      d = zsub(a, zdiv(zmk(b * b, 0.0), dprev));
+      phi = zdiv(zmul(phiprev, zmk(-b, 0.0)), d);
+    }
+    mp.d[2 * j] = cuCreal(d);
+    mp.d[2 * j + 1] = cuCimag(d);
+    mp.phi[2 * j] = cuCreal(phi);
+    mp.phi[2 * j + 1] = cuCimag(phi);
+    const double r = bnext * zabs(phi);
+    mp.resid[j] = r;
+    worst = fmax(worst, r);
+  }
+  worst = block_max(worst, red);
+  if (threadIdx.x == 0) {
+    c->itx = i;
+    c->errnum = worst;
+    c->errden = 1.0;
+    if (worst < mp.eps || c->breakdown) {
+      c->done = 1;
+      c->conv = 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+  }
+}
+
+// Solves the N shifted tridiagonal systems of dimension m, forms the
+// coefficients of y = eta V_{m+1} Tbar_m g, g = Im(sum_j c_j z_j).
+__global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams mp) {
+  KCtrl* c = st.ctrl;
+  if (c->info != 0) return;
+  if (c->beta0 == 0.0) {
+    if (threadIdx.x == 0) c->nterms = 0;
+    return;
+  }
+  const int m = c->itx;
+  const double beta = c->beta0;
+  zc* Z = (zc*)st.fscratch;                 // N * m solutions
+  zc* band = Z + (size_t)mp.N * m;          // per shift: d, du, du2, dl (4 m)
+  double* g = st.fscratch + 2 * (size_t)mp.N * m + 8 * (size_t)mp.N * m;
+  int bad = 0;
+  for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
+    const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
+    zc* d = band + (size_t)j * 4 * m;
+    zc* du = d + m;
+    zc* du2 = du + m;
+    zc* dl = du2 + m;
+    zc* b = Z + (size_t)j * m;
+    for (int k = 0; k < m; ++k) {
+      d[k] = zadd(xi, zmk(mp.sign * HAT(st, k + 1, k + 1), 0.0));
+      const double off = (k + 1 < m) ? mp.sign * HAT(st, k + 2, k + 1) : 0.0;
+      du[k] = zmk(off, 0.0);
+      dl[k] = zmk(off, 0.0);
+      du2[k] = zmk(0.0, 0.0);
+      b[k] = zmk(k == 0 ? beta : 0.0, 0.0);
+    }
+    for (int k = 0; k < m - 1 && !bad; ++k) {
+      if (zabs(d[k]) < zabs(dl[k])) {
+        zc t;
+        t = d[k]; d[k] = dl[k]; dl[k] = t;
+        t = du[k]; du[k] = d[k + 1]; d[k + 1] = t;
+        if (k + 1 < m - 1) { t = du2[k]; du2[k] = du[k + 1]; du[k + 1] = t; }
+        t = b[k]; b[k] = b[k + 1]; b[k + 1] = t;
+      }
+      if (zabs(d[k]) == 0.0) { bad = 1; break; }
+      const zc l = zdiv(dl[k], d[k]);
+      d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
+      if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
+      b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+    }
+    if (!bad && zabs(d[m - 1]) == 0.0) bad = 1;
+    if (!bad)
+      for (int k = m - 1; k >= 0; --k) {
+        zc s = b[k];
+        if (k + 1 < m) s = zsub(s, zmul(du[k], b[k + 1]));
+        if (k + 2 < m) s = zsub(s, zmul(du2[k], b[k + 2]));
+        b[k] = zdiv(s, d[k]);
+      }
+  }
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) { c->info = PSFUN_ERR_FROM_SUBROUTINE_NON; atomicOr(&c->err, DEVERR_SINGULAR); }
+    return;
+  }
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < mp.N; ++j) {
+      const zc cj = zmk(mp.c[2 * j], mp.c[2 * j + 1]);
+      acc += cuCimag(zmul(cj, Z[(size_t)j * m + k]));
+    }
+    g[k] = acc;
+  }
+  __syncthreads();
+  // h = Tbar_m g (m+1 entries); coef_r = eta * h_r * s_r
+  for (int r = threadIdx.x; r <= m; r += blockDim.x) {
+    double h = 0.0;
+    if (r < m) h = HAT(st, r + 1, r + 1) * g[r];
+    if (r >= 1) h = fma(HAT(st, r + 1, r), g[r - 1], h);
+    if (r + 1 < m) h = fma(HAT(st, r + 1, r + 2), g[r + 1], h);
+    st.coef[r] = mp.eta * h * st.s[r + 1];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c->nterms = m + 1;
+    c->derr = c->errnum;
+  }
+}
+
+int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, double eta, double sign,
+                      const double* x, double* y, double eps, int itmax, int* iter, double* err) {
+  if (!a || !xi || !cw) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (N < 1 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  static psfun_krylov* meth = nullptr;
+  if (!meth) meth = new psfun_krylov();
+  const int64_t n = a->n;
+  const int nl = itmax;
+  PSF_TRY(ensure_workspace(meth, n, nl, 1));
+  static DevBuf msbuf;
+  PSF_TRY(msbuf.ensure(sizeof(double) * (4 * (size_t)N + 4 * (size_t)N + N) + 256));
+  // the final solve keeps N*m complex solutions and 4*N*m band entries
+  const size_t need = 2 * (size_t)N * nl + 8 * (size_t)N * nl + (size_t)nl + 64;
+  if (meth->scratch.bytes < sizeof(double) * need) PSF_TRY(meth->scratch.ensure(sizeof(double) * need));
+  cudaStream_t s = stream();
+  double* mb = msbuf.as<double>();
+  MsParams mp;
+  mp.N = N;
+  mp.xi = mb;
+  mp.c = mb + 2 * N;
+  mp.d = mb + 4 * N;
+  mp.phi = mb + 6 * N;
+  mp.resid = mb + 8 * N;
+  mp.sign = sign;
+  mp.eta = eta;
+  mp.eps = eps;
+  PSF_CUDA(cudaMemcpyAsync((void*)mp.xi, xi, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+  PSF_CUDA(cudaMemcpyAsync((void*)mp.c, cw, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+
+  KState st;
+  st.n = n;
+  st.ldv = meth->ldv;
+  st.nl = nl;
+  st.ldh = nl + 1;
+  st.V = meth->V.as<double>();
+  st.u = meth->u.as<double>();
+  double* sm = meth->small.as<double>();
+  const size_t ldh = (size_t)nl + 1;
+  st.H = sm;
+  st.s = sm + ldh * ldh;
+  st.rs = st.s + (ldh + 2);
+  st.yk = st.rs + (ldh + 2);
+  st.e1 = st.yk + (ldh + 2);
+  st.coef = st.e1 + (ldh + 2);
+  st.partials = meth->partials.as<double>();
+  st.ctrl = meth->ctrl.as<KCtrl>();
+  st.fscratch = meth->scratch.as<double>();
+  st.ework = nullptr;
+  PSF_CUDA(cudaMemsetAsync(sm, 0, meth->small.bytes, s));
+  KCtrl h0;
+  memset(&h0, 0, sizeof h0);
+  h0.errden = 1.0;
+  PSF_CUDA(cudaMemcpyAsync(st.ctrl, &h0, sizeof h0, cudaMemcpyHostToDevice, s));
+  static volatile int* hflag = nullptr;
+  static int* dflag = nullptr;
+  if (!hflag) {
+    int* p = nullptr;
+    PSF_CUDA(cudaHostAlloc((void**)&p, 4 * sizeof(int), cudaHostAllocMapped));
+    hflag = p;
+    PSF_CUDA(cudaHostGetDevicePointer((void**)&dflag, p, 0));
+  }
+  hflag[0] = 0;
+  hflag[1] = 0;
+  st.host_flag = dflag;
+
+  const CsrDev A = a->dev();
+  const int gv = grid_for(n, kVecThreads, 8);
+  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 8);
+  k_init<<<gv, kVecThreads, 0, s>>>(st, x);
+  count_launch();
+  for (int i = 1; i <= nl; ++i) {
+    if (hflag[0]) break;
+    k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i);
+    k_lz_update<<<gv, kVecThreads, 0, s>>>(st, i);
+    k_ms_monitor<<<1, 256, 0, s>>>(st, mp, i);
+    count_launch(3);
+    PSF_CUDA(cudaGetLastError());
+    for (long spin = 0; i - hflag[1] > 24 && !hflag[0]; ++spin) {
+      if (cudaStreamQuery(s) == cudaSuccess) break;
+      if (spin > 200000000L) break;
+    }
+  }
+  k_ms_final<<<1, kDenseThreads, 0, s>>>(st, mp);
+  k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
+  count_launch(2);
+  PSF_CUDA(cudaGetLastError());
+  KCtrl hc;
+  PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (hc.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
+  if (hc.info != 0) return hc.info;
+  if (iter) *iter = hc.itx;
+  if (err) *err = hc.errnum;
+  return PSFUN_SUCCESS;
+}
+
+}  // namespace psf
+
+extern "C" {
+
+int psfun_gpu_z_quadrature_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta,
+                                        double sign, const double* x, double* y, double eps, int itmax, int* iter,
+                                        double* err) {
+  return psf::quad_apply_device(a, N, xi, c, eta, sign, x, y, eps, itmax, iter, err);
+}
+
+int psfun_gpu_z_quadrature_apply(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
+                                 const double* x, double* y, double eps, int itmax, int* iter, double* err) {
+  if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  const int64_t n = a->n;
+  psf::DevBuf dx, dy;
+  PSF_TRY(dx.ensure(sizeof(double) * (n + 1)));
+  PSF_TRY(dy.ensure(sizeof(double) * (n + 1)));
+  cudaStream_t s = psf::stream();
+  PSF_CUDA(cudaMemcpyAsync(dx.ptr, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  int rc = psf::quad_apply_device(a, N, xi, c, eta, sign, dx.as<double>(), dy.as<double>(), eps, itmax, iter, err);
+  if (rc == PSFUN_SUCCESS) {
+    PSF_CUDA(cudaMemcpyAsync(y, dy.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    PSF_CUDA(cudaStreamSynchronize(s));
+  }
+  dx.release();
+  dy.release();
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+"""Seeded synthetic workloads and MatrixMarket ingest.
+
+The reference's drivers read MatrixMarket files (examples/polynomial/arnolditest.F90:111-125)
+and ship one fixture, a 50 x 50 1-D Laplacian (examples/polynomial/laplacian.mtx).
+The benchmark problems are synthetic and seeded (numpy default_rng):
+
+  config1   2-D 5-point Dirichlet Laplacian 100 x 100, stencil [-1,-1,4,-1,-1],
+            x ~ U[-1,1]^n (seed 0) normalised; y = exp(-A) x
+  config2a  3-D 7-point Laplacian 128^3 (unscaled), x ~ N(0,1) (seed 1) normalised;
+            y = exp(-0.05 A) x by Lanczos, m = 80
+  config2b  2-D convection-diffusion 2048^2, -Lap u + beta.grad u, beta = (50, 25),
+            first-order upwind, h = 1/2049, scaled by h^-2 / h^-1; y = phi_1(-1e-3 A) x
+  config3   3-D 7-point Laplacian 96^3, x ~ N(0,1) (seed 2); y = A^{-1/2} x by the
+            HHT rule with N = 24 and the analytic spectrum bounds
+  config4   64 uneven instances (seed 3), 4 right-hand sides each
+  config5   512^2 grid-graph Laplacian with lognormal(0,0.7) conductivities (seed 4)
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+
+
+def _tridiag(n: int, lo: float, d: float, up: float) -> sp.csr_matrix:
+    return sp.diags([np.full(n - 1, lo), np.full(n, d), np.full(n - 1, up)], [-1, 0, 1], format="csr")
+
+
+def laplacian_1d(n: int) -> sp.csr_matrix:
+    """tridiag(-1, 2, -1)."""
+    return _tridiag(n, -1.0, 2.0, -1.0)
+
+
+def laplacian_2d(nx: int, ny: int | None = None) -> sp.csr_matrix:
+    """5-point Dirichlet Laplacian, unscaled: 4 on the diagonal, -1 off."""
+    ny = nx if ny is None else ny
+    A = sp.kron(sp.identity(ny), laplacian_1d(nx)) + sp.kron(laplacian_1d(ny), sp.identity(nx))
+    A = A.tocsr()
+    A.sort_indices()
+    return A
+
+
+def laplacian_3d(n1: int) -> sp.csr_matrix:
+    """7-point Dirichlet Laplacian on n1^3, unscaled: 6 on the diagonal, -1 off."""
+    T = laplacian_1d(n1)
+    I = sp.identity(n1)
+    A = sp.kron(I, sp.kron(I, T)) + sp.kron(I, sp.kron(T, I)) + sp.kron(T, sp.kron(I, I))
+    A = A.tocsr()
+    A.sort_indices()
+    return A
+
+
+def convdiff_2d(N: int, beta=(50.0, 25.0)) -> sp.csr_matrix:
+    """-Lap u + beta . grad u on the unit square, N x N interior points,
+    h = 1/(N+1), first-order upwind (beta > 0), scaled by h^-2 and h^-1."""
+    h = 1.0 / (N + 1)
+    bx, by = beta
+
+    def dir_op(b):
+        D2 = _tridiag(N, -1.0, 2.0, -1.0) / (h * h)
+        D1 = _tridiag(N, -1.0, 1.0, 0.0) * (b / h)  # (u_i - u_{i-1}) / h
+        return (D2 + D1).tocsr()
+
+    A = sp.kron(sp.identity(N), dir_op(bx)) + sp.kron(dir_op(by), sp.identity(N))
+    A = A.tocsr()
+    A.sort_indices()
+    return A
+
+
+def laplacian_3d_bounds(n1: int):
+    """Analytic extreme eigenvalues of the unscaled 7-point Laplacian on n1^3."""
+    lam = lambda k: 4.0 * math.sin(math.pi * k / (2.0 * (n1 + 1))) ** 2
+    return 3.0 * lam(1), 3.0 * lam(n1)
+
+
+def grid_edges(N: int):
+    """Edges of the N x N grid graph: horizontal ones first (row-major), then vertical."""
+    idx = np.arange(N * N).reshape(N, N)
+    hi, hj = idx[:, :-1].ravel(), idx[:, 1:].ravel()
+    vi, vj = idx[:-1, :].ravel(), idx[1:, :].ravel()
+    return np.concatenate([hi, vi]), np.concatenate([hj, vj])
+
+
+def graph_laplacian(n: int, ei, ej, w, shift: float = 0.0) -> sp.csr_matrix:
+    """L = sum_e w_e (e_i - e_j)(e_i - e_j)^T + shift * I."""
+    W = sp.coo_matrix((np.concatenate([w, w]), (np.concatenate([ei, ej]), np.concatenate([ej, ei]))),
+                      shape=(n, n)).tocsr()
+    d = np.asarray(W.sum(axis=1)).ravel() + shift
+    L = (sp.diags(d) - W).tocsr()
+    L.sum_duplicates()
+    L.sort_indices()
+    return L
+
+
+def rgg_knn_laplacian(n: int, k: int, rng: np.random.Generator, shift: float = 1e-3) -> sp.csr_matrix:
+    """Random geometric graph in the unit square, k nearest neighbours,
+    symmetrised (union, larger weight kept), weights lognormal(0, 0.5),
+    graph Laplacian + shift * I."""
+    from scipy.spatial import cKDTree
+
+    pts = rng.random((n, 2))
+    _, nb = cKDTree(pts).query(pts, k=k + 1)
+    ei = np.repeat(np.arange(n), k)
+    ej = nb[:, 1:].ravel()
+    w = rng.lognormal(0.0, 0.5, size=ei.shape[0])
+    W = sp.coo_matrix((w, (ei, ej)), shape=(n, n)).tocsr()
+    W = W.maximum(W.T).tocoo()
+    upper = W.row < W.col
+    return graph_laplacian(n, W.row[upper], W.col[upper], W.data[upper], shift)
+
+
+def read_matrix_market(path) -> sp.csr_matrix:
+    """Coordinate real/integer MatrixMarket, general or symmetric, 1-based."""
+    with open(path) as f:
+        header = f.readline().lower().split()
+        if len(header) < 5 or header[0] != "%%matrixmarket" or header[2] != "coordinate":
+            raise ValueError("only coordinate MatrixMarket files are supported")
+        symm = header[4] in ("symmetric", "skew-symmetric")
+        skew = header[4] == "skew-symmetric"
+        line = f.readline()
+        while line.startswith("%"):
+            line = f.readline()
+        nr, nc, nz = (int(t) for t in line.split())
+        data = np.loadtxt(f, ndmin=2, max_rows=nz)
+    i = data[:, 0].astype(np.int64) - 1
+    j = data[:, 1].astype(np.int64) - 1
+    v = data[:, 2] if data.shape[1] > 2 else np.ones(len(i))
+    if symm:
+        off = i != j
+        i, j, v = (np.concatenate([i, j[off]]), np.concatenate([j, i[off]]),
+                   np.concatenate([v, -v[off] if skew else v[off]]))
+    A = sp.coo_matrix((v, (i, j)), shape=(nr, nc)).tocsr()
+    A.sort_indices()
+    return A
+
+
+def unit(v: np.ndarray) -> np.ndarray:
+    return v / np.linalg.norm(v)
+
+
+@dataclass
+class Problem:
+    name: str
+    A: sp.csr_matrix
+    x: np.ndarray
+    params: dict
+
+
+def config1() -> Problem:
+    A = laplacian_2d(100)
+    x = unit(np.random.default_rng(0).uniform(-1.0, 1.0, A.shape[0]))
+    return Problem("laplace2d-100x100 exp(-A)x m<=50 eps=1e-10", A, x,
+                   dict(t=1.0, itmax=50, eps=1e-10))
+
+
+def config2a(n1: int = 128) -> Problem:
+    A = laplacian_3d(n1)
+    x = unit(np.random.default_rng(1).standard_normal(A.shape[0]))
+    return Problem(f"laplace3d-{n1}^3 exp(-0.05A)x lanczos m=80", A, x, dict(t=0.05, m=80))
+
+
+def config2b(N: int = 2048) -> Problem:
+    A = convdiff_2d(N)
+    x = unit(np.random.default_rng(1).standard_normal(A.shape[0]))
+    return Problem(f"convdiff2d-{N}^2 phi1(-1e-3A)x arnoldi m=60", A, x, dict(t=1e-3, m=60))
+
+
+def config3(n1: int = 96) -> Problem:
+    A = laplacian_3d(n1)
+    x = np.random.default_rng(2).standard_normal(A.shape[0])
+    return Problem(f"laplace3d-{n1}^3 A^-1/2 x HHT N=24", A, x,
+                   dict(N=24, bounds=laplacian_3d_bounds(n1), eps=1e-10))
+
+
+def config4(count: int = 64, nrhs: int = 4, scale: float = 1.0):
+    """64 uneven instances: 32 2-D Laplacians (side ~ U{64..512}) and 32 kNN
+    random-geometric-graph Laplacians (n log-uniform in [4096, 262144]);
+    `scale` < 1 shrinks the sizes for tests."""
+    rng = np.random.default_rng(3)
+    out = []
+    for i in range(count):
+        if i < count // 2:
+            side = int(rng.integers(64, 513))
+            side = max(8, int(side * math.sqrt(scale)))
+            A = laplacian_2d(side)
+            kind = f"lap2d-{side}"
+        else:
+            n = int(round(math.exp(rng.uniform(math.log(4096), math.log(262144)))))
+            n = max(64, int(n * scale))
+            A = rgg_knn_laplacian(n, 8, rng)
+            kind = f"rgg-{n}"
+        X = rng.standard_normal((nrhs, A.shape[0]))
+        t = float(rng.uniform(0.01, 1.0))
+        out.append(Problem(kind, A, X, dict(t=t, m=60, eps=1e-8)))
+    return out
+
+
+def config5(N: int = 512):
+    rng = np.random.default_rng(4)
+    ei, ej = grid_edges(N)
+    theta = rng.lognormal(0.0, 0.7, size=ei.shape[0])
+    theta_star = rng.lognormal(0.0, 0.7, size=ei.shape[0])
+    x = rng.standard_normal(N * N)
+    return dict(N=N, ei=ei, ej=ej, theta=theta, theta_star=theta_star, x=x, t=0.1)

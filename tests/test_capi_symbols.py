@@ -1,0 +1,46 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/*.h declares."""
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        src = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(psfun_gpu_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_all_declared_symbols_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_prototypes_cover_header(lib):
+    from psfun_gb300 import _capi
+    missing = [n for n in declared_symbols() if n not in _capi.PROTOS]
+    assert not missing, missing
+
+
+def test_version_string(lib):
+    assert b"sm_103a" in lib.psfun_gpu_version()
+
+
+def test_setters_without_gpu(lib):
+    """Handle set-up and the reference's set() semantics are host logic."""
+    import psfun_gb300 as pg
+    f = pg.PsfunDSerial()
+    assert f.get()["fname"] == "EXP" and f.get()["variant"] == "EXPOKIT" and f.get()["padedegree"] == 6
+    assert f.set("fname", "PHI") == 0 and f.get()["fname"] == "PHI"
+    assert f.set("scaling", -0.5) == 0 and f.get()["scaling"] == -0.5
+    assert f.set("Pade_Degree", 8) == 0 and f.get()["padedegree"] == 8
+    assert f.set("NOPE", "x") == 111 and f.set("SCALING", 1) == 111
+    k = pg.PsfunDKrylov()
+    assert k.set("kname", "LANCZOS") == 0 and k.set("itmax", 10) == 0 and k.set("BAD", 1) == 111
+    assert k.set("ITMAX", "x") == 111

@@ -1,0 +1,53 @@
+"""Shifted CG (psb_krylov -> psfun_dcg_vect) on the GPU against the oracle."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from psfun_gb300 import matrices
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", ["NONE", "DIAG"])
+@pytest.mark.parametrize("istop", [1, 2])
+def test_cg_vs_oracle(lib, orc, prec, istop):
+    import psfun_gb300 as pg
+    A = matrices.laplacian_2d(40)
+    b = np.random.default_rng(2).standard_normal(A.shape[0])
+    eta, zeta = 1.5, 0.3
+    x, info, it, err = pg.psb_krylov("CG", pg.CsrMatrix.from_scipy(A), prec, b, eta, zeta, np.zeros_like(b),
+                                     1e-12, itmax=3000, istop=istop)
+    o = orc.dcg(orc.Csr.from_scipy(A), b, eta, zeta, eps=1e-12, itmax=3000, istop=istop, prec=prec)
+    assert info == 0 and o["info"] == 0
+    assert abs(it - o["iter"]) <= 1
+    assert np.linalg.norm(x - o["x"]) <= 1e-9 * np.linalg.norm(o["x"])
+    assert err <= 1e-12
+
+
+def test_shiftedtest_scenario(lib):
+    import psfun_gb300 as pg
+    T = -matrices.laplacian_1d(50)
+    x, info, it, err = pg.psb_krylov("CG", pg.CsrMatrix.from_scipy(T), "DIAG", np.ones(50), -1.0, 1.0,
+                                     np.zeros(50), 1e-7, itmax=500, istop=2)
+    assert info == 0 and err <= 1e-7
+    M = (-T + sp.identity(50)).toarray()
+    assert np.linalg.norm(M @ x - 1.0) <= 1e-7 * np.sqrt(50) * 1.0001
+
+
+def test_cg_itmax_and_unknown_method(lib, orc):
+    import psfun_gb300 as pg
+    A = matrices.laplacian_2d(30)
+    b = np.ones(A.shape[0])
+    x, info, it, err = pg.psb_krylov("BICGSTAB", pg.CsrMatrix.from_scipy(A), "NONE", b, 1.0, 0.0,
+                                     np.zeros_like(b), 1e-30, itmax=7, istop=2)
+    o = orc.dcg(orc.Csr.from_scipy(A), b, 1.0, 0.0, eps=1e-30, itmax=7, istop=2)
+    assert info == 0 and it == o["iter"] == 7
+    assert np.linalg.norm(x - o["x"]) <= 1e-12 * np.linalg.norm(o["x"])
+
+
+def test_cg_errors(lib):
+    import psfun_gb300 as pg
+    a = pg.CsrMatrix.from_scipy(matrices.laplacian_2d(8))
+    b = np.ones(64)
+    assert pg.psb_krylov("CG", a, "NONE", b, 1.0, 0.0, np.zeros(64), 1e-8, istop=3)[1] == 5001
+    assert pg.psb_krylov("CG", a, "ILU99", b, 1.0, 0.0, np.zeros(64), 1e-8)[1] == 111

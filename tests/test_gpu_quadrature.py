@@ -1,0 +1,62 @@
+"""Rational quadrature A^{-1/2} x (HHT rule, multi-shift solve sharing one
+Lanczos basis) against exact spectral evaluation through the Kronecker
+structure of the grid Laplacians, at test size and at the full 96^3 size."""
+import numpy as np
+import pytest
+
+from psfun_gb300 import matrices
+
+pytestmark = pytest.mark.gpu
+
+
+def spectral_1d(n1):
+    k = np.arange(1, n1 + 1)
+    lam = 4.0 * np.sin(np.pi * k / (2.0 * (n1 + 1))) ** 2
+    Q = np.sqrt(2.0 / (n1 + 1)) * np.sin(np.outer(k, k) * np.pi / (n1 + 1))
+    return lam, Q
+
+
+def apply_fun_3d(n1, x, fun):
+    lam, Q = spectral_1d(n1)
+    X = x.reshape(n1, n1, n1)
+    Xh = np.einsum("ia,jb,kc,ijk->abc", Q, Q, Q, X, optimize=True)
+    L = lam[:, None, None] + lam[None, :, None] + lam[None, None, :]
+    return np.einsum("ia,jb,kc,abc->ijk", Q, Q, Q, fun(L) * Xh, optimize=True).ravel()
+
+
+def run(n1, N, x, eps=1e-10):
+    import psfun_gb300 as pg
+    A = matrices.laplacian_3d(n1)
+    q = pg.PsfunZQuadrature()
+    info = q.computepoles(pg.hhtmethod1, lambda z: 1.0 / np.sqrt(z), N,
+                          rparams=list(matrices.laplacian_3d_bounds(n1)))
+    assert info == 0
+    q.setmatrix(pg.CsrMatrix.from_scipy(A))
+    return q, q.apply(x, eps=eps, itmax=3000)
+
+
+@pytest.mark.parametrize("n1", [6, 16])
+def test_quadrature_matches_its_rule(lib, n1):
+    """Solver error alone: the GPU sum equals the same quadrature rule evaluated exactly."""
+    x = np.random.default_rng(2).standard_normal(n1 ** 3)
+    q, (y, info, it, err) = run(n1, 24, x)
+    assert info == 0 and err < 1e-10
+    def rule(L):
+        s = sum(cj * 1.0 / (xj + q.sign * L) for xj, cj in zip(q.xi, q.c))
+        return q.eta * L * np.imag(s)
+    ref = apply_fun_3d(n1, x, rule)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-9
+
+
+def test_config3_full_size(lib):
+    """96^3, N = 24: against the exact A^{-1/2} x."""
+    p = matrices.config3()
+    q, (y, info, it, err) = run(96, 24, p.x)
+    assert info == 0 and err < 1e-10
+    ref = apply_fun_3d(96, p.x, lambda L: L ** -0.5)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-9
+
+
+def test_zero_rhs(lib):
+    _, (y, info, it, err) = run(6, 8, np.zeros(216))
+    assert info == 0 and not np.any(y)

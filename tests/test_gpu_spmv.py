@@ -1,0 +1,74 @@
+"""CSR SpMV on the GPU: index handling is bit-exact (integer-valued data makes
+every product and sum exact, so any indexing slip changes the result)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+
+
+def int_matrix(n, density, seed, long_rows=()):
+    rng = np.random.default_rng(seed)
+    A = sp.random(n, n, density=density, random_state=seed, format="lil")
+    for r in long_rows:
+        cols = rng.choice(n, size=min(n, 5000), replace=False)
+        A[r, cols] = 1.0
+    A = A.tocsr()
+    A.data = rng.integers(-3, 4, size=A.nnz).astype(np.float64)
+    A.eliminate_zeros()
+    A.sort_indices()
+    return A
+
+
+@pytest.mark.parametrize("n,density,long_rows", [(1, 1.0, ()), (37, 0.2, ()), (5000, 0.002, ()),
+                                                  (20000, 0.0004, (3, 19999)), (6000, 0.0, ())])
+def test_spmv_bit_exact(lib, n, density, long_rows):
+    import psfun_gb300 as pg
+    A = int_matrix(n, density, n, long_rows)
+    x = np.random.default_rng(1).integers(-5, 6, size=n).astype(np.float64)
+    a = pg.CsrMatrix.from_scipy(A)
+    y = a.spmv(x)
+    assert np.array_equal(y, A @ x)
+    y0 = np.random.default_rng(2).integers(-5, 6, size=n).astype(np.float64)
+    y2 = a.spmv(x, alpha=2.0, beta=-3.0, y=y0)
+    assert np.array_equal(y2, 2.0 * (A @ x) - 3.0 * y0)
+
+
+def test_spmv_one_based_input(lib):
+    import psfun_gb300 as pg
+    A = int_matrix(3000, 0.003, 7)
+    a1 = pg.CsrMatrix(A.indptr + 1, A.indices + 1, A.data, index_base=1)
+    x = np.arange(3000, dtype=np.float64) % 7 - 3
+    assert np.array_equal(a1.spmv(x), A @ x)
+
+
+def test_spmv_float_matches_oracle(lib, orc):
+    import psfun_gb300 as pg
+    from psfun_gb300 import matrices
+    A = matrices.convdiff_2d(64)
+    x = np.random.default_rng(3).standard_normal(A.shape[0])
+    y = pg.CsrMatrix.from_scipy(A).spmv(x, alpha=-0.7)
+    ref = orc.spmv(orc.Csr.from_scipy(A), x, alpha=-0.7)
+    assert np.linalg.norm(y - ref) <= 1e-14 * np.linalg.norm(ref)
+
+
+def test_invalid_csr_rejected(lib):
+    import psfun_gb300 as pg
+    with pytest.raises(pg.PsfunError) as e:
+        pg.CsrMatrix([0, 1, 2], [0, 2], [1.0, 1.0])  # column 2 out of range for n = 2
+    assert e.value.info == 9003
+    with pytest.raises(pg.PsfunError) as e:
+        pg.CsrMatrix([0, 2, 1], [0, 1], [1.0, 1.0])  # rowptr not monotone
+    assert e.value.info == 9003
+
+
+def test_spmv_device_pointers(lib):
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    A = int_matrix(4000, 0.003, 11)
+    x = np.random.default_rng(4).integers(-5, 6, size=4000).astype(np.float64)
+    a = pg.CsrMatrix.from_scipy(A)
+    xd = torch.tensor(x, device="cuda")
+    yd = a.spmv(xd)
+    torch.cuda.synchronize()
+    assert np.array_equal(yd.cpu().numpy(), A @ x)
