@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark of the f(A)x hot path on GB300.
+
+Workload (one "step" = one solve):  y = exp(-0.05 A) x on the 3-D 7-point
+Laplacian 128^3 (n = 2,097,152, nnz = 14,581,760), x ~ N(0,1) seed 1
+normalised, by Lanczos with Krylov dimension m = 80 (itmax 80, istop 2) and the
+reference's Lanczos variant EXP/CHBSYM.  Lanczos ignores fun%scaling in the
+reference (psfun_d_lanczos.f90:172-173), so the matrix passed is -0.05 A.
+
+  value      solves/s with x, y and A resident in HBM (device-pointer C-ABI)
+  e2e        solves/s through the host-pointer C-ABI (x pinned on the host,
+             H2D of x and D2H of y inside every step)
+  roofline   the Lanczos SpMV+dot kernel: algorithmic bytes per launch
+             (12 nnz + 4 (n+1) + 16 n) / its CUDA-event launch time
+  cpu_baseline  the CPU restatement (oracle) on the host cores
+
+--impl reference runs the reference's algorithm on the host CPU instead (the
+reference cannot be built on this image: no gfortran / MPI / PSBLAS), i.e. the
+oracle port of psfun_d_lanczos with OpenMP over rows, and prints the same line.
+Multi-GPU: replicas (independent solves per rank, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N1 = 128
+T_EXP = 0.05
+M_KRYLOV = 80
+VARIANT = "CHBSYM"
+METRIC = "f(A)x solves/s (exp(-0.05A)x, Lanczos m=80, 3-D 7-pt Laplacian 128^3)"
+WORKLOAD = ("3-D 7-point Laplacian 128^3 (n=2,097,152, nnz=14,581,760), y=exp(-0.05A)x, Lanczos EXP/CHBSYM, "
+            "Krylov dim m=80 (itmax=80, istop=2), FP64 CSR int32 indices")
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def algorithmic_bytes(n: int, nnz: int):
+    b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    return dict(spmv=b_spmv, update=32 * n, step=b_spmv + 32 * n)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def make_problem(n1: int = N1):
+    from psfun_gb300 import matrices
+    A = matrices.laplacian_3d(n1)
+    x = matrices.unit(np.random.default_rng(1).standard_normal(A.shape[0]))
+    return A, x
+
+
+def cpu_solve_oracle(A, x, threads: int):
+    """One solve of the same workload with the C restatement (OpenMP, `threads` cores)."""
+    from oracle import oracle as orc
+    orc.set_threads(threads)
+    Am = orc.Csr.from_scipy(-T_EXP * A)
+    fun = orc.serial("EXP", VARIANT, 1.0)
+    t0 = time.perf_counter()
+    r = orc.krylov("LANCZOS", fun, Am, x, 1e-12, itmax=M_KRYLOV, istop=2)
+    return time.perf_counter() - t0, r
+
+
+def cpu_baseline(A, x, budget_s: float = 20.0, max_solves: int = 5):
+    threads = os.cpu_count() or 1
+    times, last = [], None
+    t_start = time.perf_counter()
+    while len(times) < max_solves:
+        dt, last = cpu_solve_oracle(A, x, threads)
+        times.append(dt)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    best = min(times)
+    return {"value": 1.0 / best, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full solve(s) of the benchmark workload (C restatement of psfun_d_lanczos + "
+                      f"DSCHBV, OpenMP over rows), best time {best:.3f} s"}, last
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    A, x = make_problem()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_solve_oracle(A, x, threads)
+    times = []
+    for _ in range(args.steps):
+        dt, _r = cpu_solve_oracle(A, x, threads)
+        times.append(dt)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "parallelism": "host CPU, OpenMP"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": "every step is one full solve of the workload by the C restatement of the "
+                                   "reference's Lanczos (reference itself not buildable: no gfortran/MPI/PSBLAS)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
+                                                        "for profiling captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    torch.cuda.init()
+    import psfun_gb300 as pg
+    from psfun_gb300 import _capi
+    L = _capi.load()
+
+    A, x = make_problem(args.n1)
+    n, nnz = A.shape[0], A.nnz
+    nbytes = algorithmic_bytes(n, nnz)
+    a = pg.CsrMatrix.from_scipy(-T_EXP * A)
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", VARIANT)
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.current_stream()
+    L.psfun_gpu_set_stream(stream.cuda_stream)
+
+    def solve_dev():
+        r = meth.apply(fun, a, xd, 1e-12, itmax=M_KRYLOV, istop=2, y=yd)
+        if r.info != 0:
+            raise RuntimeError(f"solve failed: info={r.info} {_capi.last_error()}")
+        return r
+
+    for _ in range(max(3, args.warmup)):
+        solve_dev()
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident inputs ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = _capi.kernel_launches()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solve_dev()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = _capi.kernel_launches() - launches0
+    elapsed_ms = e0.elapsed_time(e1)
+    # ---- per-kernel launch times: the same solves again with CUDA events
+    # recorded around each launch on the launching stream ----
+    L.psfun_gpu_profile_enable(1)
+    for _ in range(max(3, args.steps // 4)):
+        solve_dev()
+    torch.cuda.synchronize()
+    prof = {}
+    for k, nm in enumerate(["lz_spmv", "lz_update", "ar_spmv", "ar_mgs", "final", "recombine"]):
+        cnt = C_longlong()
+        tot = C_double()
+        L.psfun_gpu_profile_read(k, cnt, tot)
+        prof[nm] = (cnt.value, tot.value)
+    L.psfun_gpu_profile_enable(0)
+
+    # ---- e2e: host buffers through the C-ABI ----
+    xh = torch.tensor(x).pin_memory().numpy()
+    yh = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        meth.apply(fun, a, xh, 1e-12, itmax=M_KRYLOV, istop=2, y=yh)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(5, args.steps // 2)
+    for _ in range(e2e_steps):
+        r = meth.apply(fun, a, xh, 1e-12, itmax=M_KRYLOV, istop=2, y=yh)
+        assert r.info == 0
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+
+    if world > 1:
+        tmax = torch.tensor([elapsed_ms, e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms, e2e_s = float(tmax[0]), float(tmax[1])
+
+    ms_per_step = elapsed_ms / args.steps
+    value = world * args.steps / (elapsed_ms / 1e3)
+    e2e_value = world * e2e_steps / e2e_s
+
+    # accuracy: the m = 80 result against a converged solve (eps 1e-14)
+    yref = meth.apply(fun, a, xd, 1e-14, itmax=200, istop=1).y
+    torch.cuda.synchronize()
+    rel_conv = float(torch.linalg.norm(yd - yref) / torch.linalg.norm(yref))
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    cnt, tot = prof["lz_spmv"]
+    spmv_ms = tot / max(cnt, 1)
+    achieved = nbytes["spmv"] / (spmv_ms * 1e-3) / 1e9
+    ucnt, utot = prof["lz_update"]
+    upd_ms = utot / max(ucnt, 1)
+    traffic = None
+    tf = ROOT / "profiles" / "lanczos_spmv_128cube_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
+    step_ms = spmv_ms + upd_ms
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy default_rng)",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (matrix 183 MB + 81-vector basis 1.36 GB > 129 MB L2)"},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_lz_spmv (SpMV + fused alpha dot)",
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": nbytes["spmv"], "launch_ms": spmv_ms},
+        "lanczos_step": {"spmv_ms": spmv_ms, "update_ms": upd_ms, "step_ms": step_ms,
+                         "step_algorithmic_bytes": nbytes["step"],
+                         "step_GBs": nbytes["step"] / (step_ms * 1e-3) / 1e9,
+                         "solve_GBs": (M_KRYLOV * nbytes["step"] + 8 * n * (M_KRYLOV + 1)) / (ms_per_step * 1e-3)
+                         / 1e9},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "accuracy": {"rel_diff_m80_vs_converged": rel_conv},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base, ro = cpu_baseline(A, x)
+        line["cpu_baseline"] = base
+        line["accuracy"]["rel_diff_vs_oracle"] = float(np.linalg.norm(yd.cpu().numpy() - ro["y"])
+                                                       / np.linalg.norm(ro["y"]))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+from ctypes import c_double as C_double, c_longlong as C_longlong  # noqa: E402
+
+if __name__ == "__main__":
+    sys.exit(main())

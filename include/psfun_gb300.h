@@ -70,6 +70,12 @@ long long psfun_gpu_kernel_launches(void);
  * on this stream has completed. */
 int psfun_gpu_set_stream(void* stream);
 void* psfun_gpu_get_stream(void);
+/* Per-kernel timing (no counterpart in the reference): when enabled, CUDA
+ * events are recorded around the main kernels of each solve on the launching
+ * stream.  kernel: 0 Lanczos SpMV+dot, 1 Lanczos update+norm, 2 Arnoldi SpMV,
+ * 3 Arnoldi MGS, 4 final f(H), 5 recombination.  Enabling resets the totals. */
+int psfun_gpu_profile_enable(int on);
+int psfun_gpu_profile_read(int kernel, long long* launches, double* total_ms);
 
 /* ------------------------------------------------------------------------ */
 /* Sparse matrix: replaces the psb_dspmat_type the reference passes to       */

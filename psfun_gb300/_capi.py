@@ -24,6 +24,8 @@ PROTOS = {
     "psfun_gpu_kernel_launches": (C.c_longlong, []),
     "psfun_gpu_set_stream": (C.c_int, [vp]),
     "psfun_gpu_get_stream": (vp, []),
+    "psfun_gpu_profile_enable": (C.c_int, [C.c_int]),
+    "psfun_gpu_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_longlong), dp]),
     "psfun_gpu_csr_create": (C.c_int, [C.c_int64, C.c_int64, ip, ip, dp, C.c_int, C.POINTER(vp)]),
     "psfun_gpu_csr_destroy": (C.c_int, [vp]),
     "psfun_gpu_csr_info": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp]),

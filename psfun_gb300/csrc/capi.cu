@@ -1,4 +1,5 @@
 // capi.cu -- extern "C" entry points of libpsfun_gb300 (see include/psfun_gb300.h).
+#include <algorithm>
 #include <atomic>
 #include <cctype>
 #include <cmath>
@@ -26,6 +27,7 @@ cudaStream_t stream() {
 }
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 void count_launch(int n) { g_launches += n; }
+long long launch_count() { return g_launches.load(); }
 int sm_count() {
   if (!g_sms) {
     int dev = 0;
@@ -72,6 +74,54 @@ static std::string upper_key(const char* what) {
   for (auto& ch : k) ch = (char)toupper((unsigned char)ch);
   while (!k.empty() && k.back() == ' ') k.pop_back();
   return k;
+}
+
+// ---- per-kernel timing ------------------------------------------------------
+static bool g_prof = false;
+struct ProfSlot {
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  size_t next = 0;
+  long long count = 0;
+  double total_ms = 0.0;
+};
+static ProfSlot g_slots[PROF_N];
+static cudaEvent_t prof_event(ProfSlot& sl) {
+  if (sl.next == sl.pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    sl.pool.push_back(e);
+  }
+  return sl.pool[sl.next++];
+}
+bool prof_enabled() { return g_prof; }
+void prof_begin(int k, cudaStream_t s) {
+  if (!g_prof) return;
+  ProfSlot& sl = g_slots[k];
+  cudaEvent_t e = prof_event(sl);
+  cudaEventRecord(e, s);
+  sl.pending.push_back({e, nullptr});
+}
+void prof_end(int k, cudaStream_t s) {
+  if (!g_prof) return;
+  ProfSlot& sl = g_slots[k];
+  cudaEvent_t e = prof_event(sl);
+  cudaEventRecord(e, s);
+  if (!sl.pending.empty()) sl.pending.back().second = e;
+}
+void prof_collect() {
+  if (!g_prof) return;
+  for (auto& sl : g_slots) {
+    for (auto& pr : sl.pending) {
+      float ms = 0.f;
+      if (pr.second && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+        sl.total_ms += ms;
+        sl.count += 1;
+      }
+    }
+    sl.pending.clear();
+    sl.next = 0;
+  }
 }
 
 bool parse_fun(const psfun_serial* fun, FunParams* fp) {
@@ -123,6 +173,24 @@ int psfun_gpu_set_stream(void* s) {
   return PSFUN_SUCCESS;
 }
 void* psfun_gpu_get_stream(void) { return (void*)stream(); }
+
+int psfun_gpu_profile_enable(int on) {
+  g_prof = (on != 0);
+  for (auto& sl : g_slots) {
+    sl.count = 0;
+    sl.total_ms = 0.0;
+    sl.pending.clear();
+    sl.next = 0;
+  }
+  return PSFUN_SUCCESS;
+}
+
+int psfun_gpu_profile_read(int kernel, long long* launches, double* total_ms) {
+  if (kernel < 0 || kernel >= PROF_N) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (launches) *launches = g_slots[kernel].count;
+  if (total_ms) *total_ms = g_slots[kernel].total_ms;
+  return PSFUN_SUCCESS;
+}
 
 // ---- CSR ------------------------------------------------------------------
 int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32_t* ja, const double* val,
@@ -182,6 +250,12 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
   }
   tiles.push_back((int32_t)n);
   a->ntiles = (int32_t)tiles.size() - 1;
+  std::vector<int2> tdesc(tiles.size());
+  for (size_t t = 0; t < tiles.size(); ++t) {
+    tdesc[t].x = tiles[t];
+    tdesc[t].y = hirp[tiles[t]];
+    if (t + 1 < tiles.size()) a->max_tile_rows = std::max<int32_t>(a->max_tile_rows, tiles[t + 1] - tiles[t]);
+  }
   // norms and diagonal
   double ninf = 0.0;
   a->h_diag.assign(n, 0.0);
@@ -206,6 +280,12 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
   if ((e = cudaMalloc(&a->ja, sizeof(int32_t) * (nnz + 16))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&a->val, sizeof(double) * (nnz + 8))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&a->tile_row, sizeof(int32_t) * tiles.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->sched, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->tile_desc, sizeof(int2) * tdesc.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMemcpyAsync(a->tile_desc, tdesc.data(), sizeof(int2) * tdesc.size(), cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return fail(e);
+  cudaMemsetAsync(a->sched, 0, 4 * sizeof(unsigned), s);
   cudaMemsetAsync(a->ja, 0, sizeof(int32_t) * (nnz + 16), s);
   cudaMemsetAsync(a->val, 0, sizeof(double) * (nnz + 8), s);
   if ((e = cudaMemcpyAsync(a->irp, hirp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess)
@@ -231,6 +311,8 @@ int psfun_gpu_csr_destroy(psfun_csr* a) {
   if (a->val) cudaFree(a->val);
   if (a->tile_row) cudaFree(a->tile_row);
   if (a->diag_inv) cudaFree(a->diag_inv);
+  if (a->sched) cudaFree(a->sched);
+  if (a->tile_desc) cudaFree(a->tile_desc);
   delete a;
   return PSFUN_SUCCESS;
 }
@@ -249,10 +331,11 @@ int psfun_gpu_csr_info(const psfun_csr* a, int64_t* n, int64_t* nnz, int64_t* nt
 namespace psf {
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_axpby(CsrDev A, const double* x, double alpha, double beta,
                                                              double* y, int* err) {
-  __shared__ SpmvSmem sm;
+  PSF_SPMV_SMEM();
   spmv_smem_init(sm);
   EpiAxpby epi{alpha, beta, y};
-  spmv_tiles(A, x, epi, sm, err, blockIdx.x, gridDim.x);
+  spmv_tiles(A, x, epi, sm, err);
+  spmv_sched_done(A);
 }
 
 int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
@@ -261,10 +344,12 @@ int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double
   cudaStream_t s = stream();
   PSF_CUDA(cudaMemsetAsync(errbuf.ptr, 0, sizeof(int), s));
   if (a->ntiles > 0) {
+    static bool attr = false;
+    if (!attr) { spmv_smem_attr(k_spmv_axpby); attr = true; }
     int g = a->ntiles;
-    const int cap = sm_count() * 8;
+    const int cap = sm_count() * 4;
     if (g > cap) g = cap;
-    k_spmv_axpby<<<g, kSpmvThreads, 0, s>>>(a->dev(), x, alpha, beta, y, errbuf.as<int>());
+    k_spmv_axpby<<<g, kSpmvThreads, kSpmvSmemBytes, s>>>(a->dev(), x, alpha, beta, y, errbuf.as<int>());
     count_launch();
     PSF_CUDA(cudaGetLastError());
   }
@@ -436,6 +521,7 @@ int psfun_gpu_krylov_destroy(psfun_krylov* meth) {
   meth->partials.release();
   meth->ctrl.release();
   meth->xy.release();
+  if (meth->graph) cudaGraphExecDestroy(meth->graph);
   delete meth;
   return PSFUN_SUCCESS;
 }

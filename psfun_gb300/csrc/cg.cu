@@ -56,12 +56,13 @@ struct EpiResid {
 };
 
 __global__ void __launch_bounds__(kSpmvThreads) k_cg_restart(CgState st, CsrDev A) {
-  __shared__ SpmvSmem sm;
+  PSF_SPMV_SMEM();
   CgCtrl* c = st.c;
   if (c->done) return;
   spmv_smem_init(sm);
   EpiResid epi{&st, 0.0};
-  spmv_tiles(A, st.x, epi, sm, &c->err, blockIdx.x, gridDim.x);
+  spmv_tiles(A, st.x, epi, sm, &c->err);
+  spmv_sched_done(A);
   const double acc = block_sum(epi.acc, sm.red);
   last_block_reduce(acc, st.part, &c->cnt0, sm.red, [&](double tot) {
     c->brk = 0;
@@ -84,12 +85,13 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_p(CgState st) {
 
 // q = eta A p + zeta p ; sigma = p.q ; alpha = rho/sigma  (:302-310)
 __global__ void __launch_bounds__(kSpmvThreads) k_cg_q(CgState st, CsrDev A) {
-  __shared__ SpmvSmem sm;
+  PSF_SPMV_SMEM();
   CgCtrl* c = st.c;
   if (c->done || c->brk) return;
   spmv_smem_init(sm);
   EpiShiftDot epi{st.eta, st.zeta, st.p, st.q, 0.0};
-  spmv_tiles(A, st.p, epi, sm, &c->err, blockIdx.x, gridDim.x);
+  spmv_tiles(A, st.p, epi, sm, &c->err);
+  spmv_sched_done(A);
   const double acc = block_sum(epi.acc, sm.red);
   last_block_reduce(acc, st.part, &c->cnt0, sm.red, [&](double tot) {
     c->it += 1;
@@ -288,7 +290,9 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   h0.errden = 1.0;
   PSF_CUDA(cudaMemcpyAsync(st.c, &h0, sizeof h0, cudaMemcpyHostToDevice, s));
   const int gv = std::max(1, std::min<int>((int)((n + kCgThreads - 1) / kCgThreads), sm_count() * 8));
-  const int gs = std::max(1, std::min<int>(a->ntiles, sm_count() * 8));
+  static bool attr = false;
+  if (!attr) { spmv_smem_attr(k_cg_restart); spmv_smem_attr(k_cg_q); attr = true; }
+  const int gs = std::max(1, std::min<int>(a->ntiles, sm_count() * 4));
   k_cg_bnorm<<<gv, kCgThreads, 0, s>>>(st);
   k_cg_bnorm_fin<<<1, kCgThreads, 0, s>>>(st, gv);
   count_launch(2);
@@ -296,14 +300,14 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   int itx_host = 0;
   while (itx_host < itmax) {  // restart loop (:252-253)
     hflag[2] = 0;
-    k_cg_restart<<<gs, kSpmvThreads, 0, s>>>(st, A);
+    k_cg_restart<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
     count_launch();
     PSF_CUDA(cudaGetLastError());
     // enqueue iterations ahead of the device; device flags end them
     for (int k = itx_host; k <= itmax + 1; ++k) {
       if (hflag[0] || hflag[2]) break;
       k_cg_p<<<gv, kCgThreads, 0, s>>>(st);
-      k_cg_q<<<gs, kSpmvThreads, 0, s>>>(st, A);
+      k_cg_q<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
       k_cg_xr<<<gv, kCgThreads, 0, s>>>(st);
       count_launch(3);
       for (long spin = 0; k - hflag[1] > 32 && !hflag[0] && !hflag[2]; ++spin) {

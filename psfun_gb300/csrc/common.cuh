@@ -190,6 +190,22 @@ PSF_DEVINL void bulk_g2s(void* dst_smem, const void* src_gmem, unsigned bytes, u
 
 PSF_DEVINL void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// v * 2^k, exact.  For a normal v whose scaled value stays normal the scaling
+// is an integer add on the exponent field (INT pipe, no FP64 instruction);
+// zeros, subnormals, Inf/NaN and out-of-range results take an exact multiply.
+PSF_DEVINL double scale_pow2(double v, int k) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const int ek = ex + k;
+  if (ex > 0 && ex < 0x7ff && ek > 0 && ek < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
+  return v * ldexp(1.0, k);
+}
+
+// floor(log2(|x|)) of a normal, finite, nonzero x (integer extraction).
+PSF_DEVINL int ilog2_normal(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+}
+
 // Streaming loads that should not displace reused data in L1.
 PSF_DEVINL double ld_stream(const double* p) {
   double v;

@@ -16,6 +16,7 @@ namespace psf {
 cudaStream_t stream();
 void set_last_error(const std::string& msg);
 void count_launch(int n = 1);
+long long launch_count();
 int sm_count();
 
 // CUDA call -> status code, recording the message.
@@ -76,10 +77,15 @@ struct psfun_csr {
   int32_t ntiles = 0;
   double norm_inf = 0.0;
   double* diag_inv = nullptr;  // Jacobi preconditioner (lazy)
+  unsigned* sched = nullptr;   // SpMV tile work counter + blocks-done counter (zero between launches)
+  int2* tile_desc = nullptr;   // per tile {first row, first stored entry}, ntiles + 1 entries
+  int32_t max_tile_rows = 0;
   std::vector<double> h_diag;  // diagonal of A (host copy, for DIAG)
   psf::CsrDev dev() const {
     psf::CsrDev d;
     d.n = n; d.nnz = nnz; d.irp = irp; d.ja = ja; d.val = val; d.tile_row = tile_row; d.ntiles = ntiles;
+    d.sched = sched;
+    d.tile_desc = tile_desc;
     return d;
   }
 };
@@ -103,6 +109,11 @@ struct psfun_krylov {
   psf::DevBuf V, u, small, scratch, partials, ctrl, xy;
   int64_t ldv = 0;
   int nl_cap = 0;
+  // CUDA graph of a whole fixed-length (istop = 2) solve, replayed while the
+  // launch key is unchanged
+  cudaGraphExec_t graph = nullptr;
+  std::vector<unsigned char> graph_key;
+  int graph_kernels = 0;  // kernel nodes in the graph (launch accounting)
 };
 
 namespace psf {
@@ -121,4 +132,12 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                       const double* x, double* y, double eps, int itmax, int* iter, double* err);
 int userf_eval(psfun_userf f, double scaling, const double* w_dev, double* fv_dev, int m);
+
+// Optional per-kernel timing: CUDA events recorded around selected launches
+// on the launching stream, accumulated when the solve synchronises.
+enum ProfKernel { PROF_LZ_SPMV = 0, PROF_LZ_UPDATE, PROF_AR_SPMV, PROF_AR_MGS, PROF_FINAL, PROF_RECOMBINE, PROF_N };
+bool prof_enabled();
+void prof_begin(int kernel, cudaStream_t s);
+void prof_end(int kernel, cudaStream_t s);
+void prof_collect();  // call after the stream has synchronised
 }  // namespace psf

@@ -57,6 +57,20 @@ constexpr int kMgsThreads = 1024;
 // kernels
 // ---------------------------------------------------------------------------
 
+// Resets the solve state (capturable: no host memory involved).
+__global__ void k_reset(KState st, size_t small_doubles) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < small_doubles; t += (size_t)gridDim.x * blockDim.x)
+    st.H[t] = 0.0;  // H, s, rs, yk, e1, coef are contiguous from st.H
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    KCtrl* c = st.ctrl;
+    c->done = c->conv = c->breakdown = c->itx = c->yk_len = c->nterms = c->err = c->info = 0;
+    c->bar_count = c->bar_gen = c->red_counter = c->red_counter2 = 0u;
+    c->beta0 = c->errnum = c->c1 = c->c2 = c->derr = 0.0;
+    c->errden = 1.0;
+  }
+}
+__global__ void k_set_e1(KState st) { st.e1[0] = 1.0; }
+
 // W_1 = x ; beta0 = ||x|| ; s_1 = 1/beta0  (psfun_d_arnoldi.f90:183-197)
 __global__ void __launch_bounds__(kVecThreads) k_init(KState st, const double* __restrict__ x) {
   __shared__ double red[32];
@@ -82,9 +96,11 @@ __global__ void __launch_bounds__(kVecThreads) k_init(KState st, const double* _
   });
 }
 
-// Lanczos: u = A v_i and alpha_i = u . v_i   (psfun_d_lanczos.f90:198-204, :239-246)
+// Lanczos: u = A W_i and alpha_i = v_i . A v_i = s_i^2 (W_i . u)
+// (psfun_d_lanczos.f90:198-204, :239-246).  u stays unscaled; s_i is folded
+// into alpha and into the update coefficients.
 __global__ void __launch_bounds__(kSpmvThreads) k_lz_spmv(KState st, CsrDev A, int i) {
-  __shared__ SpmvSmem sm;
+  PSF_SPMV_SMEM();
   KCtrl* c = st.ctrl;
   if (c->done) return;
   if (c->breakdown) {  // |beta_i| < 1e-16 found by the previous update: exit at the top of iteration i
@@ -97,25 +113,32 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_spmv(KState st, CsrDev A, i
   spmv_smem_init(sm);
   const double sc = st.s[i];
   const double* wi = WAT(st, i);
-  EpiScaleDot epi{sc, st.u, wi, 0.0};
-  spmv_tiles(A, wi, epi, sm, &c->err, blockIdx.x, gridDim.x);
+  EpiDot epi{st.u, wi, 0.0};
+  spmv_tiles(A, wi, epi, sm, &c->err);
+  spmv_sched_done(A);
   const double acc = block_sum(epi.acc, sm.red);
   last_block_reduce(acc, st.partials, &c->red_counter, sm.red, [&](double tot) {
-    const double alpha = sc * tot;
+    const double alpha = sc * sc * tot;
     HAT(st, i, i) = alpha;
-    c->c1 = alpha * sc;
-    c->c2 = (i >= 2) ? HAT(st, i - 1, i) * st.s[i - 1] : 0.0;
+    // w = s_i (u - alpha W_i - (beta_i s_{i-1} / s_i) W_{i-1})
+    c->c1 = alpha;
+    c->c2 = (i >= 2) ? HAT(st, i - 1, i) * st.s[i - 1] / sc : 0.0;
     if (i >= 2) c->itx = i - 1;
   });
 }
 
-// Lanczos: w = u - alpha_i v_i - beta_i v_{i-1}, beta_{i+1} = ||w||
-// (psfun_d_lanczos.f90:212, :221-230, :254-266)
-__global__ void __launch_bounds__(kVecThreads) k_lz_update(KState st, int i) {
+// Lanczos: w = A v_i - alpha_i v_i - beta_i v_{i-1} = s_i w' with
+// w' = u - alpha_i W_i - (beta_i s_{i-1}/s_i) W_{i-1}; stored as
+// W_{i+1} = 2^k w', 2^k the power of two nearest below s_i, so the stored
+// vectors keep norms of order ||A|| (the power-of-two scaling is exact and
+// costs no FP64 instruction).  beta_{i+1} = ||w|| = s_i ||w'||,
+// s_{i+1} = 1 / (2^k ||w'||).  (psfun_d_lanczos.f90:212, :221-230, :254-266)
+__global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) {
   __shared__ double red[32];
   KCtrl* c = st.ctrl;
   if (c->done) return;
   const double c1 = c->c1, c2 = c->c2;
+  const int k2 = ilog2_normal(st.s[i]);
   const double* __restrict__ u = st.u;
   const double* __restrict__ wi = WAT(st, i);
   const double* __restrict__ wm = (i >= 2) ? WAT(st, i - 1) : wi;
@@ -127,25 +150,28 @@ __global__ void __launch_bounds__(kVecThreads) k_lz_update(KState st, int i) {
     const double2 uu = reinterpret_cast<const double2*>(u)[p];
     const double2 a = reinterpret_cast<const double2*>(wi)[p];
     const double2 b = reinterpret_cast<const double2*>(wm)[p];
+    const double w0 = fma(-c2, b.x, fma(-c1, a.x, uu.x));
+    const double w1 = fma(-c2, b.y, fma(-c1, a.y, uu.y));
+    acc = fma(w0, w0, acc);
+    acc = fma(w1, w1, acc);
     double2 w;
-    w.x = fma(-c2, b.x, fma(-c1, a.x, uu.x));
-    w.y = fma(-c2, b.y, fma(-c1, a.y, uu.y));
+    w.x = scale_pow2(w0, k2);
+    w.y = scale_pow2(w1, k2);
     reinterpret_cast<double2*>(wo)[p] = w;
-    acc = fma(w.x, w.x, acc);
-    acc = fma(w.y, w.y, acc);
   }
   if ((st.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     const int64_t r = st.n - 1;
     const double w = fma(-c2, wm[r], fma(-c1, wi[r], u[r]));
-    wo[r] = w;
+    wo[r] = scale_pow2(w, k2);
     acc = fma(w, w, acc);
   }
   acc = block_sum(acc, red);
   last_block_reduce(acc, st.partials, &c->red_counter, red, [&](double tot) {
-    const double b = sqrt(tot);
+    const double wn = sqrt(tot);
+    const double b = st.s[i] * wn;
     HAT(st, i, i + 1) = b;
     HAT(st, i + 1, i) = b;
-    st.s[i + 1] = 1.0 / b;
+    st.s[i + 1] = 1.0 / ldexp(wn, k2);
     if (i + 1 <= st.nl && fabs(b) < 1e-16) {  // checked at the top of iteration i+1
       c->breakdown = 1;
       c->itx = i;
@@ -154,14 +180,145 @@ __global__ void __launch_bounds__(kVecThreads) k_lz_update(KState st, int i) {
   });
 }
 
+// ---------------------------------------------------------------------------
+// Persistent Lanczos: steps [i_begin, i_end) in one cooperative launch.
+// Each CTA owns a contiguous range of row tiles (static schedule: the tile
+// after next is staged by TMA while the current one is computed).  Per step:
+//   phase 1  u = A W_i on the CTA's rows, partial W_i . u
+//   barrier  every CTA sums the partials in the same order -> alpha_i
+//   phase 2  W_{i+1} = 2^k (u - alpha W_i - c2 W_{i-1}), partial ||.||^2
+//   barrier  every CTA sums -> beta_{i+1}, s_{i+1}
+// Every CTA derives the scalars itself, so none is re-read from memory, and
+// CTA 0 records H, s and itx for the estimate / final kernels.
+// ---------------------------------------------------------------------------
+PSF_DEVINL bool lz_phase1(const CsrDev& A, const double* __restrict__ x, int t0, int t1, SpmvSmem& sm,
+                          double* __restrict__ u, double& acc, int* err) {
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 2; ++q) {
+      const int t = t0 + q;
+      if (t < t1) {
+        const TileInfo ti = tile_info(A, t);
+        if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue(A, ti, sm, q);
+      }
+    }
+  }
+  for (int t = t0; t < t1; ++t) {
+    const int b = (t - t0) & 1;
+    const TileInfo ti = tile_info(A, t);
+    if (ti.k1 - ti.k0 > kTileNnz) {
+      double s = 0.0;
+      for (int k = ti.k0 + threadIdx.x; k < ti.k1; k += blockDim.x) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
+      s = block_sum(s, sm.red);
+      if (threadIdx.x == 0) {
+        u[ti.r0] = s;
+        acc = fma(s, x[ti.r0], acc);
+      }
+    } else {
+      const bool ok = mbar_wait(&sm.bar[b], sm.phase[b]);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, DEVERR_TIMEOUT);
+        mbar_wait(&sm.bar[b], sm.phase[b]);
+        mbar_wait(&sm.bar[b ^ 1], sm.phase[b ^ 1]);
+        return false;
+      }
+      const SpmvTile& tb = sm.buf[b];
+      const int nr = ti.r1 - ti.r0;
+      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+        const int r = ti.r0 + lr;
+        const double s = spmv_row(tb, ti, lr, x);
+        u[r] = s;
+        acc = fma(s, __ldg(x + r), acc);
+      }
+      if (threadIdx.x == 0) sm.phase[b] ^= 1u;
+    }
+    __syncthreads();  // buffer b is free
+    if (threadIdx.x == 0 && t + 2 < t1) {
+      const TileInfo tj = tile_info(A, t + 2);
+      if (tj.k1 - tj.k0 <= kTileNnz) spmv_issue(A, tj, sm, b);
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A, int i_begin, int i_end,
+                                                             int tiles_per_cta) {
+  PSF_SPMV_SMEM();
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  if (c->breakdown) {  // found by the previous launch: exit at the top of iteration i_begin
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      c->done = 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+    return;
+  }
+  spmv_smem_init(sm);
+  const int G = gridDim.x, bid = blockIdx.x;
+  const int t0 = min(A.ntiles, bid * tiles_per_cta);
+  const int t1 = min(A.ntiles, t0 + tiles_per_cta);
+  const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
+  double sc = st.s[i_begin];
+  double sprev = (i_begin >= 2) ? st.s[i_begin - 1] : 0.0;
+  double beta_i = (i_begin >= 2) ? HAT(st, i_begin - 1, i_begin) : 0.0;
+  double* __restrict__ u = st.u;
+  for (int i = i_begin; i < i_end; ++i) {
+    const double* __restrict__ wi = WAT(st, i);
+    // ---- phase 1
+    double acc = 0.0;
+    lz_phase1(A, wi, t0, t1, sm, u, acc, &c->err);
+    acc = block_sum(acc, sm.red);
+    if (threadIdx.x == 0) st.partials[bid] = acc;
+    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+    const double alpha = sc * sc * block_sum_array(st.partials, G, sm.red);
+    const double c2 = (i >= 2) ? beta_i * sprev / sc : 0.0;
+    if (bid == 0 && threadIdx.x == 0) {
+      HAT(st, i, i) = alpha;
+      if (i >= 2) c->itx = i - 1;
+    }
+    // ---- phase 2
+    const int k2 = ilog2_normal(sc);
+    const double* __restrict__ wm = (i >= 2) ? WAT(st, i - 1) : wi;
+    double* __restrict__ wo = WAT(st, i + 1);
+    double acc2 = 0.0;
+    for (int r = rb + threadIdx.x; r < re; r += blockDim.x) {
+      const double w = fma(-c2, wm[r], fma(-alpha, wi[r], u[r]));
+      acc2 = fma(w, w, acc2);
+      wo[r] = scale_pow2(w, k2);
+    }
+    acc2 = block_sum(acc2, sm.red);
+    if (threadIdx.x == 0) st.partials[G + bid] = acc2;
+    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+    const double wn = sqrt(block_sum_array(st.partials + G, G, sm.red));
+    const double beta = sc * wn;
+    const double snext = 1.0 / ldexp(wn, k2);
+    if (bid == 0 && threadIdx.x == 0) {
+      HAT(st, i, i + 1) = beta;
+      HAT(st, i + 1, i) = beta;
+      st.s[i + 1] = snext;
+      if (st.host_flag) st.host_flag[1] = i;
+    }
+    if (i + 1 <= st.nl && fabs(beta) < 1e-16) {  // checked at the top of iteration i+1
+      if (bid == 0 && threadIdx.x == 0) {
+        c->breakdown = 1;
+        c->itx = i;
+      }
+      return;
+    }
+    sprev = sc;
+    sc = snext;
+    beta_i = beta;
+  }
+}
+
 // Arnoldi: w = scaling * A v_{i-1} into slot i   (psfun_d_arnoldi.f90:202)
 __global__ void __launch_bounds__(kSpmvThreads) k_ar_spmv(KState st, CsrDev A, int i, double scaling) {
-  __shared__ SpmvSmem sm;
+  PSF_SPMV_SMEM();
   KCtrl* c = st.ctrl;
   if (c->done || c->breakdown) return;
   spmv_smem_init(sm);
   EpiAxpby epi{scaling * st.s[i - 1], 0.0, WAT(st, i)};
-  spmv_tiles(A, WAT(st, i - 1), epi, sm, &c->err, blockIdx.x, gridDim.x);
+  spmv_tiles(A, WAT(st, i - 1), epi, sm, &c->err);
+  spmv_sched_done(A);
 }
 
 // Arnoldi: modified Gram-Schmidt of slot i against slots 1..i-1, one pass over
@@ -434,6 +591,39 @@ static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder)
   return PSFUN_SUCCESS;
 }
 
+static void spmv_kernel_attrs() {
+  static bool done = false;
+  if (done) return;
+  spmv_smem_attr(k_lz_spmv);
+  spmv_smem_attr(k_ar_spmv);
+  spmv_smem_attr(k_lz_persist);
+  done = true;
+}
+
+// Cooperative grid of the persistent Lanczos kernel: every CTA co-resident.
+static int persist_grid() {
+  static int g = 0;
+  if (g == 0) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lz_persist, kSpmvThreads, kSpmvSmemBytes);
+    if (per < 1) per = 1;
+    g = sm_count() * per;
+  }
+  return g;
+}
+
+static int launch_lz_persist(KState& st, const CsrDev& A, int i_begin, int i_end, cudaStream_t s) {
+  int G = persist_grid();
+  int tpc = (A.ntiles + G - 1) / G;
+  if (tpc < 1) tpc = 1;
+  G = (A.ntiles + tpc - 1) / tpc;
+  if (G < 1) G = 1;
+  void* args[] = {(void*)&st, (void*)&A, (void*)&i_begin, (void*)&i_end, (void*)&tpc};
+  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_lz_persist, dim3(G), dim3(kSpmvThreads), args, kSpmvSmemBytes, s));
+  count_launch();
+  return PSFUN_SUCCESS;
+}
+
 static int grid_for(int64_t items, int threads, int per_sm) {
   int64_t g = (items + threads - 1) / threads;
   const int64_t cap = (int64_t)sm_count() * per_sm;
@@ -512,16 +702,6 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   st.ework = st.fscratch + fh_scratch_doubles(nl + 1, fp.phiorder);
   st.host_flag = nullptr;
 
-  // reset the solve state
-  PSF_CUDA(cudaMemsetAsync(sm, 0, meth->small.bytes, s));
-  KCtrl h0;
-  memset(&h0, 0, sizeof h0);
-  h0.errnum = 0.0;
-  h0.errden = 1.0;
-  PSF_CUDA(cudaMemcpyAsync(st.ctrl, &h0, sizeof h0, cudaMemcpyHostToDevice, s));
-  const double one = 1.0;
-  PSF_CUDA(cudaMemcpyAsync(st.e1, &one, sizeof(double), cudaMemcpyHostToDevice, s));
-
   // host-visible progress flag for early termination of the enqueue loop
   static volatile int* hflag = nullptr;
   static int* dflag = nullptr;
@@ -536,77 +716,142 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   st.host_flag = dflag;
 
   const CsrDev A = a->dev();
-  const int gv = grid_for(n, kVecThreads, 8);
-  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 8);
+  spmv_kernel_attrs();
+  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
+  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
   const int gm = mgs_grid();
   const int tridiag = arnoldi ? 0 : 1;
+  const size_t small_doubles = meth->small.bytes / sizeof(double);
 
-  k_init<<<gv, kVecThreads, 0, s>>>(st, x);
-  count_launch();
-  if (!arnoldi) {
-    k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, 1);
-    k_lz_update<<<gv, kVecThreads, 0, s>>>(st, 1);
-    count_launch(2);
-  }
-  PSF_CUDA(cudaGetLastError());
-  const int max_ahead = 24;
-  for (int i = 2; i <= nl; ++i) {
-    if (istop == 1 && hflag[0]) break;
+  // Lanczos prologue (psfun_d_lanczos.f90:183-217) = step 1 of the persistent kernel.
+  auto enqueue_prologue = [&](bool lz_step1) -> int {
+    k_reset<<<64, 256, 0, s>>>(st, small_doubles);
+    k_set_e1<<<1, 1, 0, s>>>(st);
+    k_init<<<gv, kVecThreads, 0, s>>>(st, x);
+    count_launch(3);
+    PSF_CUDA(cudaGetLastError());
+    if (!arnoldi && lz_step1) {
+      prof_begin(PROF_LZ_SPMV, s);
+      PSF_TRY(launch_lz_persist(st, A, 1, 2, s));
+      prof_end(PROF_LZ_SPMV, s);
+    }
+    return PSFUN_SUCCESS;
+  };
+  auto enqueue_step = [&](int i) -> int {
     if (arnoldi) {
-      k_ar_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i, scaling);
+      prof_begin(PROF_AR_SPMV, s);
+      k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
+      prof_end(PROF_AR_SPMV, s);
       void* args[] = {(void*)&st, (void*)&i};
+      prof_begin(PROF_AR_MGS, s);
       PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
+      prof_end(PROF_AR_MGS, s);
       count_launch(2);
     } else {
-      k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i);
-      k_lz_update<<<gv, kVecThreads, 0, s>>>(st, i);
-      count_launch(2);
-    }
-    if (istop == 1) {
-      if (userf) {
-        // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
-        PSF_CUDA(cudaStreamSynchronize(s));
-        KCtrl hc;
-        PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
-        if (hc.done) break;
-        PSF_TRY(userf_apply(fun->f_ptr, 1.0, i - 1, st.H, st.ldh, st.e1, st.yk, st.ework));
-        k_estimate_tail<<<1, kDenseThreads, 0, s>>>(st, i, eps);
-        count_launch();
-      } else {
-        k_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, tridiag);
-        count_launch();
-      }
+      prof_begin(PROF_LZ_SPMV, s);
+      PSF_TRY(launch_lz_persist(st, A, i, i + 1, s));
+      prof_end(PROF_LZ_SPMV, s);
     }
     PSF_CUDA(cudaGetLastError());
-    // keep at most max_ahead steps queued ahead of the device
-    if (istop == 1 && !userf) {
-      for (long spin = 0; i - hflag[1] > max_ahead && !hflag[0]; ++spin) {
-        if (cudaStreamQuery(s) == cudaSuccess) break;
-        if (spin > 200000000L) break;
+    return PSFUN_SUCCESS;
+  };
+  auto enqueue_epilogue = [&](int mode) -> int {
+    prof_begin(PROF_FINAL, s);
+    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, mode);
+    prof_end(PROF_FINAL, s);
+    prof_begin(PROF_RECOMBINE, s);
+    k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
+    prof_end(PROF_RECOMBINE, s);
+    count_launch(2);
+    PSF_CUDA(cudaGetLastError());
+    return PSFUN_SUCCESS;
+  };
+
+  if (istop == 2 && !userf && !prof_enabled()) {
+    // fixed-length solve: one CUDA graph, captured once per launch key
+    struct Key {
+      const void* a; const void* x; void* y; const void* V; int64_t n; int nl, arnoldi, keeplast, gs, gv, gm;
+      FunParams fp; double scaling;
+    } key;
+    memset(&key, 0, sizeof key);
+    key.a = a; key.x = x; key.y = y; key.V = st.V; key.n = n; key.nl = nl; key.arnoldi = arnoldi;
+    key.keeplast = meth->keeplast; key.gs = gs; key.gv = gv; key.gm = gm; key.fp = fpk; key.scaling = scaling;
+    const unsigned char* kb = reinterpret_cast<const unsigned char*>(&key);
+    std::vector<unsigned char> kv(kb, kb + sizeof key);
+    if (!meth->graph || meth->graph_key != kv) {
+      if (meth->graph) { cudaGraphExecDestroy(meth->graph); meth->graph = nullptr; }
+      cudaGraph_t g = nullptr;
+      const long long l0 = launch_count();
+      PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_prologue(false);
+      if (!arnoldi) {
+        if (rc == PSFUN_SUCCESS) rc = launch_lz_persist(st, A, 1, nl + 1, s);  // every step, one launch
+      } else {
+        for (int i = 2; i <= nl && rc == PSFUN_SUCCESS; ++i) rc = enqueue_step(i);
+      }
+      if (rc == PSFUN_SUCCESS) rc = enqueue_epilogue(0);
+      cudaError_t ec = cudaStreamEndCapture(s, &g);
+      if (rc != PSFUN_SUCCESS) { if (g) cudaGraphDestroy(g); return rc; }
+      PSF_CUDA(ec);
+      cudaError_t ei = cudaGraphInstantiate(&meth->graph, g, 0);
+      cudaGraphDestroy(g);
+      PSF_CUDA(ei);
+      meth->graph_key = kv;
+      meth->graph_kernels = (int)(launch_count() - l0);
+      count_launch(-meth->graph_kernels);  // captured, not launched
+    }
+    PSF_CUDA(cudaGraphLaunch(meth->graph, s));
+    count_launch(meth->graph_kernels);
+  } else {
+    PSF_TRY(enqueue_prologue(true));
+    const int max_ahead = 24;
+    for (int i = 2; i <= nl; ++i) {
+      if (istop == 1 && hflag[0]) break;
+      PSF_TRY(enqueue_step(i));
+      if (istop == 1) {
+        if (userf) {
+          // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
+          PSF_CUDA(cudaStreamSynchronize(s));
+          KCtrl hc;
+          PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
+          if (hc.done) break;
+          PSF_TRY(userf_apply(fun->f_ptr, 1.0, i - 1, st.H, st.ldh, st.e1, st.yk, st.ework));
+          k_estimate_tail<<<1, kDenseThreads, 0, s>>>(st, i, eps);
+          count_launch();
+        } else {
+          k_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, tridiag);
+          count_launch();
+        }
+      }
+      PSF_CUDA(cudaGetLastError());
+      // keep at most max_ahead steps queued ahead of the device
+      if (istop == 1 && !userf) {
+        for (long spin = 0; i - hflag[1] > max_ahead && !hflag[0]; ++spin) {
+          if (cudaStreamQuery(s) == cudaSuccess) break;
+          if (spin > 200000000L) break;
+        }
       }
     }
-  }
-  if (userf) {
-    PSF_CUDA(cudaStreamSynchronize(s));
-    KCtrl hc;
-    PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
-    if (hc.info == 0 && hc.beta0 != 0.0 && !hc.conv) {
-      const int m = (arnoldi && hc.breakdown) ? hc.itx : hc.itx - 1;
-      if (m >= 1) PSF_TRY(userf_apply(fun->f_ptr, 1.0, m, st.H, st.ldh, st.e1, st.yk, st.ework));
+    if (userf) {
+      PSF_CUDA(cudaStreamSynchronize(s));
+      KCtrl hc;
+      PSF_CUDA(cudaMemcpy(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost));
+      if (hc.info == 0 && hc.beta0 != 0.0 && !hc.conv) {
+        const int m = (arnoldi && hc.breakdown) ? hc.itx : hc.itx - 1;
+        if (m >= 1) PSF_TRY(userf_apply(fun->f_ptr, 1.0, m, st.H, st.ldh, st.e1, st.yk, st.ework));
+      }
+      PSF_TRY(enqueue_epilogue(1));
+    } else {
+      PSF_TRY(enqueue_epilogue(0));
     }
-    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, 1);
-  } else {
-    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, 0);
   }
-  k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
-  count_launch(2);
-  PSF_CUDA(cudaGetLastError());
 
   KCtrl hc;
   PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
   std::vector<double> hrs(nl + 1);
   PSF_CUDA(cudaMemcpyAsync(hrs.data(), st.rs, sizeof(double) * (nl + 1), cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
+  prof_collect();
   if (hc.err & DEVERR_TIMEOUT) {
     set_last_error("device-side wait timed out");
     return PSFUN_ERR_DEVICE_TIMEOUT;
@@ -885,13 +1130,14 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   st.host_flag = dflag;
 
   const CsrDev A = a->dev();
-  const int gv = grid_for(n, kVecThreads, 8);
-  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 8);
+  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  spmv_kernel_attrs();
+  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
   k_init<<<gv, kVecThreads, 0, s>>>(st, x);
   count_launch();
   for (int i = 1; i <= nl; ++i) {
     if (hflag[0]) break;
-    k_lz_spmv<<<gs, kSpmvThreads, 0, s>>>(st, A, i);
+    k_lz_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i);
     k_lz_update<<<gv, kVecThreads, 0, s>>>(st, i);
     k_ms_monitor<<<1, 256, 0, s>>>(st, mp, i);
     count_launch(3);

@@ -19,9 +19,9 @@
 
 namespace psf {
 
-constexpr int kSpmvThreads = 256;
-constexpr int kTileRows = 256;
-constexpr int kTileNnz = 2048;
+constexpr int kSpmvThreads = 512;
+constexpr int kTileRows = 512;
+constexpr int kTileNnz = 4096;
 static_assert(((kTileNnz + 2) * 8) % 16 == 0, "ja must start 16-byte aligned");
 
 struct CsrDev {
@@ -32,78 +32,177 @@ struct CsrDev {
   const double* __restrict__ val;
   const int32_t* __restrict__ tile_row;  // ntiles + 1
   int32_t ntiles;
+  unsigned* sched;  // [0] next tile, [1] blocks done: zero between launches
+  const int2* __restrict__ tile_desc;  // {first row, first stored entry} per tile (+1 sentinel)
 };
 
-// Bulk-copy destinations must be 16-byte aligned: the struct is 128-byte
-// aligned and ja starts at byte (kTileNnz + 2) * 8, a multiple of 16.
-struct __align__(128) SpmvSmem {
+// One staged tile: values, column indices and the row pointers of its rows.
+// Bulk-copy destinations must be 16-byte aligned: every member size below is
+// a multiple of 16 bytes and the buffer is 128-byte aligned.
+struct __align__(128) SpmvTile {
   double val[kTileNnz + 2];
   int32_t ja[kTileNnz + 4];
-  uint64_t bar;
-  unsigned phase;
+  int32_t irp[kTileRows + 8];
+};
+static_assert(sizeof(double) * (kTileNnz + 2) % 16 == 0, "ja offset");
+static_assert(sizeof(int32_t) * (kTileNnz + 4) % 16 == 0, "irp offset");
+
+struct __align__(128) SpmvSmem {
+  SpmvTile buf[2];
+  uint64_t bar[2];
+  unsigned phase[2];
+  int next_tile;
+  int cur_tile;
   double red[kSpmvThreads / 32];
 };
+
+// Dynamic shared memory of a kernel that runs spmv_tiles (51 KB: above the
+// 48 KB static limit, so kernels declare it with PSF_SPMV_SMEM and launch
+// with kSpmvSmemBytes after psf::spmv_smem_attr()).
+constexpr size_t kSpmvSmemBytes = sizeof(SpmvSmem);
+#define PSF_SPMV_SMEM()                                                  \
+  extern __shared__ __align__(128) unsigned char psf_spmv_smem_raw[];    \
+  ::psf::SpmvSmem& sm = *reinterpret_cast<::psf::SpmvSmem*>(psf_spmv_smem_raw)
+
+template <class K>
+inline void spmv_smem_attr(K kernel) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpmvSmemBytes);
+}
 
 // Once per kernel, before the first spmv_tiles call.
 PSF_DEVINL void spmv_smem_init(SpmvSmem& sm) {
   if (threadIdx.x == 0) {
-    mbar_init(&sm.bar, 1);
-    sm.phase = 0;
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    sm.phase[0] = sm.phase[1] = 0;
   }
   __syncthreads();
 }
 
-// Walks the tiles assigned to this block and calls epi(row, sum) once per row
-// (by exactly one thread).  Returns false if a bounded wait timed out.
+struct TileInfo {
+  int r0, r1, k0, k1, kv0, kj0, ki0;
+};
+
+PSF_DEVINL TileInfo tile_info(const CsrDev& A, int t) {
+  TileInfo ti;
+  const int2 d0 = A.tile_desc[t], d1 = A.tile_desc[t + 1];
+  ti.r0 = d0.x;
+  ti.r1 = d1.x;
+  ti.k0 = d0.y;
+  ti.k1 = d1.y;
+  ti.kv0 = ti.k0 & ~1;
+  ti.kj0 = ti.k0 & ~3;
+  ti.ki0 = ti.r0 & ~3;
+  return ti;
+}
+
+// Thread 0: stage tile t into buffer b (values, indices, row pointers).
+PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, int b) {
+  const unsigned bv = (unsigned)(((ti.k1 - ti.kv0) + 1) & ~1) * 8u;
+  const unsigned bj = (unsigned)(((ti.k1 - ti.kj0) + 3) & ~3) * 4u;
+  const unsigned bi = (unsigned)(((ti.r1 + 1 - ti.ki0) + 3) & ~3) * 4u;
+  fence_proxy_async();
+  mbar_expect_tx(&sm.bar[b], (ti.k1 > ti.k0 ? bv + bj : 0u) + bi);
+  if (ti.k1 > ti.k0) {
+    bulk_g2s(sm.buf[b].val, A.val + ti.kv0, bv, &sm.bar[b]);
+    bulk_g2s(sm.buf[b].ja, A.ja + ti.kj0, bj, &sm.bar[b]);
+  }
+  bulk_g2s(sm.buf[b].irp, A.irp + ti.ki0, bi, &sm.bar[b]);
+}
+
+// Row sum of a staged tile: up to 8 gathers are issued before their FMAs.
+PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x) {
+  const int dj = ti.kv0 - ti.kj0;  // ja index = val index + dj
+  const int di = ti.r0 - ti.ki0;
+  const int kb = tb.irp[lr + di] - ti.kv0;
+  const int ke = tb.irp[lr + di + 1] - ti.kv0;
+  double s = 0.0;
+  for (int k = kb; k < ke; k += 8) {
+    const int cnt = ke - k;
+    double xv[8], vv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q < cnt) {
+        xv[q] = __ldg(x + tb.ja[k + q + dj]);
+        vv[q] = tb.val[k + q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < cnt) s = fma(vv[q], xv[q], s);
+  }
+  return s;
+}
+
+// Walks tiles handed out by a device work counter (A.sched[0]) and calls
+// epi(row, sum) once per row, by exactly one thread.  Two tile buffers: the
+// next tile is staged by TMA while the current one is computed.  The caller
+// must end the kernel with spmv_sched_done().  Returns false if a bounded
+// wait timed out (*err is set).
 template <class Epi>
-PSF_DEVINL bool spmv_tiles(const CsrDev& A, const double* __restrict__ x, Epi& epi, SpmvSmem& sm, int* err,
-                           int first_tile, int tile_stride) {
-  unsigned phase = sm.phase;
-  for (int t = first_tile; t < A.ntiles; t += tile_stride) {
-    const int r0 = A.tile_row[t], r1 = A.tile_row[t + 1];
-    const int k0 = A.irp[r0], k1 = A.irp[r1];
-    const int nnz_t = k1 - k0;
-    if (nnz_t > kTileNnz) {
+PSF_DEVINL bool spmv_tiles(const CsrDev& A, const double* __restrict__ x, Epi& epi, SpmvSmem& sm, int* err) {
+  if (threadIdx.x == 0) sm.next_tile = (int)atomicAdd(&A.sched[0], 1u);
+  __syncthreads();
+  int t = sm.next_tile;
+  __syncthreads();  // everyone has read next_tile before thread 0 overwrites it
+  int b = 0;
+  bool staged = false;  // buffer b holds tile t
+  if (t < A.ntiles && threadIdx.x == 0) {
+    const TileInfo ti = tile_info(A, t);
+    if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue(A, ti, sm, b);
+  }
+  while (t < A.ntiles) {
+    const TileInfo ti = tile_info(A, t);
+    const bool long_row = (ti.k1 - ti.k0) > kTileNnz;
+    staged = !long_row;
+    // claim and stage the next tile into the other buffer
+    if (threadIdx.x == 0) {
+      const int tn = (int)atomicAdd(&A.sched[0], 1u);
+      sm.next_tile = tn;
+      if (tn < A.ntiles) {
+        const TileInfo tj = tile_info(A, tn);
+        if (tj.k1 - tj.k0 <= kTileNnz) spmv_issue(A, tj, sm, b ^ 1);
+      }
+    }
+    if (long_row) {
       // one long row: block-cooperative dot product from global memory
       double s = 0.0;
-      for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
+      for (int k = ti.k0 + threadIdx.x; k < ti.k1; k += blockDim.x) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
       s = block_sum(s, sm.red);
-      if (threadIdx.x == 0) epi(r0, s);
-      __syncthreads();
-      continue;
-    }
-    const int kv0 = k0 & ~1;
-    const int kj0 = k0 & ~3;
-    if (nnz_t > 0) {
-      if (threadIdx.x == 0) {
-        const unsigned bv = (unsigned)(((k1 - kv0) + 1) & ~1) * 8u;
-        const unsigned bj = (unsigned)(((k1 - kj0) + 3) & ~3) * 4u;
-        fence_proxy_async();
-        mbar_expect_tx(&sm.bar, bv + bj);
-        bulk_g2s(sm.val, A.val + kv0, bv, &sm.bar);
-        bulk_g2s(sm.ja, A.ja + kj0, bj, &sm.bar);
-      }
-      const bool ok = mbar_wait(&sm.bar, phase);
+      if (threadIdx.x == 0) epi(ti.r0, s);
+    } else {
+      const bool ok = mbar_wait(&sm.bar[b], sm.phase[b]);
       if (__syncthreads_or(!ok)) {  // block-uniform decision
         if (threadIdx.x == 0) atomicOr(err, DEVERR_TIMEOUT);
-        mbar_wait(&sm.bar, phase);  // let the copy land before the block exits
+        mbar_wait(&sm.bar[b], sm.phase[b]);
+        mbar_wait(&sm.bar[b ^ 1], sm.phase[b ^ 1]);
         return false;
       }
-      phase ^= 1u;
+      const SpmvTile& tb = sm.buf[b];
+      const int nr = ti.r1 - ti.r0;
+      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) epi(ti.r0 + lr, spmv_row(tb, ti, lr, x));
     }
-    const int nr = r1 - r0;
-    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-      const int r = r0 + lr;
-      const int kb = A.irp[r], ke = A.irp[r + 1];
-      double s = 0.0;
-      for (int k = kb; k < ke; ++k) s = fma(sm.val[k - kv0], __ldg(x + sm.ja[k - kj0]), s);
-      epi(r, s);
-    }
-    __syncthreads();
+    if (staged && threadIdx.x == 0) sm.phase[b] ^= 1u;
+    __syncthreads();  // buffer b is free again; next_tile visible
+    t = sm.next_tile;
+    b ^= 1;
   }
-  if (threadIdx.x == 0) sm.phase = phase;
-  __syncthreads();
   return true;
+}
+
+// Every block calls this once at the end of a kernel that used spmv_tiles:
+// the last block to finish resets the work counter for the next launch.
+PSF_DEVINL void spmv_sched_done(const CsrDev& A) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&A.sched[1], 1u);
+    if (prev == gridDim.x - 1) {
+      A.sched[0] = 0u;
+      A.sched[1] = 0u;
+      __threadfence();
+    }
+  }
 }
 
 // y = alpha*A*x + beta*y (psb_spmm); alpha may come from device memory.
@@ -115,16 +214,15 @@ struct EpiAxpby {
   }
 };
 
-// u = sc*A*x with the partial dot sum_r u_r * x_r (Lanczos alpha).
-struct EpiScaleDot {
-  double sc;
+// u = A*x with the partial dot sum_r u_r * x_r (Lanczos alpha; the scale of
+// x is folded into the scalars by the caller).
+struct EpiDot {
   double* __restrict__ u;
   const double* __restrict__ xown;
   double acc;
   PSF_DEVINL void operator()(int r, double s) {
-    const double v = sc * s;
-    u[r] = v;
-    acc = fma(v, xown[r], acc);
+    u[r] = s;
+    acc = fma(s, xown[r], acc);
   }
 };
 

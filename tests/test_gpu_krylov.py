@@ -161,7 +161,21 @@ def test_arnoldi_exact_breakdown_istop1(lib, orc):
     A, x = lanczos_breakdown_case()
     g = run_gpu("ARNOLDI", "EXP", "GENPADE", 1.0, A, x, 1e-14, itmax=10, istop=1)
     o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", 1.0, A, x, 1e-14, itmax=10, istop=1)
-    assert g.info == 0 and o["info"] == 0 and g.iter == o["iter"] and rel(g.y, o["y"]) <= TOL
+    assert g.info == 0 and o["info"] == 0 and g.iter == o["iter"] == 3 and rel(g.y, o["y"]) <= TOL
+    # istop 2: the native path stops at the exact breakdown and uses the whole invariant subspace
+    g2 = run_gpu("ARNOLDI", "EXP", "GENPADE", 1.0, A, x, 1e-14, itmax=10, istop=2)
+    import scipy.linalg as sl
+    ref = sl.expm(A.toarray()) @ x
+    assert g2.info == 0 and g2.iter == 3 and rel(g2.y, ref) < 1e-13
+
+
+def test_null_projected_matrix_is_error(lib):
+    import scipy.sparse as sp
+    A = sp.lil_matrix((5, 5))
+    A[0, 1] = A[1, 0] = 1.0
+    x = np.zeros(5)
+    x[0] = 1.0
+    assert run_gpu("ARNOLDI", "EXP", "GENPADE", 1.0, A.tocsr(), x, 1e-14, itmax=6).info == 4011
 
 
 def test_device_api_matches_host_api(lib):

@@ -80,12 +80,13 @@ def test_zero_vector(orc):
 
 
 def lanczos_breakdown_case():
-    """Path-graph adjacency on nodes 0-1-2 (plus isolated nodes), x = e_1: every
-    Lanczos quantity is exact and beta_4 == 0."""
+    """Path graph on nodes 0-1-2 with unit diagonal (plus isolated nodes), x = e_1:
+    every Krylov quantity is an exact small integer and the fourth basis vector is 0."""
     import scipy.sparse as sp
     n = 20
     A = sp.lil_matrix((n, n))
     A[0, 1] = A[1, 0] = A[1, 2] = A[2, 1] = 1.0
+    A[0, 0] = A[1, 1] = A[2, 2] = 1.0
     for i in range(3, n):
         A[i, i] = float(i)
     x = np.zeros(n)
@@ -100,6 +101,26 @@ def test_lanczos_breakdown(orc):
     r = orc.krylov("LANCZOS", orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-14, itmax=10,
                    istop=2)
     assert r["info"] == 0 and r["iter"] == 3
+
+
+def test_arnoldi_breakdown_istop1(orc):
+    """Arnoldi has no breakdown test: h(4,3) == 0 makes the estimate 0 and the step converges."""
+    A, x = lanczos_breakdown_case()
+    r = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-14, itmax=10)
+    assert r["info"] == 0 and r["iter"] == 3
+    import scipy.linalg as sl
+    assert np.linalg.norm(r["y"][:3] - sl.expm(A.toarray()[:3, :3])[:, 0][:3]) > 0  # reference drops one term
+
+
+def test_null_projected_matrix_is_error(orc):
+    """H(1,1) == 0 with GENPADE: DGPADM stops on a null matrix (dgpadm.f:84); 4011 here."""
+    import scipy.sparse as sp
+    A = sp.lil_matrix((5, 5))
+    A[0, 1] = A[1, 0] = 1.0
+    x = np.zeros(5)
+    x[0] = 1.0
+    r = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A.tocsr()), x, 1e-14, itmax=6)
+    assert r["info"] == 4011
 
 
 def test_lanczos_eigenvector_is_error(orc):
