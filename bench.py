@@ -140,6 +140,66 @@ def cpu_baseline(A, x, budget_s: float = 20.0, max_solves: int = 5):
                       f"DSCHBV, OpenMP over rows), best time {best:.3f} s"}, last
 
 
+def bench_batched(torch, pg, scale: float = 1.0, reps: int = 2):
+    """Config 4: 64 uneven instances x 4 right-hand sides, exp(-t_k A_k) X_k,
+    Lanczos m <= 60, eps 1e-8.  Batched (one persistent launch) against the
+    plain path (one drop-in call per instance and right-hand side)."""
+    from psfun_gb300 import matrices
+    probs = matrices.config4(scale=scale)
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", "CHBSYM")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    items, plain_mats = [], []
+    for p in probs:
+        t = -p.params["t"]
+        X = torch.tensor(p.x, device="cuda")
+        items.append((pg.CsrMatrix.from_scipy(p.A), X, torch.zeros_like(X), t))
+        plain_mats.append(pg.CsrMatrix.from_scipy(t * p.A))
+    npairs = sum(int(X.shape[0]) for _, X, _, _ in items)
+    stream = torch.cuda.current_stream()
+    pg.krylov_batch(meth, fun, items, 1e-8, itmax=60, istop=1)  # autotune + warm
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        info, infos, iters, errs = pg.krylov_batch(meth, fun, items, 1e-8, itmax=60, istop=1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / reps / 1e3
+    assert info == 0, info
+    pmeth = pg.PsfunDKrylov()
+    pmeth.set("KNAME", "LANCZOS")
+    outs = []
+    for (a, X, Y, t), am in zip(items, plain_mats):  # warm
+        pmeth.apply(fun, am, X[0], 1e-8, itmax=60, istop=1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for (a, X, Y, t), am in zip(items, plain_mats):
+        for q in range(X.shape[0]):
+            outs.append(pmeth.apply(fun, am, X[q], 1e-8, itmax=60, istop=1))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) / 1e3
+    worst = 0.0
+    j = 0
+    for (a, X, Y, t) in items:
+        for q in range(X.shape[0]):
+            yp = outs[j].y
+            worst = max(worst, float(torch.linalg.norm(Y[q] - yp) / torch.linalg.norm(yp)))
+            j += 1
+    nnz = sum(p.A.nnz for p in probs)
+    rows = sum(p.A.shape[0] for p in probs)
+    return {"workload": f"64 uneven instances (32 5-pt Laplacians side U[64,512], 32 kNN RGG Laplacians n log-U"
+                        f"[4096,262144]), 4 RHS each, exp(-tA)X, t~U[0.01,1], Lanczos m<=60, eps 1e-8; "
+                        f"rows={rows}, nnz={nnz}",
+            "batched_solves_per_s": npairs / t_batch, "plain_solves_per_s": npairs / t_plain,
+            "speedup_vs_plain": t_plain / t_batch, "batched_ms": 1e3 * t_batch, "plain_ms": 1e3 * t_plain,
+            "max_rel_diff_batched_vs_plain": worst, "mean_iters": float(np.mean(iters)),
+            "max_iters": int(np.max(iters))}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -176,6 +236,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the batched (64-instance) comparison")
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
     args = ap.parse_args()
@@ -315,6 +376,8 @@ def main():
         "gpu_launches": int(launches),
         "accuracy": {"rel_diff_m80_vs_converged": rel_conv},
     }
+    if rank == 0 and world == 1 and not args.no_secondary:
+        line["batched"] = bench_batched(torch, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base, ro = cpu_baseline(A, x)
         line["cpu_baseline"] = base

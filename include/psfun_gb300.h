@@ -179,6 +179,26 @@ int psfun_gpu_z_quadrature_apply_device(psfun_csr* a, int N, const double* xi, c
                                         double sign, const double* x, double* y, double eps, int itmax, int* iter,
                                         double* err);
 
+/* ------------------------------------------------------------------------ */
+/* Batched f(A)X: many uneven instances in one persistent launch (no          */
+/* counterpart in the reference; each instance is what one                    */
+/* psfun_d_krylov%apply with kname 'LANCZOS' computes, per right-hand side).  */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  psfun_csr* a;    /* instance matrix (symmetric) */
+  int nrhs;        /* right-hand sides, 1..4, the same for every item */
+  const double* x; /* device, n x nrhs column-major (rhs j at x + j*n) */
+  double* y;       /* device, n x nrhs column-major */
+  double scaling;  /* t: the item computes f(t A) X */
+} psfun_batch_item;
+/* Lanczos with f = EXP / CHBSYM|CHBGEN on every (item, rhs) pair, one
+ * cooperative launch for the whole batch.  eps/itmax/istop as in
+ * psfun_gpu_d_krylov_apply, for every pair.  iters, errs, infos (may be
+ * NULL) receive count*nrhs entries (item-major).  Returns the first nonzero
+ * pair info, or the launch status. */
+int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count, const psfun_batch_item* items,
+                             double eps, int itmax, int istop, int* iters, double* errs, int* infos);
+
 #ifdef __cplusplus
 }
 #endif

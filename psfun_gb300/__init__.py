@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     ellipj,
     ellipkkp,
     hhtmethod1,
+    krylov_batch,
     horner,
     psb_krylov,
 )

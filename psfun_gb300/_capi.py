@@ -17,6 +17,12 @@ vp = C.c_void_p
 USERF = C.CFUNCTYPE(C.c_double, C.c_double, C.c_int)
 ZFUN = C.CFUNCTYPE(None, dp, dp, C.c_void_p)
 
+class BatchItem(C.Structure):
+    """psfun_batch_item"""
+    _fields_ = [("a", C.c_void_p), ("nrhs", C.c_int), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("scaling", C.c_double)]
+
+
 # name -> (restype, argtypes)
 PROTOS = {
     "psfun_gpu_version": (C.c_char_p, []),
@@ -48,6 +54,8 @@ PROTOS = {
                                            C.POINTER(C.c_int), dp, dp, C.c_int, C.POINTER(C.c_int)]),
     "psfun_gpu_d_krylov_apply_device": (C.c_int, [vp, vp, vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int,
                                                   C.POINTER(C.c_int), dp, dp, C.c_int, C.POINTER(C.c_int)]),
+    "psfun_gpu_d_krylov_batch": (C.c_int, [vp, vp, C.c_int, C.POINTER(BatchItem), C.c_double, C.c_int, C.c_int,
+                                            C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]),
     "psfun_gpu_dcg": (C.c_int, [C.c_char_p, vp, C.c_char_p, dp, C.c_double, C.c_double, dp, C.c_double, C.c_int,
                                 C.c_int, C.POINTER(C.c_int), dp]),
     "psfun_gpu_dcg_device": (C.c_int, [C.c_char_p, vp, C.c_char_p, vp, C.c_double, C.c_double, vp, C.c_double,

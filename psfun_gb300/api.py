@@ -239,6 +239,29 @@ class PsfunDKrylov:
             pass
 
 
+def krylov_batch(meth: "PsfunDKrylov", fun: "PsfunDSerial", items, eps: float, itmax: int = 200,
+                 istop: int = 1):
+    """Batched Lanczos f(t_k A_k) X_k for items [(CsrMatrix, X, Y, t_k), ...] in one
+    persistent launch.  X, Y: CUDA float64 tensors of shape (nrhs, n) (column-major
+    n x nrhs, the same nrhs for every item).  Returns (info, infos, iters, errs), the
+    per-pair arrays shaped (count, nrhs)."""
+    count = len(items)
+    arr = (_capi.BatchItem * count)()
+    R = int(items[0][1].shape[0])
+    for k, (a, X, Y, t) in enumerate(items):
+        if not (_is_device(X) and _is_device(Y)):
+            raise TypeError("krylov_batch takes CUDA tensors")
+        arr[k] = _capi.BatchItem(a.handle, int(X.shape[0]), X.data_ptr(), Y.data_ptr(), float(t))
+    iters = np.zeros(count * R, dtype=np.int32)
+    errs = np.zeros(count * R)
+    infos = np.zeros(count * R, dtype=np.int32)
+    _sync_stream()
+    info = _lib().psfun_gpu_d_krylov_batch(meth.handle, fun.handle, count, arr, eps, int(itmax), int(istop),
+                                           iters.ctypes.data_as(C.POINTER(C.c_int)), _dp(errs),
+                                           infos.ctypes.data_as(C.POINTER(C.c_int)))
+    return info, infos.reshape(count, R), iters.reshape(count, R), errs.reshape(count, R)
+
+
 # ---------------------------------------------------------------------------
 def psb_krylov(method: str, a: CsrMatrix, prec: str, b, eta: float, zeta: float, x, eps: float,
                itmax: int = 1000, istop: int = 2):

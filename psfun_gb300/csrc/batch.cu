@@ -1,0 +1,765 @@
+// batch.cu -- many uneven f(A)X problems in one persistent launch.
+//
+// psfun_gpu_d_krylov_batch runs the Lanczos f(A)x method of the reference
+// (krylov/polynomial/psfun_d_lanczos.f90:97-391, per right-hand side) for a
+// list of instances (A_k, X_k with R right-hand sides, scaling t_k) in ONE
+// cooperative kernel:
+//
+//   * the R right-hand sides of an instance are interleaved (row-major n x R)
+//     so one pass over A_k serves all of them (SpMM: R FMAs per gathered
+//     32-byte row of the basis);
+//   * every phase walks a global queue of row tiles (all instances' CSR tiles
+//     concatenated) handed out by an atomic counter -- the device work queue --
+//     so instances of very different sizes share the GPU without idle SMs;
+//   * the last CTA to finish a phase on an instance finalises that instance's
+//     scalars in tile order (deterministic) and, after the update phase, runs
+//     the per-pair a posteriori estimate (CRAM on the tridiagonal t_k T);
+//   * instances whose right-hand sides have all stopped leave the queue;
+//   * two bounded grid barriers per Krylov step.
+//
+// Each pair (instance, right-hand side) follows the reference's control flow:
+// the estimate of iteration i uses T(1:i-1) and beta_i, breakdown |beta| <
+// 1e-16 ends the pair with itx = i-1, the non-converged result uses
+// f(T(1:itx-1)), and the assembly drops the last coefficient unless KEEPLAST.
+// f is EXP evaluated with the CHBSYM/CHBGEN rational (CRAM) on t_k T, the
+// reference's Lanczos variant (examples/polynomial/lanczos.inp).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace psf {
+
+constexpr int kBatchMaxRhs = 4;
+constexpr int kBatchThreads = kSpmvThreads;
+
+// per-pair scalar arrays, each nl + 2 long
+enum { PA_ALPHA = 0, PA_BETA, PA_S, PA_RS, PA_YK, PA_COEF, PA_N };
+
+struct PairState {
+  int done;   // stopped (converged, breakdown or error)
+  int conv;
+  int itx;
+  int yk_len;
+  int nterms;
+  int info;
+  double beta0;
+  double errnum, errden;
+};
+
+struct BInst {
+  CsrDev A;
+  int n, R, tile_begin, ntiles, mapping, pad;
+  int64_t ldv;  // slot stride in doubles (>= n*R, multiple of 32)
+  double t;
+  double* V;
+  double* u;
+  double* scal;  // R * PA_N * (nl+2)
+  double* part;  // 2 * ntiles * R tile partials
+  double* cram;  // R * 7 * 5 * (nl+2) complex scratch
+  PairState* ps; // R
+  const double* X;
+  double* Y;
+  unsigned* cnt;  // [0] phase tile counter, [1] active pairs
+};
+
+struct BatchArgs {
+  BInst* inst;
+  int count;
+  int total_tiles;
+  int nl;
+  int istop;
+  int keeplast;
+  double eps;
+  unsigned* queue;  // one counter per phase, zeroed before the launch
+  unsigned* bar;    // [0] count, [1] gen
+  int* err;
+  unsigned* active; // instances still running
+};
+
+PSF_DEVINL double* pa(const BInst& I, int q, int which, int nl) {
+  return I.scal + ((size_t)q * PA_N + which) * (size_t)(nl + 2);
+}
+
+// Instance of a global tile (binary search on tile_begin).
+PSF_DEVINL int find_inst(const BatchArgs& B, int g) {
+  int lo = 0, hi = B.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (B.inst[mid].tile_begin <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---- CRAM on the tridiagonal t*T(1:m): y = exp(t T) e1 (dnchbv.f:54-69 rule,
+// banded GEPP per pole, one thread per pole).
+PSF_DEVINL void cram_pole_tridiag(int m, double t, const double* alpha, const double* beta, int p, zc* band,
+                                  zc* b, int* bad) {
+  const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
+  zc* d = band;
+  zc* du = d + m;
+  zc* du2 = du + m;
+  zc* dl = du2 + m;
+  for (int i = 0; i < m; ++i) {
+    d[i] = zsub(zmk(-t * alpha[i + 1], 0.0), theta);  // alpha is 1-based
+    const double off = (i + 1 < m) ? -t * beta[i + 2] : 0.0;  // beta[i+2] = T(i+2,i+1)
+    du[i] = zmk(off, 0.0);
+    dl[i] = zmk(off, 0.0);
+    du2[i] = zmk(0.0, 0.0);
+    b[i] = zmk(i == 0 ? 1.0 : 0.0, 0.0);
+  }
+  for (int k = 0; k < m - 1; ++k) {
+    if (zabs(d[k]) < zabs(dl[k])) {
+      zc tt;
+      tt = d[k]; d[k] = dl[k]; dl[k] = tt;
+      tt = du[k]; du[k] = d[k + 1]; d[k + 1] = tt;
+      if (k + 1 < m - 1) { tt = du2[k]; du2[k] = du[k + 1]; du[k + 1] = tt; }
+      tt = b[k]; b[k] = b[k + 1]; b[k + 1] = tt;
+    }
+    if (zabs(d[k]) == 0.0) { *bad = 1; return; }
+    const zc l = zdiv(dl[k], d[k]);
+    d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
+    if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
+    b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+  }
+  if (zabs(d[m - 1]) == 0.0) { *bad = 1; return; }
+  for (int i = m - 1; i >= 0; --i) {
+    zc s = b[i];
+    if (i + 1 < m) s = zsub(s, zmul(du[i], b[i + 1]));
+    if (i + 2 < m) s = zsub(s, zmul(du2[i], b[i + 2]));
+    b[i] = zdiv(s, d[i]);
+  }
+}
+
+// yk = exp(t T(1:m)) e1 for the pairs q of instance I with bit q set in
+// `mask`, block-wide.  Returns false if a pole solve met a zero pivot.
+PSF_DEVINL bool block_fT(const BInst& I, int nl, int m, unsigned mask) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const size_t stride = (size_t)(nl + 2);
+  for (int task = threadIdx.x; task < I.R * 7; task += blockDim.x) {
+    const int q = task / 7, p = task - q * 7;
+    if (!((mask >> q) & 1u)) continue;
+    zc* base = reinterpret_cast<zc*>(I.cram) + ((size_t)q * 7 + p) * 5 * stride;
+    int b = 0;
+    cram_pole_tridiag(m, I.t, pa(I, q, PA_ALPHA, nl), pa(I, q, PA_BETA, nl), p, base + stride, base, &b);
+    if (b) atomicOr(&bad, 1);
+  }
+  __syncthreads();
+  if (bad) return false;
+  for (int task = threadIdx.x; task < I.R * m; task += blockDim.x) {
+    const int q = task / m, j = task - q * m;
+    if (!((mask >> q) & 1u)) continue;
+    double acc = (j == 0) ? kCramAlpha0 : 0.0;
+    for (int p = 0; p < 7; ++p) {
+      const zc* sol = reinterpret_cast<const zc*>(I.cram) + ((size_t)q * 7 + p) * 5 * stride;
+      acc = acc + cuCreal(zmul(zmk(kCramAlpha[p][0], kCramAlpha[p][1]), sol[j]));
+    }
+    pa(I, q, PA_YK, nl)[j] = acc;
+  }
+  __syncthreads();
+  return true;
+}
+
+// ---- phases ------------------------------------------------------------------
+enum { PH_INIT = 0, PH_SPMM = 1, PH_UPDATE = 2, PH_RECOMB = 3 };
+
+// Row-level work of one tile for phase `ph`; returns the R partial sums.
+template <int R>
+PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs& B, SpmvSmem& sm, double* accR) {
+  const TileInfo ti = tile_info(I.A, lt);
+  const int nr = ti.r1 - ti.r0;
+  if (ph == PH_INIT) {
+    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+      const int r = ti.r0 + lr;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const double v = I.X[(size_t)q * I.n + r];
+        I.V[(size_t)r * R + q] = v;
+        accR[q] = fma(v, v, accR[q]);
+      }
+    }
+    return;
+  }
+  const double* __restrict__ wi = I.V + (size_t)(i - 1) * I.ldv;
+  if (ph == PH_SPMM) {
+    // stage the tile (values, indices, row pointers) and form u = A W_i
+    if (ti.k1 - ti.k0 > kTileNnz) {
+      for (int lr = 0; lr < nr; ++lr) {  // one long row
+        double s[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) s[q] = 0.0;
+        for (int k = ti.k0 + threadIdx.x; k < ti.k1; k += blockDim.x) {
+          const double a = I.A.val[k];
+          const int c = I.A.ja[k];
+#pragma unroll
+          for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(wi + (size_t)c * R + q), s[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          const double v = block_sum(s[q], sm.red);
+          if (threadIdx.x == 0) {
+            I.u[(size_t)ti.r0 * R + q] = v;
+            accR[q] = fma(v, wi[(size_t)ti.r0 * R + q], accR[q]);
+          }
+        }
+      }
+      return;
+    }
+    if (threadIdx.x == 0) spmv_issue(I.A, ti, sm, 0);
+    const bool ok = mbar_wait(&sm.bar[0], sm.phase[0]);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(B.err, DEVERR_TIMEOUT);
+      mbar_wait(&sm.bar[0], sm.phase[0]);
+      return;
+    }
+    const SpmvTile& tb = sm.buf[0];
+    const int dj = ti.kv0 - ti.kj0, di = ti.r0 - ti.ki0;
+    if (I.mapping == 0) {  // one thread per row, R accumulators
+      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+        const int kb = tb.irp[lr + di] - ti.kv0, ke = tb.irp[lr + di + 1] - ti.kv0;
+        double s[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) s[q] = 0.0;
+        for (int k = kb; k < ke; ++k) {
+          const double a = tb.val[k];
+          const double* xr = wi + (size_t)tb.ja[k + dj] * R;
+          if (R == 4) {
+            const double2 x01 = __ldg(reinterpret_cast<const double2*>(xr));
+            const double2 x23 = __ldg(reinterpret_cast<const double2*>(xr) + 1);
+            s[0] = fma(a, x01.x, s[0]);
+            s[1] = fma(a, x01.y, s[1]);
+            s[2 % R] = fma(a, x23.x, s[2 % R]);
+            s[3 % R] = fma(a, x23.y, s[3 % R]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
+          }
+        }
+        const int r = ti.r0 + lr;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          I.u[(size_t)r * R + q] = s[q];
+          accR[q] = fma(s[q], wi[(size_t)r * R + q], accR[q]);
+        }
+      }
+    } else {  // R threads per row, one right-hand side each
+      for (int task = threadIdx.x; task < nr * R; task += blockDim.x) {
+        const int lr = task / R, q = task - lr * R;
+        const int kb = tb.irp[lr + di] - ti.kv0, ke = tb.irp[lr + di + 1] - ti.kv0;
+        double s = 0.0;
+        for (int k = kb; k < ke; ++k) s = fma(tb.val[k], __ldg(wi + (size_t)tb.ja[k + dj] * R + q), s);
+        const int r = ti.r0 + lr;
+        I.u[(size_t)r * R + q] = s;
+        const double pv = s * wi[(size_t)r * R + q];
+        // accumulate into the right slot: every thread handles a fixed q when blockDim % R == 0
+#pragma unroll
+        for (int qq = 0; qq < R; ++qq)
+          if (qq == q) accR[qq] += pv;
+      }
+    }
+    if (threadIdx.x == 0) sm.phase[0] ^= 1u;
+    return;
+  }
+  if (ph == PH_UPDATE) {
+    const double* __restrict__ wm = (i >= 2) ? I.V + (size_t)(i - 2) * I.ldv : wi;
+    double* __restrict__ wo = I.V + (size_t)i * I.ldv;
+    double c1[R], c2[R];
+    int k2[R];
+    bool live[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const double sc = pa(I, q, PA_S, B.nl)[i];
+      c1[q] = pa(I, q, PA_ALPHA, B.nl)[i];
+      c2[q] = (i >= 2) ? pa(I, q, PA_BETA, B.nl)[i] * pa(I, q, PA_S, B.nl)[i - 1] / sc : 0.0;
+      k2[q] = ilog2_normal(sc);
+      live[q] = !I.ps[q].done;
+    }
+    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+      const size_t r = (size_t)(ti.r0 + lr) * R;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        if (!live[q]) continue;
+        const double w = fma(-c2[q], wm[r + q], fma(-c1[q], wi[r + q], I.u[r + q]));
+        accR[q] = fma(w, w, accR[q]);
+        wo[r + q] = scale_pow2(w, k2[q]);
+      }
+    }
+    return;
+  }
+  // PH_RECOMB: Y[q*n + r] = sum_j coef_{q,j} W_j[r*R + q]
+  for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+    const int r = ti.r0 + lr;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int nt = I.ps[q].nterms;
+      const double* cf = pa(I, q, PA_COEF, B.nl);
+      double acc = 0.0;
+      for (int j = 0; j < nt; ++j) acc = fma(cf[j], I.V[(size_t)j * I.ldv + (size_t)r * R + q], acc);
+      I.Y[(size_t)q * I.n + r] = acc;
+    }
+  }
+}
+
+// Finalisation by the last CTA of an instance (deterministic tile order).
+template <int R>
+PSF_DEVINL void finalize(const BInst& I, int ph, int i, const BatchArgs& B, double* red) {
+  const int nl = B.nl;
+  const double* part = I.part + (size_t)((ph == PH_UPDATE) ? 1 : 0) * I.ntiles * R;
+  double tot[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    double v = 0.0;
+    for (int t = threadIdx.x; t < I.ntiles; t += blockDim.x) v += part[(size_t)t * R + q];
+    tot[q] = block_sum(v, red);
+  }
+  if (ph == PH_INIT) {
+    if (threadIdx.x == 0) {
+      int live = 0;
+      for (int q = 0; q < R; ++q) {
+        PairState& P = I.ps[q];
+        const double b0 = sqrt(tot[q]);
+        P.beta0 = b0;
+        pa(I, q, PA_RS, nl)[1] = b0;
+        P.errnum = 0.0;
+        P.errden = 1.0;
+        if (b0 == 0.0) { P.done = 1; P.itx = 0; }
+        else { pa(I, q, PA_S, nl)[1] = 1.0 / b0; ++live; }
+      }
+      I.cnt[1] = live;
+      if (live == 0) atomicSub(B.active, 1u);
+    }
+    return;
+  }
+  if (ph == PH_SPMM) {
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < R; ++q) {
+        if (I.ps[q].done) continue;
+        const double sc = pa(I, q, PA_S, nl)[i];
+        pa(I, q, PA_ALPHA, nl)[i] = sc * sc * tot[q];
+        if (i >= 2) I.ps[q].itx = i - 1;
+      }
+    }
+    return;
+  }
+  // PH_UPDATE: beta_{i+1}, s_{i+1}; then iteration i+1's top: breakdown test
+  // and the estimate with T(1:i), beta_{i+1}
+  __shared__ int est_q[kBatchMaxRhs];
+  __shared__ int nest;
+  if (threadIdx.x == 0) {
+    nest = 0;
+    for (int q = 0; q < R; ++q) {
+      PairState& P = I.ps[q];
+      if (P.done) continue;
+      const double sc = pa(I, q, PA_S, nl)[i];
+      const double wn = sqrt(tot[q]);
+      const double beta = sc * wn;
+      pa(I, q, PA_BETA, nl)[i + 1] = beta;
+      pa(I, q, PA_S, nl)[i + 1] = 1.0 / ldexp(wn, ilog2_normal(sc));
+      if (i + 1 > nl) { P.done = 1; continue; }
+      P.itx = i;
+      if (fabs(beta) < 1e-16) { P.done = 1; continue; }  // psfun_d_lanczos.f90:225-230
+      if (B.istop == 1) est_q[nest++] = q;
+      else if (i + 1 == nl) P.done = 1;
+    }
+  }
+  __syncthreads();
+  if (nest > 0) {
+    // yk = exp(t T(1:i)) e1 for the pairs still running
+    unsigned mask = 0u;
+    for (int e = 0; e < nest; ++e) mask |= 1u << est_q[e];
+    if (!block_fT(I, nl, i, mask)) {
+      if (threadIdx.x == 0)
+        for (int e = 0; e < nest; ++e) { I.ps[est_q[e]].done = 1; I.ps[est_q[e]].info = PSFUN_ERR_FROM_SUBROUTINE_NON; }
+    } else if (threadIdx.x == 0) {
+      for (int e = 0; e < nest; ++e) {
+        const int q = est_q[e];
+        PairState& P = I.ps[q];
+        const double* yk = pa(I, q, PA_YK, nl);
+        double ss = 0.0;
+        for (int j = 0; j < i; ++j) ss += yk[j] * yk[j];
+        const double errnum = P.beta0 * fabs(I.t * pa(I, q, PA_BETA, nl)[i + 1]) * fabs(yk[i - 1]);
+        const double errden = sqrt(ss);
+        P.errnum = errnum;
+        P.errden = errden;
+        pa(I, q, PA_RS, nl)[i + 1] = errnum / errden;
+        if (errnum / errden < B.eps) {
+          P.done = 1;
+          P.conv = 1;
+          P.yk_len = i;
+          // keep the converged coefficients apart from later estimates
+          double* cf = pa(I, q, PA_COEF, nl);
+          for (int j = 0; j < i; ++j) cf[j] = yk[j];
+        } else if (i + 1 == nl) {
+          P.done = 1;  // loop ends after iteration nl
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int live = 0;
+    for (int q = 0; q < R; ++q) live += !I.ps[q].done;
+    if (live == 0 && I.cnt[1] != 0) atomicSub(B.active, 1u);
+    I.cnt[1] = live;
+  }
+}
+
+// Final f and assembly coefficients of every pair (block per instance).
+template <int R>
+PSF_DEVINL void final_pairs(const BInst& I, const BatchArgs& B, double* red) {
+  const int nl = B.nl;
+  __shared__ int mq[kBatchMaxRhs];
+  __shared__ int need;
+  if (threadIdx.x == 0) {
+    need = 0;
+    for (int q = 0; q < R; ++q) {
+      PairState& P = I.ps[q];
+      mq[q] = 0;
+      if (P.info || P.beta0 == 0.0) continue;
+      if (!P.conv) {
+        const int m = P.itx - 1;
+        if (m < 1) { P.info = PSFUN_ERR_FROM_SUBROUTINE_NON; continue; }
+        mq[q] = m;
+        need = max(need, m);
+      }
+    }
+  }
+  __syncthreads();
+  // pairs that did not converge: f(T(1:itx-1)); pairs share the dimension only
+  // when equal, so evaluate per distinct m
+  for (int q = 0; q < R; ++q) {
+    const int m = mq[q];
+    if (m == 0) continue;
+    if (!block_fT(I, nl, m, 1u << q)) {
+      if (threadIdx.x == 0) I.ps[q].info = PSFUN_ERR_FROM_SUBROUTINE_NON;
+      continue;
+    }
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < m; ++j) pa(I, q, PA_COEF, nl)[j] = pa(I, q, PA_YK, nl)[j];
+      I.ps[q].yk_len = m;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < R; ++q) {
+      PairState& P = I.ps[q];
+      if (P.info || P.beta0 == 0.0) { P.nterms = 0; continue; }
+      int nterms = (P.conv && !B.keeplast) ? max(P.itx - 1, 1) : P.yk_len;
+      nterms = min(nterms, P.yk_len);
+      double* cf = pa(I, q, PA_COEF, nl);
+      const double* s = pa(I, q, PA_S, nl);
+      for (int j = 0; j < nterms; ++j) cf[j] = P.beta0 * cf[j] * s[j + 1];
+      P.nterms = nterms;
+    }
+  }
+  __syncthreads();
+}
+
+template <int R>
+PSF_DEVINL bool run_phase(const BatchArgs& B, int ph, int i, unsigned* qctr, SpmvSmem& sm) {
+  __shared__ int g_sh, last_sh, skip_sh;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      // -1 drains the queue after a device error; decided once per block
+      g_sh = (*(volatile int*)B.err != 0) ? -1 : (int)atomicAdd(qctr, 1u);
+      skip_sh = 0;
+      if (g_sh >= 0 && g_sh < B.total_tiles && ph != PH_INIT && ph != PH_RECOMB)
+        skip_sh = (*(volatile unsigned*)&B.inst[find_inst(B, g_sh)].cnt[1] == 0u);
+    }
+    __syncthreads();
+    const int g = g_sh;
+    const bool skip = skip_sh != 0;
+    __syncthreads();
+    if (g < 0 || g >= B.total_tiles) break;
+    const int k = find_inst(B, g);
+    const BInst& I = B.inst[k];
+    const int lt = g - I.tile_begin;
+    double accR[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) accR[q] = 0.0;
+    if (!skip) tile_work<R>(I, ph, i, lt, B, sm, accR);
+    if (ph == PH_RECOMB) { __syncthreads(); continue; }
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const double v = block_sum(accR[q], sm.red);
+      if (threadIdx.x == 0) I.part[((size_t)((ph == PH_UPDATE) ? 1 : 0) * I.ntiles + lt) * R + q] = v;
+    }
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last_sh = (atomicAdd(&I.cnt[0], 1u) == (unsigned)I.ntiles - 1);
+    }
+    __syncthreads();
+    if (last_sh) {
+      __threadfence();
+      if (threadIdx.x == 0) I.cnt[0] = 0u;
+      if (!skip) finalize<R>(I, ph, i, B, sm.red);
+      __threadfence();
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kBatchThreads) k_batch(BatchArgs B) {
+  PSF_SPMV_SMEM();
+  spmv_smem_init(sm);
+  int ph_idx = 0;
+  run_phase<R>(B, PH_INIT, 0, &B.queue[ph_idx++], sm);
+  if (!grid_barrier(&B.bar[0], &B.bar[1], B.err)) return;
+  __shared__ unsigned act;
+  for (int i = 1; i <= B.nl; ++i) {
+    if (threadIdx.x == 0) act = *(volatile unsigned*)B.active;
+    __syncthreads();
+    if (act == 0u) break;  // block-uniform; identical in every block after the barrier
+    run_phase<R>(B, PH_SPMM, i, &B.queue[ph_idx++], sm);
+    if (!grid_barrier(&B.bar[0], &B.bar[1], B.err)) return;
+    run_phase<R>(B, PH_UPDATE, i, &B.queue[ph_idx++], sm);
+    if (!grid_barrier(&B.bar[0], &B.bar[1], B.err)) return;
+  }
+  // final f per instance (CTA k handles instances k, k+G, ...)
+  for (int k = blockIdx.x; k < B.count; k += gridDim.x) final_pairs<R>(B.inst[k], B, sm.red);
+  if (!grid_barrier(&B.bar[0], &B.bar[1], B.err)) return;
+  run_phase<R>(B, PH_RECOMB, 0, &B.queue[2 * B.nl + 2], sm);
+}
+
+// ---- autotuner ----------------------------------------------------------------
+// The SpMM mapping (one thread per row with R accumulators, or R threads per
+// row) is chosen per size bucket by timing a standalone run of the same tile
+// code on the bucket's first instance; the choice is cached per (bucket, R).
+template <int R>
+__global__ void __launch_bounds__(kBatchThreads) k_batch_spmm_probe(BatchArgs B, int k) {
+  PSF_SPMV_SMEM();
+  spmv_smem_init(sm);
+  const BInst& I = B.inst[k];
+  double accR[R];
+  for (int lt = blockIdx.x; lt < I.ntiles; lt += gridDim.x) {
+    for (int q = 0; q < R; ++q) accR[q] = 0.0;
+    tile_work<R>(I, PH_SPMM, 1, lt, B, sm, accR);
+    __syncthreads();
+  }
+}
+
+static int bucket_of(int64_t n) {
+  if (n < 16384) return 0;
+  if (n < 65536) return 1;
+  if (n < 262144) return 2;
+  return 3;
+}
+
+struct TuneCache {
+  int choice[4][kBatchMaxRhs + 1];
+  bool have[4][kBatchMaxRhs + 1];
+};
+static TuneCache g_tune;
+
+int batch_tuned_mapping(int bucket, int R) {
+  return g_tune.have[bucket][R] ? g_tune.choice[bucket][R] : -1;
+}
+
+template <int R>
+static int autotune(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, cudaStream_t s) {
+  for (int bkt = 0; bkt < 4; ++bkt) {
+    if (g_tune.have[bkt][R]) {
+      for (auto& I : hinst)
+        if (bucket_of(I.n) == bkt) I.mapping = g_tune.choice[bkt][R];
+      continue;
+    }
+    int k = -1;
+    for (int j = 0; j < (int)hinst.size(); ++j)
+      if (bucket_of(hinst[j].n) == bkt) { k = j; break; }
+    if (k < 0) continue;
+    float best = 1e30f;
+    int best_map = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int map = 0; map < 2; ++map) {
+      hinst[k].mapping = map;
+      PSF_CUDA(cudaMemcpyAsync(dinst + k, &hinst[k], sizeof(BInst), cudaMemcpyHostToDevice, s));
+      const int g = std::max(1, std::min(hinst[k].ntiles, sm_count() * 2));
+      for (int rep = 0; rep < 2; ++rep)
+        k_batch_spmm_probe<R><<<g, kBatchThreads, kSpmvSmemBytes, s>>>(B, k);
+      cudaEventRecord(e0, s);
+      for (int rep = 0; rep < 5; ++rep)
+        k_batch_spmm_probe<R><<<g, kBatchThreads, kSpmvSmemBytes, s>>>(B, k);
+      cudaEventRecord(e1, s);
+      count_launch(7);
+      PSF_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) { best = ms; best_map = map; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_tune.choice[bkt][R] = best_map;
+    g_tune.have[bkt][R] = true;
+    for (auto& I : hinst)
+      if (bucket_of(I.n) == bkt) I.mapping = best_map;
+  }
+  PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * hinst.size(), cudaMemcpyHostToDevice, s));
+  return PSFUN_SUCCESS;
+}
+
+template <int R>
+static void batch_attrs() {
+  static bool done = false;
+  if (!done) {
+    spmv_smem_attr(k_batch<R>);
+    spmv_smem_attr(k_batch_spmm_probe<R>);
+    done = true;
+  }
+}
+
+template <int R>
+static int batch_launch(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, cudaStream_t s, int tune) {
+  batch_attrs<R>();
+  if (tune) PSF_TRY(autotune<R>(B, hinst, dinst, s));
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch<R>, kBatchThreads, kSpmvSmemBytes);
+  if (per < 1) per = 1;
+  int G = sm_count() * per;
+  if (G > B.total_tiles) G = std::max(1, B.total_tiles);
+  void* args[] = {(void*)&B};
+  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_batch<R>, dim3(G), dim3(kBatchThreads), args, kSpmvSmemBytes, s));
+  count_launch();
+  return PSFUN_SUCCESS;
+}
+
+}  // namespace psf
+
+using namespace psf;
+
+extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count,
+                                        const psfun_batch_item* items, double eps, int itmax, int istop,
+                                        int* iters, double* errs, int* infos) {
+  if (!meth || !fun || count < 1 || !items) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  char kn[32];
+  {
+    int n = 0;
+    for (; meth->kname[n] && n < 31; ++n) kn[n] = (char)toupper((unsigned char)meth->kname[n]);
+    while (n > 0 && kn[n - 1] == ' ') --n;
+    kn[n] = 0;
+  }
+  if (strcmp(kn, "LANCZOS") != 0) {
+    set_last_error("the batched path implements LANCZOS");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  if (istop < 1 || istop > 2) return PSFUN_ERR_INVALID_ISTOP;
+  FunParams fp;
+  if (!parse_fun(fun, &fp) || fp.fname != FN_EXP || (fp.variant != VAR_CHBSYM && fp.variant != VAR_CHBGEN)) {
+    set_last_error("the batched path evaluates EXP with the CHBSYM/CHBGEN rational");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  if (itmax < 2) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  const int R = items[0].nrhs;
+  if (R < 1 || R > kBatchMaxRhs) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  for (int k = 0; k < count; ++k) {
+    if (!items[k].a || items[k].nrhs != R) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    if (!items[k].x || !items[k].y) return PSFUN_ERR_INVALID_VECT_STATE;
+  }
+  const int nl = itmax;
+  cudaStream_t s = stream();
+  // workspace: one allocation, carved per instance
+  std::vector<BInst> hinst(count);
+  size_t off = 0;
+  int tiles = 0;
+  auto carve = [&](size_t doubles) {
+    const size_t o = off;
+    off += (doubles + 31) & ~(size_t)31;
+    return o;
+  };
+  std::vector<size_t> oV(count), oU(count), oS(count), oP(count), oC(count), oPS(count), oCnt(count);
+  for (int k = 0; k < count; ++k) {
+    psfun_csr* a = items[k].a;
+    BInst& I = hinst[k];
+    memset(&I, 0, sizeof I);
+    I.A = a->dev();
+    I.n = (int)a->n;
+    I.R = R;
+    I.tile_begin = tiles;
+    I.ntiles = a->ntiles;
+    I.t = items[k].scaling;
+    I.ldv = ((int64_t)a->n * R + 31) & ~(int64_t)31;
+    I.X = items[k].x;
+    I.Y = items[k].y;
+    tiles += a->ntiles;
+    oV[k] = carve((size_t)(nl + 1) * I.ldv);
+    oU[k] = carve((size_t)I.ldv);
+    oS[k] = carve((size_t)R * PA_N * (nl + 2));
+    oP[k] = carve((size_t)2 * a->ntiles * R);
+    oC[k] = carve((size_t)R * 7 * 5 * (nl + 2) * 2);
+    oPS[k] = carve((sizeof(PairState) * R + 7) / 8);
+    oCnt[k] = carve(2);
+  }
+  const size_t oInst = carve((sizeof(BInst) * count + 7) / 8);
+  const size_t oQ = carve(2 * (size_t)nl + 8);
+  const size_t oMisc = carve(8);
+  DevBuf& ws = meth->scratch;  // reuse the handle's scratch for the batch
+  PSF_TRY(ws.ensure(sizeof(double) * off));
+  double* base = ws.as<double>();
+  // zero pair state, counters, queues; V needs no clearing
+  for (int k = 0; k < count; ++k) {
+    PSF_CUDA(cudaMemsetAsync(base + oS[k], 0, sizeof(double) * (oP[k] - oS[k]), s));
+    PSF_CUDA(cudaMemsetAsync(base + oPS[k], 0, sizeof(double) * (oInst > oPS[k] ? (oCnt[k] + 2 - oPS[k]) : 0), s));
+  }
+  PSF_CUDA(cudaMemsetAsync(base + oQ, 0, sizeof(double) * (oMisc + 8 - oQ), s));
+  for (int k = 0; k < count; ++k) {
+    BInst& I = hinst[k];
+    I.V = base + oV[k];
+    I.u = base + oU[k];
+    I.scal = base + oS[k];
+    I.part = base + oP[k];
+    I.cram = base + oC[k];
+    I.ps = reinterpret_cast<PairState*>(base + oPS[k]);
+    I.cnt = reinterpret_cast<unsigned*>(base + oCnt[k]);
+  }
+  BInst* dinst = reinterpret_cast<BInst*>(base + oInst);
+  PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * count, cudaMemcpyHostToDevice, s));
+  unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
+  BatchArgs B;
+  B.inst = dinst;
+  B.count = count;
+  B.total_tiles = tiles;
+  B.nl = nl;
+  B.istop = istop;
+  B.keeplast = meth->keeplast;
+  B.eps = eps;
+  B.queue = reinterpret_cast<unsigned*>(base + oQ);
+  B.bar = misc;
+  B.err = reinterpret_cast<int*>(misc + 2);
+  B.active = misc + 3;
+  const unsigned active = (unsigned)count;
+  PSF_CUDA(cudaMemcpyAsync(B.active, &active, sizeof active, cudaMemcpyHostToDevice, s));
+  int rc;
+  switch (R) {
+    case 1: rc = batch_launch<1>(B, hinst, dinst, s, 1); break;
+    case 2: rc = batch_launch<2>(B, hinst, dinst, s, 1); break;
+    case 3: rc = batch_launch<3>(B, hinst, dinst, s, 1); break;
+    default: rc = batch_launch<4>(B, hinst, dinst, s, 1); break;
+  }
+  if (rc != PSFUN_SUCCESS) return rc;
+  int herr = 0;
+  PSF_CUDA(cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  std::vector<PairState> hps((size_t)count * R);
+  for (int k = 0; k < count; ++k)
+    PSF_CUDA(cudaMemcpyAsync(&hps[(size_t)k * R], hinst[k].ps, sizeof(PairState) * R, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (herr & DEVERR_TIMEOUT) {
+    set_last_error("device-side wait timed out");
+    return PSFUN_ERR_DEVICE_TIMEOUT;
+  }
+  int worst = PSFUN_SUCCESS;
+  for (size_t p = 0; p < hps.size(); ++p) {
+    const PairState& P = hps[p];
+    if (iters) iters[p] = P.itx;
+    if (errs) errs[p] = (P.errden > 0.0) ? P.errnum / P.errden : P.errnum;
+    if (infos) infos[p] = P.info;
+    if (P.info && worst == PSFUN_SUCCESS) worst = P.info;
+  }
+  return worst;
+}

@@ -1,0 +1,86 @@
+"""Batched f(t A) X (one persistent launch for many uneven instances) against
+the plain per-instance drop-in calls and the oracle, pair by pair."""
+import numpy as np
+import pytest
+
+from psfun_gb300 import matrices
+
+pytestmark = pytest.mark.gpu
+
+
+def make_items(seed=0, R=4):
+    rng = np.random.default_rng(seed)
+    mats = [matrices.laplacian_2d(s) for s in (9, 23, 40, 31)]
+    mats += [matrices.rgg_knn_laplacian(n, 8, rng) for n in (300, 1500, 4100)]
+    out = []
+    for A in mats:
+        X = rng.standard_normal((R, A.shape[0]))
+        t = float(rng.uniform(0.01, 1.0))
+        out.append((A, X, t))
+    return out
+
+
+def plain(A, x, t, eps, itmax, istop=1):
+    import psfun_gb300 as pg
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", "CHBSYM")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    return meth.apply(fun, pg.CsrMatrix.from_scipy(t * A), x, eps, itmax=itmax, istop=istop)
+
+
+@pytest.mark.parametrize("istop", [1, 2])
+@pytest.mark.parametrize("R", [1, 4])
+def test_batch_matches_plain(lib, orc, istop, R):
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    eps, itmax = 1e-8, 40
+    items = make_items(1, R)
+    handles = []
+    for A, X, t in items:
+        a = pg.CsrMatrix.from_scipy(A)
+        Xd = torch.tensor(X, device="cuda")
+        Yd = torch.zeros_like(Xd)
+        handles.append((a, Xd, Yd, t))
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", "CHBSYM")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    info, infos, iters, errs = pg.krylov_batch(meth, fun, handles, eps, itmax=itmax, istop=istop)
+    torch.cuda.synchronize()
+    assert info == 0 and not infos.any()
+    for k, ((A, X, t), (a, Xd, Yd, _)) in enumerate(zip(items, handles)):
+        Y = Yd.cpu().numpy()
+        for q in range(R):
+            r = plain(A, X[q], t, eps, itmax, istop)
+            o = orc.krylov("LANCZOS", orc.serial("EXP", "CHBSYM", 1.0), orc.Csr.from_scipy(t * A), X[q], eps,
+                           itmax=itmax, istop=istop)
+            assert r.info == 0 and o["info"] == 0
+            assert iters[k, q] == r.iter == o["iter"], (k, q, iters[k, q], r.iter, o["iter"])
+            assert np.linalg.norm(Y[q] - r.y) <= 1e-10 * np.linalg.norm(r.y), (k, q)
+            assert np.linalg.norm(Y[q] - o["y"]) <= 1e-10 * np.linalg.norm(o["y"]), (k, q)
+
+
+def test_batch_zero_rhs_and_errors(lib):
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    A = matrices.laplacian_2d(12)
+    a = pg.CsrMatrix.from_scipy(A)
+    X = torch.zeros((2, 144), dtype=torch.float64, device="cuda")
+    X[1] = 1.0
+    Y = torch.full_like(X, 7.0)
+    fun = pg.PsfunDSerial()
+    fun.set("VARIANT", "CHBSYM")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    info, infos, iters, errs = pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)
+    torch.cuda.synchronize()
+    assert info == 0 and iters[0, 0] == 0 and not Y[0].any()
+    assert torch.isfinite(Y[1]).all()
+    fun.set("VARIANT", "GENPADE")
+    assert pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)[0] == 111
+    fun.set("VARIANT", "CHBSYM")
+    meth.set("KNAME", "ARNOLDI")
+    assert pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)[0] == 111
