@@ -199,6 +199,27 @@ typedef struct {
 int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count, const psfun_batch_item* items,
                              double eps, int itmax, int istop, int* iters, double* errs, int* infos);
 
+/* ------------------------------------------------------------------------ */
+/* Adjoint of y = exp(t A) x, A symmetric (no counterpart in the reference).  */
+/* ------------------------------------------------------------------------ */
+/* Nodes / weights of the N-point optimized Talbot rule (Trefethen, Weideman,
+ * Schmelzer, BIT 46 (2006)): exp(M) b ~ Re sum_k c_k (z_k I - M)^{-1} b over
+ * the N/2 returned nodes (z, c: N interleaved complex doubles each). */
+int psfun_gpu_talbot_rule(int N, double* z, double* c);
+/* Given g = dL/dy, computes (device pointers; any output may be NULL)
+ *   y        = exp(tA) x
+ *   grad_x   = exp(tA) g                       (second Lanczos run)
+ *   *grad_t  = g^T A y                         (host scalar)
+ *   grad_vals[k] = dL/dA_ij for the k-th stored entry (i,j) of A:
+ *              t Re sum_k c_k [(z_k - tA)^{-1} g]_i [(z_k - tA)^{-1} x]_j
+ * with the nquad-point Talbot rule; the shifted solutions share the two
+ * Lanczos bases (stopped when every shifted FOM residual < eps).
+ * recompute = 1 keeps one basis in memory and rebuilds the forward one.
+ * iters[2] receives the two Krylov dimensions. */
+int psfun_gpu_d_expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps,
+                                    int itmax, int recompute, double* y, double* grad_x, double* grad_t,
+                                    double* grad_vals, int* iters);
+
 #ifdef __cplusplus
 }
 #endif

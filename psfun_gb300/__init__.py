@@ -13,7 +13,9 @@ from .api import (  # noqa: F401
     PsfunZQuadrature,
     ellipj,
     ellipkkp,
+    expm_adjoint,
     hhtmethod1,
+    talbot_rule,
     krylov_batch,
     horner,
     psb_krylov,

@@ -56,6 +56,9 @@ PROTOS = {
                                                   C.POINTER(C.c_int), dp, dp, C.c_int, C.POINTER(C.c_int)]),
     "psfun_gpu_d_krylov_batch": (C.c_int, [vp, vp, C.c_int, C.POINTER(BatchItem), C.c_double, C.c_int, C.c_int,
                                             C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]),
+    "psfun_gpu_talbot_rule": (C.c_int, [C.c_int, dp, dp]),
+    "psfun_gpu_d_expm_adjoint_device": (C.c_int, [vp, C.c_double, vp, vp, C.c_int, C.c_double, C.c_int, C.c_int, vp,
+                                                  vp, dp, vp, C.POINTER(C.c_int)]),
     "psfun_gpu_dcg": (C.c_int, [C.c_char_p, vp, C.c_char_p, dp, C.c_double, C.c_double, dp, C.c_double, C.c_int,
                                 C.c_int, C.POINTER(C.c_int), dp]),
     "psfun_gpu_dcg_device": (C.c_int, [C.c_char_p, vp, C.c_char_p, vp, C.c_double, C.c_double, vp, C.c_double,

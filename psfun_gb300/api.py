@@ -262,6 +262,43 @@ def krylov_batch(meth: "PsfunDKrylov", fun: "PsfunDSerial", items, eps: float, i
     return info, infos.reshape(count, R), iters.reshape(count, R), errs.reshape(count, R)
 
 
+def talbot_rule(N: int = 32):
+    """Nodes z_k and weights c_k (N/2 of each) of the optimized Talbot rule:
+    exp(M) b ~ Re sum_k c_k (z_k I - M)^{-1} b."""
+    z = np.zeros(N)
+    c = np.zeros(N)
+    info = _lib().psfun_gpu_talbot_rule(int(N), _dp(z), _dp(c))
+    if info != SUCCESS:
+        raise PsfunError(info, "psfun_gpu_talbot_rule")
+    return z[0::2] + 1j * z[1::2], c[0::2] + 1j * c[1::2]
+
+
+def expm_adjoint(a: CsrMatrix, t: float, x, g=None, nquad: int = 32, eps: float = 1e-15, itmax: int = 300,
+                 recompute: bool = False, want=("y", "grad_x", "grad_t", "grad_vals")):
+    """y = exp(tA) x and, given g = dL/dy, the gradients dL/dx = exp(tA) g,
+    dL/dt = g^T A y and dL/dA on the CSR pattern of A (one value per stored
+    entry).  x, g: CUDA float64 tensors.  Returns a dict of CUDA tensors / floats."""
+    import torch
+    out = {}
+    y = torch.empty_like(x) if "y" in want else None
+    gx = torch.empty_like(x) if (g is not None and "grad_x" in want) else None
+    gv = torch.empty(a.nnz, dtype=torch.float64, device=x.device) if (g is not None and "grad_vals" in want) else None
+    gt = C.c_double(0.0)
+    it = (C.c_int * 2)()
+    gg = g if g is not None else x
+    _sync_stream()
+    info = _lib().psfun_gpu_d_expm_adjoint_device(
+        a.handle, float(t), C.c_void_p(x.data_ptr()), C.c_void_p(gg.data_ptr()), int(nquad), float(eps), int(itmax),
+        1 if recompute else 0, C.c_void_p(y.data_ptr()) if y is not None else None,
+        C.c_void_p(gx.data_ptr()) if gx is not None else None,
+        C.byref(gt) if (g is not None and "grad_t" in want) else None,
+        C.c_void_p(gv.data_ptr()) if gv is not None else None, it)
+    if info != SUCCESS:
+        raise PsfunError(info, "psfun_gpu_d_expm_adjoint_device")
+    out.update(y=y, grad_x=gx, grad_t=gt.value if g is not None else None, grad_vals=gv, iters=(it[0], it[1]))
+    return out
+
+
 # ---------------------------------------------------------------------------
 def psb_krylov(method: str, a: CsrMatrix, prec: str, b, eta: float, zeta: float, x, eps: float,
                itmax: int = 1000, istop: int = 2):

@@ -169,6 +169,10 @@ PSF_DEVINL bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return done != 0;
 }
 
+PSF_DEVINL void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Waits for phase `parity` of the barrier; false after kWaitLimitNs.
 PSF_DEVINL bool mbar_wait(uint64_t* bar, unsigned parity) {
   if (mbar_try_wait(bar, parity)) return true;

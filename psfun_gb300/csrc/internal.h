@@ -131,7 +131,7 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
               int istop, int* iter, double* err);
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                       const double* x, double* y, double eps, int itmax, int* iter, double* err);
-int userf_eval(psfun_userf f, double scaling, const double* w_dev, double* fv_dev, int m);
+int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y);
 
 // Optional per-kernel timing: CUDA events recorded around selected launches
 // on the launching stream, accumulated when the solve synchronises.

@@ -191,51 +191,92 @@ __global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) 
 // Every CTA derives the scalars itself, so none is re-read from memory, and
 // CTA 0 records H, s and itx for the estimate / final kernels.
 // ---------------------------------------------------------------------------
-PSF_DEVINL bool lz_phase1(const CsrDev& A, const double* __restrict__ x, int t0, int t1, SpmvSmem& sm,
-                          double* __restrict__ u, double& acc, int* err) {
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < 2; ++q) {
-      const int t = t0 + q;
-      if (t < t1) {
-        const TileInfo ti = tile_info(A, t);
-        if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue(A, ti, sm, q);
-      }
-    }
+// Warp-specialised tile pipeline of the persistent Lanczos kernel.  The last
+// warp produces: its lane 0 stages every regular tile of the CTA's range by
+// TMA into one of two buffers, after the consumer warps have released it
+// ("empty" mbarrier, one arrival per consumer warp).  The other warps consume:
+// they wait on the buffer's "full" transaction barrier, form their rows and
+// release the buffer -- no block-wide barrier per tile.  Staged tiles are
+// counted from the start of the kernel; the n-th staged tile uses buffer n&1
+// and phase parity (n>>1)&1 on both barriers.  Because the matrix does not
+// change between steps, the producer stages the first two tiles of the next
+// step as soon as their buffers are free, overlapping that transfer with the
+// update phase and the grid barriers.  Rows longer than a tile are formed from
+// global memory by consumer warp 0 alone.
+constexpr int kConsumerWarps = kSpmvThreads / 32 - 1;
+
+struct PipeCounters {
+  unsigned issued;    // producer: tiles staged so far
+  unsigned consumed;  // consumers: tiles consumed so far
+};
+
+PSF_DEVINL bool is_regular(const CsrDev& A, int t) {
+  const int2 d0 = A.tile_desc[t], d1 = A.tile_desc[t + 1];
+  return d1.y - d0.y <= kTileNnz;
+}
+
+// Producer: stage regular tiles of [tb, te); returns false on timeout.
+PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, SpmvSmem& sm, unsigned& issued) {
+  for (int t = tb; t < te; ++t) {
+    if (!is_regular(A, t)) continue;
+    const int b = issued & 1u;
+    if (issued >= 2u && !mbar_wait(&sm.empty[b], ((issued >> 1) + 1u) & 1u)) return false;
+    spmv_issue(A, tile_info(A, t), sm, b);
+    ++issued;
   }
+  return true;
+}
+
+PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int t0, int t1, SpmvSmem& sm,
+                             double* __restrict__ u, double& acc, int* err, PipeCounters& pc, bool prefetch_next) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  bool ok = true;
+  if (warp == kConsumerWarps) {
+    if (lane == 0) {
+      // tiles t0, t0+1 were staged ahead (previous step or prologue)
+      int skip = 0, t = t0;
+      while (t < t1 && skip < 2) { if (is_regular(A, t)) ++skip; ++t; }
+      ok = pipe_produce(A, t, t1, sm, pc.issued);
+      if (ok && prefetch_next) {
+        int cnt = 0, tn = t0;
+        while (tn < t1 && cnt < 2) { if (is_regular(A, tn)) ++cnt; ++tn; }
+        ok = pipe_produce(A, t0, tn, sm, pc.issued);
+      }
+      if (!ok) atomicOr(err, DEVERR_TIMEOUT);
+    }
+    return ok;
+  }
+  const int ctid = threadIdx.x;  // 0 .. kConsumerWarps*32-1
   for (int t = t0; t < t1; ++t) {
-    const int b = (t - t0) & 1;
     const TileInfo ti = tile_info(A, t);
     if (ti.k1 - ti.k0 > kTileNnz) {
-      double s = 0.0;
-      for (int k = ti.k0 + threadIdx.x; k < ti.k1; k += blockDim.x) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
-      s = block_sum(s, sm.red);
-      if (threadIdx.x == 0) {
-        u[ti.r0] = s;
-        acc = fma(s, x[ti.r0], acc);
+      if (warp == 0) {
+        double s = 0.0;
+        for (int k = ti.k0 + lane; k < ti.k1; k += 32) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
+        s = warp_sum(s);
+        if (lane == 0) {
+          u[ti.r0] = s;
+          acc = fma(s, x[ti.r0], acc);
+        }
       }
-    } else {
-      const bool ok = mbar_wait(&sm.bar[b], sm.phase[b]);
-      if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicOr(err, DEVERR_TIMEOUT);
-        mbar_wait(&sm.bar[b], sm.phase[b]);
-        mbar_wait(&sm.bar[b ^ 1], sm.phase[b ^ 1]);
-        return false;
-      }
-      const SpmvTile& tb = sm.buf[b];
-      const int nr = ti.r1 - ti.r0;
-      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-        const int r = ti.r0 + lr;
-        const double s = spmv_row(tb, ti, lr, x);
-        u[r] = s;
-        acc = fma(s, __ldg(x + r), acc);
-      }
-      if (threadIdx.x == 0) sm.phase[b] ^= 1u;
+      continue;
     }
-    __syncthreads();  // buffer b is free
-    if (threadIdx.x == 0 && t + 2 < t1) {
-      const TileInfo tj = tile_info(A, t + 2);
-      if (tj.k1 - tj.k0 <= kTileNnz) spmv_issue(A, tj, sm, b);
+    const int b = pc.consumed & 1u;
+    if (!mbar_wait(&sm.bar[b], (pc.consumed >> 1) & 1u)) {
+      atomicOr(err, DEVERR_TIMEOUT);
+      return false;
     }
+    ++pc.consumed;
+    const SpmvTile& tb = sm.buf[b];
+    const int nr = ti.r1 - ti.r0;
+    for (int lr = ctid; lr < nr; lr += kConsumerWarps * 32) {
+      const int r = ti.r0 + lr;
+      const double s = spmv_row(tb, ti, lr, x);
+      u[r] = s;
+      acc = fma(s, __ldg(x + r), acc);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.empty[b]);
   }
   return true;
 }
@@ -252,11 +293,17 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     }
     return;
   }
-  spmv_smem_init(sm);
+  spmv_smem_init(sm, kConsumerWarps);
   const int G = gridDim.x, bid = blockIdx.x;
   const int t0 = min(A.ntiles, bid * tiles_per_cta);
   const int t1 = min(A.ntiles, t0 + tiles_per_cta);
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
+  PipeCounters pc{0u, 0u};
+  if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first two tiles
+    int cnt = 0, tn = t0;
+    while (tn < t1 && cnt < 2) { if (is_regular(A, tn)) ++cnt; ++tn; }
+    if (!pipe_produce(A, t0, tn, sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
+  }
   double sc = st.s[i_begin];
   double sprev = (i_begin >= 2) ? st.s[i_begin - 1] : 0.0;
   double beta_i = (i_begin >= 2) ? HAT(st, i_begin - 1, i_begin) : 0.0;
@@ -265,7 +312,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     const double* __restrict__ wi = WAT(st, i);
     // ---- phase 1
     double acc = 0.0;
-    lz_phase1(A, wi, t0, t1, sm, u, acc, &c->err);
+    lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
     acc = block_sum(acc, sm.red);
     if (threadIdx.x == 0) st.partials[bid] = acc;
     if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
@@ -1063,24 +1110,26 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
   }
 }
 
-int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, double eta, double sign,
-                      const double* x, double* y, double eps, int itmax, int* iter, double* err) {
-  if (!a || !xi || !cw) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
-  if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
-  if (N < 1 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
-  static psfun_krylov* meth = nullptr;
-  if (!meth) meth = new psfun_krylov();
+// Lanczos basis of A started from b, run until every shifted system
+// (xi_j I + sign A) u = b has FOM residual < eps (or itmax steps); the basis,
+// T and the scales stay in the workspace `ws`.  Returns the steps in *m.
+struct ShiftedRun {
+  KState st;
+  MsParams mp;
+  int m;
+  double err;
+};
+
+static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const double* b, int N,
+                           const double* xi_host, const double* c_host, double sign, double eps, int itmax,
+                           ShiftedRun* out) {
   const int64_t n = a->n;
   const int nl = itmax;
-  PSF_TRY(ensure_workspace(meth, n, nl, 1));
-  static DevBuf msbuf;
+  PSF_TRY(ensure_workspace(ws, n, nl, 1));
   PSF_TRY(msbuf.ensure(sizeof(double) * (4 * (size_t)N + 4 * (size_t)N + N) + 256));
-  // the final solve keeps N*m complex solutions and 4*N*m band entries
-  const size_t need = 2 * (size_t)N * nl + 8 * (size_t)N * nl + (size_t)nl + 64;
-  if (meth->scratch.bytes < sizeof(double) * need) PSF_TRY(meth->scratch.ensure(sizeof(double) * need));
   cudaStream_t s = stream();
   double* mb = msbuf.as<double>();
-  MsParams mp;
+  MsParams& mp = out->mp;
   mp.N = N;
   mp.xi = mb;
   mp.c = mb + 2 * N;
@@ -1088,19 +1137,18 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   mp.phi = mb + 6 * N;
   mp.resid = mb + 8 * N;
   mp.sign = sign;
-  mp.eta = eta;
+  mp.eta = 0.0;
   mp.eps = eps;
-  PSF_CUDA(cudaMemcpyAsync((void*)mp.xi, xi, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
-  PSF_CUDA(cudaMemcpyAsync((void*)mp.c, cw, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
-
-  KState st;
+  PSF_CUDA(cudaMemcpyAsync((void*)mp.xi, xi_host, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+  if (c_host) PSF_CUDA(cudaMemcpyAsync((void*)mp.c, c_host, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+  KState& st = out->st;
   st.n = n;
-  st.ldv = meth->ldv;
+  st.ldv = ws->ldv;
   st.nl = nl;
   st.ldh = nl + 1;
-  st.V = meth->V.as<double>();
-  st.u = meth->u.as<double>();
-  double* sm = meth->small.as<double>();
+  st.V = ws->V.as<double>();
+  st.u = ws->u.as<double>();
+  double* sm = ws->small.as<double>();
   const size_t ldh = (size_t)nl + 1;
   st.H = sm;
   st.s = sm + ldh * ldh;
@@ -1108,11 +1156,11 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   st.yk = st.rs + (ldh + 2);
   st.e1 = st.yk + (ldh + 2);
   st.coef = st.e1 + (ldh + 2);
-  st.partials = meth->partials.as<double>();
-  st.ctrl = meth->ctrl.as<KCtrl>();
-  st.fscratch = meth->scratch.as<double>();
+  st.partials = ws->partials.as<double>();
+  st.ctrl = ws->ctrl.as<KCtrl>();
+  st.fscratch = ws->scratch.as<double>();
   st.ework = nullptr;
-  PSF_CUDA(cudaMemsetAsync(sm, 0, meth->small.bytes, s));
+  PSF_CUDA(cudaMemsetAsync(sm, 0, ws->small.bytes, s));
   KCtrl h0;
   memset(&h0, 0, sizeof h0);
   h0.errden = 1.0;
@@ -1128,12 +1176,11 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   hflag[0] = 0;
   hflag[1] = 0;
   st.host_flag = dflag;
-
   const CsrDev A = a->dev();
-  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
   spmv_kernel_attrs();
   const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
-  k_init<<<gv, kVecThreads, 0, s>>>(st, x);
+  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  k_init<<<gv, kVecThreads, 0, s>>>(st, b);
   count_launch();
   for (int i = 1; i <= nl; ++i) {
     if (hflag[0]) break;
@@ -1147,17 +1194,333 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
       if (spin > 200000000L) break;
     }
   }
-  k_ms_final<<<1, kDenseThreads, 0, s>>>(st, mp);
-  k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
-  count_launch(2);
-  PSF_CUDA(cudaGetLastError());
   KCtrl hc;
   PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
   if (hc.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
   if (hc.info != 0) return hc.info;
+  out->m = hc.itx;
+  out->err = hc.errnum;
+  return PSFUN_SUCCESS;
+}
+
+int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, double eta, double sign,
+                      const double* x, double* y, double eps, int itmax, int* iter, double* err) {
+  if (!a || !xi || !cw) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (N < 1 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  static psfun_krylov* meth = nullptr;
+  if (!meth) meth = new psfun_krylov();
+  static DevBuf msbuf;
+  ShiftedRun run;
+  PSF_TRY(shifted_lanczos(meth, msbuf, a, x, N, xi, cw, sign, eps, itmax, &run));
+  // the final solve keeps N*m complex solutions and 4*N*m band entries
+  const size_t need = 2 * (size_t)N * itmax + 8 * (size_t)N * itmax + (size_t)itmax + 64;
+  if (meth->scratch.bytes < sizeof(double) * need) {
+    PSF_TRY(meth->scratch.ensure(sizeof(double) * need));
+    run.st.fscratch = meth->scratch.as<double>();
+  }
+  run.mp.eta = eta;
+  cudaStream_t s = stream();
+  const int gv = grid_for(a->n / 8 + 1, kVecThreads, 4);
+  k_ms_final<<<1, kDenseThreads, 0, s>>>(run.st, run.mp);
+  k_recombine<<<gv, kVecThreads, 0, s>>>(run.st, y);
+  count_launch(2);
+  PSF_CUDA(cudaGetLastError());
+  KCtrl hc;
+  PSF_CUDA(cudaMemcpyAsync(&hc, run.st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (hc.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
+  if (hc.info != 0) return hc.info;
   if (iter) *iter = hc.itx;
   if (err) *err = hc.errnum;
+  return PSFUN_SUCCESS;
+}
+
+// ===========================================================================
+// Adjoint of y = exp(t A) x for symmetric A.
+//
+// exp(M) is represented by the N-point optimized Talbot rule of Trefethen,
+// Weideman & Schmelzer (BIT 46 (2006) 653-670): exp(M) b ~ Re sum_k c_k
+// (z_k I - M)^{-1} b over the N/2 nodes of the upper half contour.  With
+// M = tA, u_k = (z_k I - tA)^{-1} g and v_k = (z_k I - tA)^{-1} x:
+//   dL/dx      = exp(tA) g                     (second Lanczos run, on g)
+//   dL/dt      = g^T A y
+//   dL/dA_ij   = t Re sum_k c_k u_k[i] v_k[j]  on the CSR pattern of A
+// u_k, v_k come from the Lanczos bases of g and x (FOM: v_k = V_x xi_k,
+// xi_k = (z_k - t T_x)^{-1} beta_x e1), so the sampled outer product is
+//   S = W_g R' W_x^T restricted to the pattern,
+//   R' = t diag(s_g) Re(sum_k c_k zeta_k xi_k^T) diag(s_x),
+// formed as P = W_g R' (tall FP64 GEMM) and one SDDMM pass over the CSR rows.
+// ===========================================================================
+struct AdjShifts {
+  int Nq;            // distinct shifts (upper half of the contour)
+  const double* z;   // 2*Nq
+  const double* c;   // 2*Nq (weights of the real-part rule)
+  double t;
+};
+
+// sol_k = (z_k I - t T(1:m))^{-1} beta0 e1 (banded GEPP, one thread per
+// shift); coef[p] = Re(sum_k c_k sol_k[p]) * s[p+1].
+__global__ void k_adj_solve(KState st, AdjShifts sh, int m, double* sol, double* band, double* coef,
+                            double* s_save) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const double beta0 = st.ctrl->beta0;
+  for (int k = threadIdx.x; k < sh.Nq; k += blockDim.x) {
+    const zc z = zmk(sh.z[2 * k], sh.z[2 * k + 1]);
+    zc* d = reinterpret_cast<zc*>(band) + (size_t)k * 4 * m;
+    zc* du = d + m;
+    zc* du2 = du + m;
+    zc* dl = du2 + m;
+    zc* b = reinterpret_cast<zc*>(sol) + (size_t)k * m;
+    for (int i = 0; i < m; ++i) {
+      d[i] = zsub(z, zmk(sh.t * HAT(st, i + 1, i + 1), 0.0));
+      const double off = (i + 1 < m) ? -sh.t * HAT(st, i + 2, i + 1) : 0.0;
+      du[i] = zmk(off, 0.0);
+      dl[i] = zmk(off, 0.0);
+      du2[i] = zmk(0.0, 0.0);
+      b[i] = zmk(i == 0 ? beta0 : 0.0, 0.0);
+    }
+    int fail = 0;
+    for (int i = 0; i < m - 1 && !fail; ++i) {
+      if (zabs(d[i]) < zabs(dl[i])) {
+        zc tt;
+        tt = d[i]; d[i] = dl[i]; dl[i] = tt;
+        tt = du[i]; du[i] = d[i + 1]; d[i + 1] = tt;
+        if (i + 1 < m - 1) { tt = du2[i]; du2[i] = du[i + 1]; du[i + 1] = tt; }
+        tt = b[i]; b[i] = b[i + 1]; b[i + 1] = tt;
+      }
+      if (zabs(d[i]) == 0.0) { fail = 1; break; }
+      const zc l = zdiv(dl[i], d[i]);
+      d[i + 1] = zsub(d[i + 1], zmul(l, du[i]));
+      if (i + 1 < m - 1) du[i + 1] = zsub(du[i + 1], zmul(l, du2[i]));
+      b[i + 1] = zsub(b[i + 1], zmul(l, b[i]));
+    }
+    if (!fail && zabs(d[m - 1]) == 0.0) fail = 1;
+    if (fail) { atomicOr(&bad, 1); continue; }
+    for (int i = m - 1; i >= 0; --i) {
+      zc sv = b[i];
+      if (i + 1 < m) sv = zsub(sv, zmul(du[i], b[i + 1]));
+      if (i + 2 < m) sv = zsub(sv, zmul(du2[i], b[i + 2]));
+      b[i] = zdiv(sv, d[i]);
+    }
+  }
+  __syncthreads();
+  if (bad) {
+    if (threadIdx.x == 0) { st.ctrl->info = PSFUN_ERR_FROM_SUBROUTINE_NON; atomicOr(&st.ctrl->err, DEVERR_SINGULAR); }
+    return;
+  }
+  for (int p = threadIdx.x; p < m; p += blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < sh.Nq; ++k)
+      acc += cuCreal(zmul(zmk(sh.c[2 * k], sh.c[2 * k + 1]), reinterpret_cast<const zc*>(sol)[(size_t)k * m + p]));
+    coef[p] = acc * st.s[p + 1];
+  }
+  for (int p = threadIdx.x; p < m + 2; p += blockDim.x) s_save[p] = st.s[p];
+}
+
+// R'[p][q] = t s_g[p+1] s_x[q+1] Re sum_k c_k zeta_k[p] xi_k[q]
+__global__ void k_adj_R(AdjShifts sh, int mg, int mx, const double* solg, const double* solx, const double* sg,
+                        const double* sx, double* R) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < mg * mx; e += gridDim.x * blockDim.x) {
+    const int p = e / mx, q = e - p * mx;
+    double acc = 0.0;
+    for (int k = 0; k < sh.Nq; ++k) {
+      const zc ck = zmk(sh.c[2 * k], sh.c[2 * k + 1]);
+      const zc zg = reinterpret_cast<const zc*>(solg)[(size_t)k * mg + p];
+      const zc zx = reinterpret_cast<const zc*>(solx)[(size_t)k * mx + q];
+      acc += cuCreal(zmul(ck, zmul(zg, zx)));
+    }
+    R[e] = sh.t * sg[p + 1] * sx[q + 1] * acc;
+  }
+}
+
+// y = sum_p coef[p] W_p (p < m)
+__global__ void __launch_bounds__(kVecThreads) k_lincomb(const double* V, int64_t ldv, int64_t n, const double* coef,
+                                                         int m, double* y) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int p = 0; p < m; ++p) acc = fma(coef[p], V[(size_t)p * ldv + r], acc);
+    y[r] = acc;
+  }
+}
+
+constexpr int kAdjChunk = 16;
+
+// P[q][i] = sum_p Wg[p][i] R'[p][q], q in chunks of 16 held in registers
+__global__ void __launch_bounds__(kVecThreads) k_adj_P(const double* Wg, int64_t ldg, int mg, const double* R, int mx,
+                                                       int64_t n, double* P, int64_t ldp) {
+  extern __shared__ double Rs[];  // mg x kAdjChunk
+  for (int q0 = 0; q0 < mx; q0 += kAdjChunk) {
+    const int qn = min(kAdjChunk, mx - q0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < mg * kAdjChunk; e += blockDim.x) {
+      const int p = e / kAdjChunk, qq = e - p * kAdjChunk;
+      Rs[e] = (qq < qn) ? R[(size_t)p * mx + q0 + qq] : 0.0;
+    }
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      double acc[kAdjChunk];
+#pragma unroll
+      for (int qq = 0; qq < kAdjChunk; ++qq) acc[qq] = 0.0;
+      for (int p = 0; p < mg; ++p) {
+        const double w = Wg[(size_t)p * ldg + i];
+#pragma unroll
+        for (int qq = 0; qq < kAdjChunk; ++qq) acc[qq] = fma(w, Rs[p * kAdjChunk + qq], acc[qq]);
+      }
+      for (int qq = 0; qq < qn; ++qq) P[(size_t)(q0 + qq) * ldp + i] = acc[qq];
+    }
+  }
+}
+
+// grad[k] = sum_q P[q][i] Wx[q][ja[k]] for every stored entry k of row i
+__global__ void __launch_bounds__(kVecThreads) k_adj_sddmm(CsrDev A, const double* P, int64_t ldp, const double* Wx,
+                                                           int64_t ldx, int mx, double* grad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int kb = A.irp[i], ke = A.irp[i + 1];
+    for (int q0 = 0; q0 < mx; q0 += kAdjChunk) {
+      const int qn = min(kAdjChunk, mx - q0);
+      double pi[kAdjChunk];
+#pragma unroll
+      for (int qq = 0; qq < kAdjChunk; ++qq) pi[qq] = (qq < qn) ? P[(size_t)(q0 + qq) * ldp + i] : 0.0;
+      for (int k = kb; k < ke; ++k) {
+        const int j = A.ja[k];
+        double acc = (q0 == 0) ? 0.0 : grad[k];
+        for (int qq = 0; qq < qn; ++qq) acc = fma(pi[qq], __ldg(Wx + (size_t)(q0 + qq) * ldx + j), acc);
+        grad[k] = acc;
+      }
+    }
+  }
+}
+
+// out = g . v (two-pass, deterministic)
+__global__ void __launch_bounds__(kVecThreads) k_dot_partial(const double* a, const double* b, int64_t n, double* part) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    acc = fma(a[r], b[r], acc);
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+__global__ void k_dot_final(const double* part, int nb, double* out) {
+  __shared__ double red[32];
+  const double v = block_sum_array(part, nb, red);
+  if (threadIdx.x == 0) *out = v;
+}
+
+int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps, int itmax,
+                        int recompute, double* y, double* grad_x, double* grad_t, double* grad_vals, int* iters) {
+  if (!a || !x || !g) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (nquad < 4 || (nquad & 1) || itmax < 2 || t == 0.0) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const int Nq = nquad / 2;
+  std::vector<double> zc_h(2 * Nq), cw_h(2 * Nq), xi_h(2 * Nq);
+  if (psfun_gpu_talbot_rule(nquad, zc_h.data(), cw_h.data()) != PSFUN_SUCCESS) return PSFUN_ERR_INTERNAL;
+  // monitor form: (z I - tA) = |t| ((z/|t|) I + sign A), sign = -sgn(t)
+  const double at = fabs(t), sign = (t > 0) ? -1.0 : 1.0;
+  for (int k = 0; k < 2 * Nq; ++k) xi_h[k] = zc_h[k] / at;
+  static psfun_krylov* wsx = nullptr;
+  static psfun_krylov* wsg = nullptr;
+  if (!wsx) wsx = new psfun_krylov();
+  if (!wsg) wsg = new psfun_krylov();
+  psfun_krylov* wg = recompute ? wsx : wsg;
+  static DevBuf msb, adj, pbuf, tmpv;
+  cudaStream_t s = stream();
+  const int64_t n = a->n;
+  const int64_t ld = (n + 31) & ~(int64_t)31;
+  // small buffers: shifts, solutions, bands, coefficients, saved scales, R
+  const size_t nsmall = 4 * (size_t)Nq + 2 * (2 * (size_t)Nq * itmax) + 8 * (size_t)Nq * itmax + 4 * (size_t)itmax +
+                        2 * (size_t)(itmax + 2) + (size_t)itmax * itmax + 4096 + 64;
+  PSF_TRY(adj.ensure(sizeof(double) * nsmall));
+  double* ab = adj.as<double>();
+  double* dz = ab;
+  double* dc = dz + 2 * Nq;
+  double* solx = dc + 2 * Nq;
+  double* solg = solx + 2 * (size_t)Nq * itmax;
+  double* band = solg + 2 * (size_t)Nq * itmax;
+  double* coefy = band + 8 * (size_t)Nq * itmax;
+  double* coefg = coefy + itmax;
+  double* sx = coefg + itmax;
+  double* sg = sx + (itmax + 2);
+  double* R = sg + (itmax + 2);
+  double* part = R + (size_t)itmax * itmax;
+  double* gt = part + 4000;
+  PSF_CUDA(cudaMemcpyAsync(dz, zc_h.data(), sizeof(double) * 2 * Nq, cudaMemcpyHostToDevice, s));
+  PSF_CUDA(cudaMemcpyAsync(dc, cw_h.data(), sizeof(double) * 2 * Nq, cudaMemcpyHostToDevice, s));
+  AdjShifts sh{Nq, dz, dc, t};
+  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  PSF_TRY(tmpv.ensure(sizeof(double) * ld * 2));
+  double* ytmp = y ? y : tmpv.as<double>();
+  double* Ay = tmpv.as<double>() + ld;
+
+  // forward basis (x): y = exp(tA) x
+  ShiftedRun rx;
+  PSF_TRY(shifted_lanczos(wsx, msb, a, x, Nq, xi_h.data(), nullptr, sign, eps, itmax, &rx));
+  const int mx = rx.m;
+  if (mx < 1) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  k_adj_solve<<<1, 32, 0, s>>>(rx.st, sh, mx, solx, band, coefy, sx);
+  k_lincomb<<<gv, kVecThreads, 0, s>>>(rx.st.V, rx.st.ldv, n, coefy, mx, ytmp);
+  count_launch(2);
+  if (!grad_x && !grad_t && !grad_vals) {  // forward only
+    KCtrl hx;
+    PSF_CUDA(cudaMemcpyAsync(&hx, rx.st.ctrl, sizeof hx, cudaMemcpyDeviceToHost, s));
+    PSF_CUDA(cudaStreamSynchronize(s));
+    if (hx.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
+    if (hx.info) return hx.info;
+    if (iters) { iters[0] = mx; iters[1] = 0; }
+    return PSFUN_SUCCESS;
+  }
+  // adjoint basis (g): dL/dx = exp(tA) g
+  ShiftedRun rg;
+  PSF_TRY(shifted_lanczos(wg, msb, a, g, Nq, xi_h.data(), nullptr, sign, eps, itmax, &rg));
+  const int mg = rg.m;
+  if (mg < 1) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  k_adj_solve<<<1, 32, 0, s>>>(rg.st, sh, mg, solg, band, coefg, sg);
+  count_launch();
+  if (grad_x) {
+    k_lincomb<<<gv, kVecThreads, 0, s>>>(rg.st.V, rg.st.ldv, n, coefg, mg, grad_x);
+    count_launch();
+  }
+  if (grad_vals) {
+    k_adj_R<<<std::max(1, (mg * mx + 255) / 256), 256, 0, s>>>(sh, mg, mx, solg, solx, sg, sx, R);
+    PSF_TRY(pbuf.ensure(sizeof(double) * (size_t)mx * ld));
+    k_adj_P<<<gv, kVecThreads, sizeof(double) * mg * kAdjChunk, s>>>(rg.st.V, rg.st.ldv, mg, R, mx, n,
+                                                                       pbuf.as<double>(), ld);
+    count_launch(2);
+    const double* Wx = rx.st.V;
+    int64_t ldx = rx.st.ldv;
+    if (recompute) {  // rebuild the forward basis over the adjoint one
+      ShiftedRun rx2;
+      PSF_TRY(shifted_lanczos(wsx, msb, a, x, Nq, xi_h.data(), nullptr, sign, eps, itmax, &rx2));
+      if (rx2.m != mx) {
+        set_last_error("recomputed forward basis differs");
+        return PSFUN_ERR_INTERNAL;
+      }
+      Wx = rx2.st.V;
+      ldx = rx2.st.ldv;
+    }
+    k_adj_sddmm<<<gv, kVecThreads, 0, s>>>(a->dev(), pbuf.as<double>(), ld, Wx, ldx, mx, grad_vals);
+    count_launch();
+  }
+  if (grad_t) {
+    PSF_TRY(spmv_device(a, 1.0, ytmp, 0.0, Ay));
+    const int nb = std::min(gv, 4000);
+    k_dot_partial<<<nb, kVecThreads, 0, s>>>(g, Ay, n, part);
+    k_dot_final<<<1, 256, 0, s>>>(part, nb, gt);
+    count_launch(2);
+    PSF_CUDA(cudaMemcpyAsync(grad_t, gt, sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  PSF_CUDA(cudaGetLastError());
+  KCtrl hx, hg;
+  PSF_CUDA(cudaMemcpyAsync(&hg, rg.st.ctrl, sizeof hg, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (!recompute) PSF_CUDA(cudaMemcpy(&hx, rx.st.ctrl, sizeof hx, cudaMemcpyDeviceToHost));
+  else hx = hg;
+  if ((hg.err | hx.err) & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
+  if (hg.info) return hg.info;
+  if (hx.info) return hx.info;
+  if (iters) { iters[0] = mx; iters[1] = mg; }
   return PSFUN_SUCCESS;
 }
 
@@ -1169,6 +1532,12 @@ int psfun_gpu_z_quadrature_apply_device(psfun_csr* a, int N, const double* xi, c
                                         double sign, const double* x, double* y, double eps, int itmax, int* iter,
                                         double* err) {
   return psf::quad_apply_device(a, N, xi, c, eta, sign, x, y, eps, itmax, iter, err);
+}
+
+int psfun_gpu_d_expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps,
+                                    int itmax, int recompute, double* y, double* grad_x, double* grad_t,
+                                    double* grad_vals, int* iters) {
+  return psf::expm_adjoint_device(a, t, x, g, nquad, eps, itmax, recompute, y, grad_x, grad_t, grad_vals, iters);
 }
 
 int psfun_gpu_z_quadrature_apply(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,

@@ -207,4 +207,33 @@ int psfun_gpu_hhtmethod1(psfun_zfun zfun, void* ctx, int N, const double* rparam
   return PSFUN_SUCCESS;
 }
 
+// Optimized Talbot contour of Trefethen, Weideman & Schmelzer, "Talbot
+// quadratures and rational approximations", BIT 46 (2006) 653-670:
+//   z(th) = N (0.5017 th cot(0.6407 th) - 0.6122 + 0.2645 i th),  -pi < th < pi,
+// midpoint rule th_k = -pi + (k - 1/2) 2 pi / N, so that
+//   exp(M) b ~ sum_k c_k (z_k I - M)^{-1} b,  c_k = exp(z_k) z'(th_k) / (i N).
+// For real M and b the nodes th and -th give conjugate terms; this returns the
+// N/2 nodes with th > 0 and weights 2 c_k, to be used with the real part.
+int psfun_gpu_talbot_rule(int N, double* z, double* c) {
+  if (N < 2 || (N & 1) || !z || !c) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const double mu = 0.5017, nu = 0.6407, sigma = -0.6122, beta = 0.2645;
+  const zd I(0.0, 1.0);
+  int j = 0;
+  for (int k = 1; k <= N; ++k) {
+    const double th = -kPi + (k - 0.5) * 2.0 * kPi / N;
+    if (th <= 0.0) continue;
+    const double cot = std::cos(nu * th) / std::sin(nu * th);
+    const double sn = std::sin(nu * th);
+    const zd zk = (double)N * zd(mu * th * cot + sigma, beta * th);
+    const zd dz = (double)N * zd(mu * (cot - nu * th / (sn * sn)), beta);
+    const zd ck = 2.0 * std::exp(zk) * dz / (I * (double)N);
+    z[2 * j] = zk.real();
+    z[2 * j + 1] = zk.imag();
+    c[2 * j] = ck.real();
+    c[2 * j + 1] = ck.imag();
+    ++j;
+  }
+  return PSFUN_SUCCESS;
+}
+
 }  // extern "C"

@@ -20,7 +20,7 @@
 namespace psf {
 
 constexpr int kSpmvThreads = 512;
-constexpr int kTileRows = 512;
+constexpr int kTileRows = 480;  // 15 consumer warps x 32 in the warp-specialised pipeline
 constexpr int kTileNnz = 4096;
 static_assert(((kTileNnz + 2) * 8) % 16 == 0, "ja must start 16-byte aligned");
 
@@ -49,7 +49,8 @@ static_assert(sizeof(int32_t) * (kTileNnz + 4) % 16 == 0, "irp offset");
 
 struct __align__(128) SpmvSmem {
   SpmvTile buf[2];
-  uint64_t bar[2];
+  uint64_t bar[2];    // "full": TMA transaction barriers
+  uint64_t empty[2];  // "empty": released by the consumer warps (pipelined kernels)
   unsigned phase[2];
   int next_tile;
   int cur_tile;
@@ -70,10 +71,12 @@ inline void spmv_smem_attr(K kernel) {
 }
 
 // Once per kernel, before the first spmv_tiles call.
-PSF_DEVINL void spmv_smem_init(SpmvSmem& sm) {
+PSF_DEVINL void spmv_smem_init(SpmvSmem& sm, unsigned empty_count = 1) {
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
+    mbar_init(&sm.empty[0], empty_count);
+    mbar_init(&sm.empty[1], empty_count);
     sm.phase[0] = sm.phase[1] = 0;
   }
   __syncthreads();
