@@ -113,6 +113,16 @@ int psfun_gpu_serial_apply(psfun_serial* fun, int n, const double* a, int lda, d
 /* Sparse input: psfun_d_serial_apply_sparse (:525-568), dense conversion on
  * the device. */
 int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, const double* x);
+/* No counterpart in the reference.  y = f(scaling*a) x as psfun_gpu_serial_apply,
+ * with device pointers a (lda), x, y, for callers that must not allocate device
+ * memory: its scratch is one static 1 MiB __device__ array per device, held
+ * until the process exits, instead of a cudaMalloc/cudaFree pair per call
+ * (cudaFree waits for the whole device).  Accepts n <= 64 and phiorder <= 8;
+ * larger sizes and USERF return 111 with a message in psfun_gpu_last_error.
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture.  Calls that overlap on the GPU race on the array. */
+int psfun_gpu_serial_apply_device_static(psfun_serial* fun, int n, const double* a, int lda, double* y,
+                                         const double* x);
 
 /* ------------------------------------------------------------------------ */
 /* Krylov method object: type psfun_d_krylov                                 */

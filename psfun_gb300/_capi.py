@@ -46,6 +46,7 @@ PROTOS = {
     "psfun_gpu_serial_get": (C.c_int, [vp, C.c_char_p, C.c_char_p, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "psfun_gpu_serial_apply": (C.c_int, [vp, C.c_int, dp, C.c_int, dp, dp]),
     "psfun_gpu_serial_apply_sparse": (C.c_int, [vp, vp, dp, dp]),
+    "psfun_gpu_serial_apply_device_static": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp]),
     "psfun_gpu_krylov_create": (C.c_int, [C.POINTER(vp)]),
     "psfun_gpu_krylov_destroy": (C.c_int, [vp]),
     "psfun_gpu_krylov_set_string": (C.c_int, [vp, C.c_char_p, C.c_char_p]),

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "internal.h"
 
@@ -1561,3 +1562,104 @@ int psfun_gpu_z_quadrature_apply(psfun_csr* a, int N, const double* xi, const do
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Serial apply with static scratch: the dense f(scaling*a) x of
+// serial_apply_device for callers that must not allocate device memory.
+//
+// serial_apply_device takes its scratch from cudaMalloc and returns it with
+// cudaFree on every call.  cudaFree waits for all work on the device, so a
+// caller that evaluates a small dense f(H)x inside a running pipeline (an
+// exponential integrator stepping on one stream while other streams of the
+// same device keep working, or a host loop whose device memory is owned by
+// another allocator, such as torch's caching allocator) stalls every stream
+// or competes with that allocator for memory.  This variant takes its scratch
+// from one file-scope __device__ array instead and calls no allocating routine.
+//
+// The array holds kSerialStaticDoubles doubles (1 MiB) and is resident on every
+// device that loads the library until the process exits.  Accepted sizes:
+// n <= kSerialStaticMaxN (64) and, for PHI, phiorder <= kSerialStaticMaxPhi (8);
+// larger requests are rejected with PSFUN_ERR_INVALID_ARGS_COMBINATION.
+// Every call on a device shares the array and finds the previous call's
+// contents in it: the dense kernels write every scratch entry before reading
+// it (the Krylov workspace is reused the same way), and the status word is
+// cleared before each launch.  Calls that overlap on the GPU (two streams, or
+// two host threads) race on the array.
+// ===========================================================================
+namespace psf {
+
+constexpr int kSerialStaticMaxN = 64;
+constexpr int kSerialStaticMaxPhi = 8;
+constexpr size_t kSerialStaticDoubles = 128 * 1024;
+constexpr int kSerialStaticMaxDevices = 64;
+
+static __device__ __align__(256) double g_serial_static_scratch[kSerialStaticDoubles];
+
+static std::mutex g_serial_static_mu;
+static double* g_serial_static_ptr[kSerialStaticMaxDevices];
+
+// Device address of the array on the current device, looked up once per
+// device (the first call on a device does it, with that device current).
+static int serial_static_scratch(double** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return PSFUN_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kSerialStaticMaxDevices) {
+    set_last_error("serial_apply_static: device ordinal beyond the static table");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  std::lock_guard<std::mutex> lk(g_serial_static_mu);
+  if (!g_serial_static_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_serial_static_scratch);
+    if (e != cudaSuccess) {
+      set_last_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return PSFUN_ERR_CUDA;
+    }
+    g_serial_static_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_serial_static_ptr[dev];
+  return PSFUN_SUCCESS;
+}
+
+static int serial_apply_static(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev,
+                               const double* x_dev) {
+  if (!fun) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (!a_dev || !x_dev || !y_dev) return PSFUN_ERR_INVALID_VECT_STATE;
+  if (n < 1 || lda < n) return PSFUN_ERR_FROM_SUBROUTINE;
+  FunParams fp;
+  if (!parse_fun(fun, &fp)) return PSFUN_ERR_FROM_SUBROUTINE;
+  if (fp.fname == FN_USERF) {
+    set_last_error("serial_apply_static: USERF evaluates f on the host and is not supported here");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  // status word (one double slot) + dense scratch, as serial_apply_device
+  const size_t fs = fh_scratch_doubles(n, fp.phiorder) + 4 * (size_t)n * n + 8 * (size_t)n;
+  if (n > kSerialStaticMaxN || (fp.fname == FN_PHI && fp.phiorder > kSerialStaticMaxPhi) ||
+      fs + 32 > kSerialStaticDoubles) {
+    set_last_error("serial_apply_static: size beyond the static scratch (n <= 64, phiorder <= 8)");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  double* scr = nullptr;
+  PSF_TRY(serial_static_scratch(&scr));
+  int* dstat = reinterpret_cast<int*>(scr + fs);
+  cudaStream_t s = stream();
+  PSF_CUDA(cudaMemsetAsync(dstat, 0xff, sizeof(int), s));
+  k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr, dstat);
+  count_launch();
+  PSF_CUDA(cudaGetLastError());
+  int hs = -1;
+  PSF_CUDA(cudaMemcpyAsync(&hs, dstat, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  return hs == 0 ? PSFUN_SUCCESS : PSFUN_ERR_FROM_SUBROUTINE;
+}
+
+}  // namespace psf
+
+extern "C" int psfun_gpu_serial_apply_device_static(psfun_serial* fun, int n, const double* a, int lda, double* y,
+                                                    const double* x) {
+  return psf::serial_apply_static(fun, n, a, lda, y, x);
+}
