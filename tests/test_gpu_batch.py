@@ -30,6 +30,21 @@ def plain(A, x, t, eps, itmax, istop=1):
     return meth.apply(fun, pg.CsrMatrix.from_scipy(t * A), x, eps, itmax=itmax, istop=istop)
 
 
+def oracle_spread(orc, A, x, t, eps, itmax, istop):
+    """Relative change of the oracle's result when only its reduction order
+    changes (1 against 4 OpenMP threads): the FP64 reproducibility floor of the
+    case.  It is ~1e-15 for the converged cases and reaches ~3e-10 on the kNN
+    graph with n = 4100, whose 39 unconverged steps amplify rounding."""
+    prev = orc.set_threads(0)
+    ys = []
+    for th in (1, 4):
+        orc.set_threads(th)
+        ys.append(orc.krylov("LANCZOS", orc.serial("EXP", "CHBSYM", 1.0), orc.Csr.from_scipy(t * A), x, eps,
+                             itmax=itmax, istop=istop)["y"])
+    orc.set_threads(prev)
+    return np.linalg.norm(ys[0] - ys[1]) / np.linalg.norm(ys[0])
+
+
 @pytest.mark.parametrize("istop", [1, 2])
 @pytest.mark.parametrize("R", [1, 4])
 def test_batch_matches_plain(lib, orc, istop, R):
@@ -59,8 +74,10 @@ def test_batch_matches_plain(lib, orc, istop, R):
                            itmax=itmax, istop=istop)
             assert r.info == 0 and o["info"] == 0
             assert iters[k, q] == r.iter == o["iter"], (k, q, iters[k, q], r.iter, o["iter"])
-            assert np.linalg.norm(Y[q] - r.y) <= 1e-10 * np.linalg.norm(r.y), (k, q)
-            assert np.linalg.norm(Y[q] - o["y"]) <= 1e-10 * np.linalg.norm(o["y"]), (k, q)
+            # 1e-10, or 10x the oracle's own reduction-order spread where that is larger
+            tol = max(1e-10, 10 * oracle_spread(orc, A, X[q], t, eps, itmax, istop))
+            assert np.linalg.norm(Y[q] - r.y) <= tol * np.linalg.norm(r.y), (k, q, tol)
+            assert np.linalg.norm(Y[q] - o["y"]) <= tol * np.linalg.norm(o["y"]), (k, q, tol)
 
 
 def test_batch_zero_rhs_and_errors(lib):
