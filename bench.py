@@ -10,8 +10,11 @@ reference (psfun_d_lanczos.f90:172-173), so the matrix passed is -0.05 A.
   value      solves/s with x, y and A resident in HBM (device-pointer C-ABI)
   e2e        solves/s through the host-pointer C-ABI (x pinned on the host,
              H2D of x and D2H of y inside every step)
-  roofline   the Lanczos SpMV+dot kernel: algorithmic bytes per launch
-             (12 nnz + 4 (n+1) + 16 n) / its CUDA-event launch time
+  roofline   k_lz_persist, the cooperative kernel that runs all 80 Lanczos
+             steps: algorithmic bytes per launch (80 (B_spmv + 32 n) - 8 n,
+             B_spmv = 12 nnz + 4 (n+1) + 16 n) / its CUDA-event launch time;
+             also its FP64 multiply-adds against cuBLAS DGEMM, since GB300's
+             FP64 rate is of the same order as the HBM stream of this step
   cpu_baseline  the CPU restatement (oracle) on the host cores
 
 --impl reference runs the reference's algorithm on the host CPU instead (the
@@ -52,6 +55,32 @@ def dist_info():
 def algorithmic_bytes(n: int, nnz: int):
     b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
     return dict(spmv=b_spmv, update=32 * n, step=b_spmv + 32 * n)
+
+
+def persist_bytes(n: int, nnz: int, steps: int) -> int:
+    """Algorithmic bytes of one k_lz_persist launch over Lanczos steps 1..steps:
+    per step the SpMV (B_spmv) and the three-term update (read u, v_i, v_{i-1},
+    write v_{i+1}: 32 n); step 1 has no v_{i-1}."""
+    b = algorithmic_bytes(n, nnz)
+    return steps * b["step"] - 8 * n
+
+
+def dgemm_fma_rate(torch, size: int = 4096, reps: int = 3) -> float:
+    """FP64 multiply-adds per second of cuBLAS DGEMM on this GPU (the FP64 peak
+    the Lanczos step is held against)."""
+    a = torch.randn(size, size, dtype=torch.float64, device="cuda")
+    b = torch.randn(size, size, dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        c = a @ b
+    e1.record()
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / reps / 1e3
+    del a, b, c
+    return size ** 3 / dt
 
 
 class ClockSampler:
@@ -200,6 +229,103 @@ def bench_batched(torch, pg, scale: float = 1.0, reps: int = 2):
             "max_iters": int(np.max(iters))}
 
 
+def _time_dev(torch, fn, reps: int):
+    stream = torch.cuda.current_stream()
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps / 1e3, out
+
+
+def bench_arnoldi_phi(torch, pg, peak_gbs: float, reps: int = 3):
+    """phi_1(-1e-3 A) x on the 2-D convection-diffusion operator 2048^2
+    (n = 4,194,304, nnz = 20,963,328) by Arnoldi with Krylov dimension 60
+    (istop 2).  Bytes per solve: sum over steps i = 1..60 of one SpMV plus the
+    one-pass modified Gram-Schmidt of the new vector against the i previous
+    ones, B_spmv + 8 n i + 16 n."""
+    from psfun_gb300 import matrices
+    p = matrices.config2b()
+    A, x = p.A, p.x
+    n, nnz, m = A.shape[0], A.nnz, 60
+    a = pg.CsrMatrix.from_scipy(A)
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "PHI")
+    fun.set("PHIORDER", 1)
+    fun.set("SCALING", -1e-3)
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "ARNOLDI")
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.empty_like(xd)
+    dt, r = _time_dev(torch, lambda: meth.apply(fun, a, xd, 1e-12, itmax=m, istop=2, y=yd), reps)
+    assert r.info == 0, r.info
+    b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    nbytes = sum(b_spmv + 8 * n * i + 16 * n for i in range(1, m + 1)) + 8 * n * m
+    yconv = meth.apply(fun, a, xd, 1e-14, itmax=200, istop=1).y
+    rel = float(torch.linalg.norm(yd - yconv) / torch.linalg.norm(yconv))
+    del a, xd, yd, yconv
+    return {"workload": "2-D convection-diffusion 2048^2 (n=4,194,304, nnz=20,963,328), y=phi_1(-1e-3 A)x, "
+                        "Arnoldi m=60 (istop 2)",
+            "ms_per_solve": 1e3 * dt, "solves_per_s": 1.0 / dt, "algorithmic_bytes_per_solve": nbytes,
+            "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs,
+            "rel_diff_m60_vs_converged": rel}
+
+
+def bench_multishift(torch, pg, peak_gbs: float, reps: int = 3):
+    """A^{-1/2} x on the 3-D 7-point Laplacian 96^3 (n = 884,736) through the
+    HHT conformal-map rule with N = 24 shifts, all shifted systems solved on one
+    shared Lanczos basis (tolerance 1e-10 on every shift).  Bytes per iteration:
+    B_spmv + 32 n (the Lanczos step), plus 8 n per basis vector for the final
+    recombination."""
+    from psfun_gb300 import matrices
+    p = matrices.config3()
+    A, x = p.A, p.x
+    n, nnz = A.shape[0], A.nnz
+    q = pg.PsfunZQuadrature()
+    info = q.computepoles(pg.hhtmethod1, lambda z: 1.0 / np.sqrt(z), 24,
+                          rparams=list(matrices.laplacian_3d_bounds(96)))
+    assert info == 0
+    q.setmatrix(pg.CsrMatrix.from_scipy(A))
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.empty_like(xd)
+    dt, (y, info, it, err) = _time_dev(torch, lambda: q.apply(xd, eps=1e-10, itmax=3000, y=yd), reps)
+    assert info == 0, info
+    b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    nbytes = it * (b_spmv + 32 * n) + 8 * n * (it + 1)
+    return {"workload": "3-D 7-point Laplacian 96^3 (n=884,736, nnz=6,137,856), y=A^{-1/2}x, HHT rule N=24, "
+                        "multi-shift on one Lanczos basis, eps 1e-10",
+            "ms_per_solve": 1e3 * dt, "iterations": int(it), "max_shift_residual": float(err),
+            "algorithmic_bytes_per_solve": nbytes, "achieved_GBs": nbytes / dt / 1e9,
+            "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs}
+
+
+def bench_adjoint(torch, pg, reps: int = 3):
+    """Gradient of L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2 on the 512 x 512
+    grid-graph Laplacian (n = 262,144, 523,264 edge weights theta): the cost of
+    the forward exp(tA)x against forward plus all gradients (x, t, and every
+    stored entry of A, from which dL/dtheta follows by the chain rule)."""
+    from psfun_gb300 import matrices
+    cfg = matrices.config5()
+    N, ei, ej = cfg["N"], cfg["ei"], cfg["ej"]
+    n = N * N
+    a = pg.CsrMatrix.from_scipy(matrices.graph_laplacian(n, ei, ej, cfg["theta"]))
+    astar = pg.CsrMatrix.from_scipy(matrices.graph_laplacian(n, ei, ej, cfg["theta_star"]))
+    x = torch.tensor(cfg["x"], device="cuda")
+    t = -cfg["t"]
+    ystar = pg.expm_adjoint(astar, t, x, None, want=("y",))["y"]
+    t_fwd, out = _time_dev(torch, lambda: pg.expm_adjoint(a, t, x, None, want=("y",)), reps)
+    g = out["y"] - ystar
+    t_all, out2 = _time_dev(torch, lambda: pg.expm_adjoint(a, t, x, g), reps)
+    return {"workload": "512x512 grid-graph Laplacian (n=262,144, 523,264 edges), L=1/2||exp(-0.1A)x-y*||^2, "
+                        "gradients w.r.t. x, t and every stored entry of A (32-point Talbot rule, eps 1e-15)",
+            "forward_ms": 1e3 * t_fwd, "forward_plus_gradients_ms": 1e3 * t_all,
+            "cost_ratio_vs_forward": t_all / t_fwd, "krylov_dims": list(out2["iters"])}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -346,16 +472,18 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # k_lz_persist: one cooperative launch runs all M_KRYLOV Lanczos steps
     cnt, tot = prof["lz_spmv"]
-    spmv_ms = tot / max(cnt, 1)
-    achieved = nbytes["spmv"] / (spmv_ms * 1e-3) / 1e9
-    ucnt, utot = prof["lz_update"]
-    upd_ms = utot / max(ucnt, 1)
+    launch_ms = tot / max(cnt, 1)
+    bytes_launch = persist_bytes(n, nnz, M_KRYLOV)
+    fma_launch = M_KRYLOV * (nnz + 4 * n)
+    achieved = bytes_launch / (launch_ms * 1e-3) / 1e9
+    fp64_peak = dgemm_fma_rate(torch)
     traffic = None
-    tf = ROOT / "profiles" / "lanczos_spmv_128cube_traffic.json"
+    tf = ROOT / "profiles" / "lanczos_persist_128cube_traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
-    step_ms = spmv_ms + upd_ms
+    step_ms = launch_ms / M_KRYLOV
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -364,18 +492,28 @@ def main():
                    "l2": "inputs larger than L2 (matrix 183 MB + 81-vector basis 1.36 GB > 129 MB L2)"},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "k_lz_spmv (SpMV + fused alpha dot)",
+                     "traffic": traffic,
+                     "kernel": f"k_lz_persist (all {M_KRYLOV} Lanczos steps in one cooperative launch: SpMV + "
+                               "alpha dot, grid barrier, three-term update + norm, grid barrier)",
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_launch": nbytes["spmv"], "launch_ms": spmv_ms},
-        "lanczos_step": {"spmv_ms": spmv_ms, "update_ms": upd_ms, "step_ms": step_ms,
-                         "step_algorithmic_bytes": nbytes["step"],
+                     "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": launch_ms,
+                     "fp64": {"fma_per_launch": fma_launch, "achieved_gfma_s": fma_launch / (launch_ms * 1e-3) / 1e9,
+                              "peak_gfma_s": fp64_peak / 1e9,
+                              "frac": fma_launch / (launch_ms * 1e-3) / fp64_peak,
+                              "peak_source": "measured in this run: cuBLAS DGEMM (torch.matmul, 4096^3 float64)"}},
+        "lanczos_step": {"step_ms": step_ms, "step_algorithmic_bytes": nbytes["step"],
                          "step_GBs": nbytes["step"] / (step_ms * 1e-3) / 1e9,
-                         "solve_GBs": (M_KRYLOV * nbytes["step"] + 8 * n * (M_KRYLOV + 1)) / (ms_per_step * 1e-3)
-                         / 1e9},
+                         "solve_GBs": (bytes_launch + 8 * n * (M_KRYLOV + 1)) / (ms_per_step * 1e-3) / 1e9},
         "clocks": clk,
         "gpu_launches": int(launches),
         "accuracy": {"rel_diff_m80_vs_converged": rel_conv},
     }
+    if rank == 0 and world == 1 and not args.no_secondary:
+        line["arnoldi_phi1"] = bench_arnoldi_phi(torch, pg, peak)
+        torch.cuda.empty_cache()
+        line["multishift"] = bench_multishift(torch, pg, peak)
+        line["adjoint"] = bench_adjoint(torch, pg)
+        torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_secondary:
         line["batched"] = bench_batched(torch, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -77,6 +77,45 @@ PSF_DEVINL double block_max(double v, double* red) {
   return t;
 }
 
+// Thread 0 stores the sum of the block's values to *out, in the order of
+// block_sum.  `red` must not be in use by another block-wide reduction (the
+// caller separates consecutive uses by a block barrier).
+PSF_DEVINL void block_sum_store(double v, double* red, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double t = (lane < nw) ? red[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) *out = t;
+  }
+}
+
+// Sum of p[0..count) (count <= 256), bit-identical to block_sum_array(p,
+// count) run by a block of at least `count` threads, formed with less latency:
+// warps 0..7 reduce one chunk of 32 partials each in parallel, and thread 0
+// adds the chunk sums in the order of the second butterfly of block_sum
+// (chunks past the last are exact zeros there).  Only thread 0 gets the total.
+PSF_DEVINL double partials_sum_to0(const volatile double* p, int count, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nch = (count + 31) >> 5;
+  if (wid < nch) {
+    double v = (32 * wid + lane < count) ? p[32 * wid + lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0) red[wid] = v;
+  }
+  __syncthreads();
+  double tot = 0.0;
+  if (threadIdx.x == 0) {
+    double t[8];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t[w] = (w < nch) ? red[w] : 0.0;
+    tot = ((t[0] + t[4]) + (t[2] + t[6])) + ((t[1] + t[5]) + (t[3] + t[7]));
+  }
+  return tot;
+}
+
 // Sum of `count` partials in a fixed order by one block (all threads get it).
 PSF_DEVINL double block_sum_array(const volatile double* p, int count, double* red) {
   double v = 0.0;
@@ -196,13 +235,20 @@ PSF_DEVINL void fence_proxy_async() { asm volatile("fence.proxy.async.shared::ct
 
 // v * 2^k, exact.  For a normal v whose scaled value stays normal the scaling
 // is an integer add on the exponent field (INT pipe, no FP64 instruction);
-// zeros, subnormals, Inf/NaN and out-of-range results take an exact multiply.
+// zeros are returned as they are; subnormals, Inf/NaN and out-of-range results
+// take an exact multiply in a separate, non-inlined function, so that the
+// compiler cannot evaluate it speculatively on the fast path (ldexp costs
+// several FP64 instructions, and the FP64 pipe is a bottleneck of the kernels
+// that scale every element).
+static __device__ __noinline__ double scale_pow2_slow(double v, int k) { return v * ldexp(1.0, k); }
+
 PSF_DEVINL double scale_pow2(double v, int k) {
   const long long b = __double_as_longlong(v);
   const int ex = (int)((b >> 52) & 0x7ff);
   const int ek = ex + k;
   if (ex > 0 && ex < 0x7ff && ek > 0 && ek < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
-  return v * ldexp(1.0, k);
+  if ((b & 0x7fffffffffffffffLL) == 0) return v;  // +-0
+  return scale_pow2_slow(v, k);
 }
 
 // floor(log2(|x|)) of a normal, finite, nonzero x (integer extraction).

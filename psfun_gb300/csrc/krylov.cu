@@ -194,17 +194,40 @@ __global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) 
 // ---------------------------------------------------------------------------
 // Warp-specialised tile pipeline of the persistent Lanczos kernel.  The last
 // warp produces: its lane 0 stages every regular tile of the CTA's range by
-// TMA into one of two buffers, after the consumer warps have released it
+// TMA into one of kLzStages buffers, after the consumer warps have released it
 // ("empty" mbarrier, one arrival per consumer warp).  The other warps consume:
 // they wait on the buffer's "full" transaction barrier, form their rows and
 // release the buffer -- no block-wide barrier per tile.  Staged tiles are
-// counted from the start of the kernel; the n-th staged tile uses buffer n&1
-// and phase parity (n>>1)&1 on both barriers.  Because the matrix does not
-// change between steps, the producer stages the first two tiles of the next
-// step as soon as their buffers are free, overlapping that transfer with the
-// update phase and the grid barriers.  Rows longer than a tile are formed from
-// global memory by consumer warp 0 alone.
+// counted from the start of the kernel; the n-th staged tile uses buffer
+// n % kLzStages and phase parity (n / kLzStages) & 1 on both barriers.  With
+// four 50 KB stages about 150 KB of matrix is in flight per SM, enough to
+// cover the HBM latency at this SM's share of the bandwidth.  Because the
+// matrix does not change between steps, the producer stages the first tiles
+// of the next step as soon as their buffers are free, overlapping that
+// transfer with the update phase and the grid barriers.  Rows longer than a
+// tile are formed from global memory by consumer warp 0 alone.
 constexpr int kConsumerWarps = kSpmvThreads / 32 - 1;
+constexpr int kLzStages = 4;
+
+struct __align__(128) LzSmem {
+  SpmvTile buf[kLzStages];
+  uint64_t bar[kLzStages];    // "full": TMA transaction barriers
+  uint64_t empty[kLzStages];  // "empty": one arrival per consumer warp
+  double red[kSpmvThreads / 32];
+  double scal[4];             // per-step scalars computed by thread 0: alpha, c2, beta, s_{i+1}
+};
+constexpr size_t kLzSmemBytes = sizeof(LzSmem);
+static_assert(kLzSmemBytes <= 227 * 1024, "persistent Lanczos stages exceed the shared memory of a CTA");
+
+PSF_DEVINL void lz_smem_init(LzSmem& sm) {
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kLzStages; ++b) {
+      mbar_init(&sm.bar[b], 1);
+      mbar_init(&sm.empty[b], kConsumerWarps);
+    }
+  }
+  __syncthreads();
+}
 
 struct PipeCounters {
   unsigned issued;    // producer: tiles staged so far
@@ -216,33 +239,36 @@ PSF_DEVINL bool is_regular(const CsrDev& A, int t) {
   return d1.y - d0.y <= kTileNnz;
 }
 
+// First tile index past the first `count` regular tiles of [tb, te).
+PSF_DEVINL int skip_regular(const CsrDev& A, int tb, int te, int count) {
+  int t = tb;
+  for (int c = 0; t < te && c < count; ++t)
+    if (is_regular(A, t)) ++c;
+  return t;
+}
+
 // Producer: stage regular tiles of [tb, te); returns false on timeout.
-PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, SpmvSmem& sm, unsigned& issued) {
+PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, LzSmem& sm, unsigned& issued) {
   for (int t = tb; t < te; ++t) {
     if (!is_regular(A, t)) continue;
-    const int b = issued & 1u;
-    if (issued >= 2u && !mbar_wait(&sm.empty[b], ((issued >> 1) + 1u) & 1u)) return false;
-    spmv_issue(A, tile_info(A, t), sm, b);
+    const unsigned b = issued % kLzStages;
+    const unsigned use = issued / kLzStages;
+    if (use >= 1u && !mbar_wait(&sm.empty[b], (use + 1u) & 1u)) return false;
+    spmv_issue_to(A, tile_info(A, t), sm.buf[b], &sm.bar[b]);
     ++issued;
   }
   return true;
 }
 
-PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int t0, int t1, SpmvSmem& sm,
+PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int t0, int t1, LzSmem& sm,
                              double* __restrict__ u, double& acc, int* err, PipeCounters& pc, bool prefetch_next) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   bool ok = true;
   if (warp == kConsumerWarps) {
     if (lane == 0) {
-      // tiles t0, t0+1 were staged ahead (previous step or prologue)
-      int skip = 0, t = t0;
-      while (t < t1 && skip < 2) { if (is_regular(A, t)) ++skip; ++t; }
-      ok = pipe_produce(A, t, t1, sm, pc.issued);
-      if (ok && prefetch_next) {
-        int cnt = 0, tn = t0;
-        while (tn < t1 && cnt < 2) { if (is_regular(A, tn)) ++cnt; ++tn; }
-        ok = pipe_produce(A, t0, tn, sm, pc.issued);
-      }
+      // the first kLzStages regular tiles were staged ahead (previous step or prologue)
+      ok = pipe_produce(A, skip_regular(A, t0, t1, kLzStages), t1, sm, pc.issued);
+      if (ok && prefetch_next) ok = pipe_produce(A, t0, skip_regular(A, t0, t1, kLzStages), sm, pc.issued);
       if (!ok) atomicOr(err, DEVERR_TIMEOUT);
     }
     return ok;
@@ -262,8 +288,8 @@ PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int 
       }
       continue;
     }
-    const int b = pc.consumed & 1u;
-    if (!mbar_wait(&sm.bar[b], (pc.consumed >> 1) & 1u)) {
+    const unsigned b = pc.consumed % kLzStages;
+    if (!mbar_wait(&sm.bar[b], (pc.consumed / kLzStages) & 1u)) {
       atomicOr(err, DEVERR_TIMEOUT);
       return false;
     }
@@ -284,7 +310,8 @@ PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int 
 
 __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A, int i_begin, int i_end,
                                                              int tiles_per_cta) {
-  PSF_SPMV_SMEM();
+  extern __shared__ __align__(128) unsigned char lz_smem_raw[];
+  LzSmem& sm = *reinterpret_cast<LzSmem*>(lz_smem_raw);
   KCtrl* c = st.ctrl;
   if (c->done) return;
   if (c->breakdown) {  // found by the previous launch: exit at the top of iteration i_begin
@@ -294,18 +321,18 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     }
     return;
   }
-  spmv_smem_init(sm, kConsumerWarps);
+  lz_smem_init(sm);
   const int G = gridDim.x, bid = blockIdx.x;
   const int t0 = min(A.ntiles, bid * tiles_per_cta);
   const int t1 = min(A.ntiles, t0 + tiles_per_cta);
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
   PipeCounters pc{0u, 0u};
-  if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first two tiles
-    int cnt = 0, tn = t0;
-    while (tn < t1 && cnt < 2) { if (is_regular(A, tn)) ++cnt; ++tn; }
-    if (!pipe_produce(A, t0, tn, sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
+  if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first tiles
+    if (!pipe_produce(A, t0, skip_regular(A, t0, t1, kLzStages), sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
   }
-  double sc = st.s[i_begin];
+  double sc = st.s[i_begin];       // s_i (thread 0 keeps it current; others read it after each barrier)
+  double wn_prev = 0.0;            // thread 0: ||W_i|| and k of the previous step
+  int k2_prev = 0;
   double sprev = (i_begin >= 2) ? st.s[i_begin - 1] : 0.0;
   double beta_i = (i_begin >= 2) ? HAT(st, i_begin - 1, i_begin) : 0.0;
   double* __restrict__ u = st.u;
@@ -314,48 +341,98 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     // ---- phase 1
     double acc = 0.0;
     lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
-    acc = block_sum(acc, sm.red);
-    if (threadIdx.x == 0) st.partials[bid] = acc;
-    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
-    const double alpha = sc * sc * block_sum_array(st.partials, G, sm.red);
-    const double c2 = (i >= 2) ? beta_i * sprev / sc : 0.0;
-    if (bid == 0 && threadIdx.x == 0) {
-      HAT(st, i, i) = alpha;
-      if (i >= 2) c->itx = i - 1;
+    // The per-step scalars are formed by thread 0 and broadcast through shared
+    // memory: a division or square root costs about ten dependent FP64
+    // instructions, which every warp would otherwise repeat on the critical
+    // path after each grid barrier.  What does not depend on this step's sums
+    // (c2, and s_i = 1 / (2^k ||w_i||) from the previous step) is formed before
+    // the barrier.
+    if (threadIdx.x == 0) {
+      if (i > i_begin) {
+        sc = 1.0 / ldexp(wn_prev, k2_prev);
+        if (bid == 0) st.s[i] = sc;
+      }
+      sm.scal[0] = sc;
+      sm.scal[1] = (i >= 2) ? beta_i * sprev / sc : 0.0;
     }
+    block_sum_store(acc, sm.red, &st.partials[bid]);
+    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+    {
+      const double S = partials_sum_to0(st.partials, G, sm.red);
+      if (threadIdx.x == 0) {
+        const double a = sc * sc * S;
+        sm.scal[2] = a;
+        if (bid == 0) {
+          HAT(st, i, i) = a;
+          if (i >= 2) c->itx = i - 1;
+        }
+      }
+    }
+    __syncthreads();
+    sc = sm.scal[0];
+    const double alpha = sm.scal[2];
+    const double c2 = sm.scal[1];
     // ---- phase 2
     const int k2 = ilog2_normal(sc);
     const double* __restrict__ wm = (i >= 2) ? WAT(st, i - 1) : wi;
     double* __restrict__ wo = WAT(st, i + 1);
+    // four rows per thread in flight: the loads of a group are issued before
+    // its arithmetic
     double acc2 = 0.0;
-    for (int r = rb + threadIdx.x; r < re; r += blockDim.x) {
+    const int bd = blockDim.x;
+    int r = rb + threadIdx.x;
+    for (; r + 3 * bd < re; r += 4 * bd) {
+      double uu[4], a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        uu[q] = u[r + q * bd];
+        a[q] = wi[r + q * bd];
+        b[q] = wm[r + q * bd];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double w = fma(-c2, b[q], fma(-alpha, a[q], uu[q]));
+        acc2 = fma(w, w, acc2);
+        wo[r + q * bd] = scale_pow2(w, k2);
+      }
+    }
+    for (; r < re; r += bd) {
       const double w = fma(-c2, wm[r], fma(-alpha, wi[r], u[r]));
       acc2 = fma(w, w, acc2);
       wo[r] = scale_pow2(w, k2);
     }
-    acc2 = block_sum(acc2, sm.red);
-    if (threadIdx.x == 0) st.partials[G + bid] = acc2;
+    block_sum_store(acc2, sm.red, &st.partials[G + bid]);
     if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
-    const double wn = sqrt(block_sum_array(st.partials + G, G, sm.red));
-    const double beta = sc * wn;
-    const double snext = 1.0 / ldexp(wn, k2);
-    if (bid == 0 && threadIdx.x == 0) {
-      HAT(st, i, i + 1) = beta;
-      HAT(st, i + 1, i) = beta;
-      st.s[i + 1] = snext;
-      if (st.host_flag) st.host_flag[1] = i;
+    {
+      const double S = partials_sum_to0(st.partials + G, G, sm.red);
+      if (threadIdx.x == 0) {
+        const double wn = sqrt(S);
+        const double bt = sc * wn;
+        sm.scal[3] = bt;
+        wn_prev = wn;
+        k2_prev = k2;
+        if (bid == 0) {
+          HAT(st, i, i + 1) = bt;
+          HAT(st, i + 1, i) = bt;
+          if (st.host_flag) st.host_flag[1] = i;
+        }
+      }
     }
+    __syncthreads();
+    const double beta = sm.scal[3];
     if (i + 1 <= st.nl && fabs(beta) < 1e-16) {  // checked at the top of iteration i+1
       if (bid == 0 && threadIdx.x == 0) {
+        st.s[i + 1] = 1.0 / ldexp(wn_prev, k2_prev);
         c->breakdown = 1;
         c->itx = i;
       }
       return;
     }
     sprev = sc;
-    sc = snext;
     beta_i = beta;
   }
+  // s of the last vector, formed ahead of the next step in the loop above
+  if (bid == 0 && threadIdx.x == 0) st.s[i_end] = 1.0 / ldexp(wn_prev, k2_prev);
 }
 
 // Arnoldi: w = scaling * A v_{i-1} into slot i   (psfun_d_arnoldi.f90:202)
@@ -644,7 +721,7 @@ static void spmv_kernel_attrs() {
   if (done) return;
   spmv_smem_attr(k_lz_spmv);
   spmv_smem_attr(k_ar_spmv);
-  spmv_smem_attr(k_lz_persist);
+  cudaFuncSetAttribute(k_lz_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
   done = true;
 }
 
@@ -653,7 +730,7 @@ static int persist_grid() {
   static int g = 0;
   if (g == 0) {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lz_persist, kSpmvThreads, kSpmvSmemBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lz_persist, kSpmvThreads, kLzSmemBytes);
     if (per < 1) per = 1;
     g = sm_count() * per;
   }
@@ -667,7 +744,7 @@ static int launch_lz_persist(KState& st, const CsrDev& A, int i_begin, int i_end
   G = (A.ntiles + tpc - 1) / tpc;
   if (G < 1) G = 1;
   void* args[] = {(void*)&st, (void*)&A, (void*)&i_begin, (void*)&i_end, (void*)&tpc};
-  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_lz_persist, dim3(G), dim3(kSpmvThreads), args, kSpmvSmemBytes, s));
+  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_lz_persist, dim3(G), dim3(kSpmvThreads), args, kLzSmemBytes, s));
   count_launch();
   return PSFUN_SUCCESS;
 }
@@ -850,6 +927,14 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     }
     PSF_CUDA(cudaGraphLaunch(meth->graph, s));
     count_launch(meth->graph_kernels);
+  } else if (istop == 2 && !arnoldi) {
+    // fixed-length Lanczos with per-launch timing on: the same single
+    // persistent launch as the graph, timed under the Lanczos slot
+    PSF_TRY(enqueue_prologue(false));
+    prof_begin(PROF_LZ_SPMV, s);
+    PSF_TRY(launch_lz_persist(st, A, 1, nl + 1, s));
+    prof_end(PROF_LZ_SPMV, s);
+    PSF_TRY(enqueue_epilogue(0));
   } else {
     PSF_TRY(enqueue_prologue(true));
     const int max_ahead = 24;

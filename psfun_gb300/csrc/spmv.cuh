@@ -99,40 +99,56 @@ PSF_DEVINL TileInfo tile_info(const CsrDev& A, int t) {
   return ti;
 }
 
-// Thread 0: stage tile t into buffer b (values, indices, row pointers).
-PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, int b) {
+// One thread: stage a tile into `buf` (values, indices, row pointers) behind
+// the transaction barrier `bar`.
+PSF_DEVINL void spmv_issue_to(const CsrDev& A, const TileInfo& ti, SpmvTile& buf, uint64_t* bar) {
   const unsigned bv = (unsigned)(((ti.k1 - ti.kv0) + 1) & ~1) * 8u;
   const unsigned bj = (unsigned)(((ti.k1 - ti.kj0) + 3) & ~3) * 4u;
   const unsigned bi = (unsigned)(((ti.r1 + 1 - ti.ki0) + 3) & ~3) * 4u;
   fence_proxy_async();
-  mbar_expect_tx(&sm.bar[b], (ti.k1 > ti.k0 ? bv + bj : 0u) + bi);
+  mbar_expect_tx(bar, (ti.k1 > ti.k0 ? bv + bj : 0u) + bi);
   if (ti.k1 > ti.k0) {
-    bulk_g2s(sm.buf[b].val, A.val + ti.kv0, bv, &sm.bar[b]);
-    bulk_g2s(sm.buf[b].ja, A.ja + ti.kj0, bj, &sm.bar[b]);
+    bulk_g2s(buf.val, A.val + ti.kv0, bv, bar);
+    bulk_g2s(buf.ja, A.ja + ti.kj0, bj, bar);
   }
-  bulk_g2s(sm.buf[b].irp, A.irp + ti.ki0, bi, &sm.bar[b]);
+  bulk_g2s(buf.irp, A.irp + ti.ki0, bi, bar);
+}
+
+// Thread 0: stage tile t into buffer b.
+PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, int b) {
+  spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
 }
 
 // Row sum of a staged tile: up to 8 gathers are issued before their FMAs.
+// The batch is cut at the longest row of the warp (a warp-uniform bound), so
+// that slots no lane of the warp needs are skipped by a uniform branch
+// instead of being evaluated and discarded: with 7 entries per row the eighth
+// FMA would otherwise cost one FP64 instruction per row.
 PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x) {
   const int dj = ti.kv0 - ti.kj0;  // ja index = val index + dj
   const int di = ti.r0 - ti.ki0;
   const int kb = tb.irp[lr + di] - ti.kv0;
   const int ke = tb.irp[lr + di + 1] - ti.kv0;
+  const int wmax = __reduce_max_sync(__activemask(), ke - kb);
   double s = 0.0;
-  for (int k = kb; k < ke; k += 8) {
-    const int cnt = ke - k;
+  for (int kk = 0; kk < wmax; kk += 8) {
+    const int k = kb + kk;
+    const int cnt = ke - k;   // this lane's entries left (may be <= 0)
+    const int wc = wmax - kk;  // the warp's
     double xv[8], vv[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      if (q < cnt) {
+      if (q < wc && q < cnt) {
         xv[q] = __ldg(x + tb.ja[k + q + dj]);
         vv[q] = tb.val[k + q];
       }
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (q < cnt) s = fma(vv[q], xv[q], s);
+    for (int q = 0; q < 8; ++q) {
+      if (q < wc) {
+        if (q < cnt) s = fma(vv[q], xv[q], s);
+      }
+    }
   }
   return s;
 }
