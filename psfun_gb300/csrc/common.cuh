@@ -182,6 +182,43 @@ PSF_DEVINL bool grid_barrier(unsigned int* count, volatile unsigned int* gen, in
   return ok != 0;
 }
 
+// Grid barrier on an arrival counter that only grows while a kernel sequence
+// runs (it is zeroed before the sequence): the k-th barrier of the sequence
+// completes when the counter reaches target = k * gridDim.x.  Compared with
+// grid_barrier, no generation word is read before arriving and the arrival is
+// a fire-and-forget reduction, which takes two L2 round trips off the release
+// path.  Memory ordering as in grid_barrier: the block barrier and the fence
+// before the arrival publish the block's writes; the acquire load and the
+// fence after the wait make the other blocks' writes visible.
+PSF_DEVINL unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+PSF_DEVINL bool grid_sync_to(unsigned int* count, unsigned int target, int* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    __threadfence();
+    atomicAdd(count, 1u);
+    const unsigned long long t0 = globaltimer_ns();
+    while (ld_acquire_gpu(count) < target) {
+      if (*(volatile int*)err != 0) { ok = 0; break; }
+      if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        atomicOr(err, DEVERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 // ---------------------------------------------------------------------------
 // TMA bulk copies (cp.async.bulk) with an mbarrier, bounded waits.
 // ---------------------------------------------------------------------------

@@ -340,13 +340,12 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     const double* __restrict__ wi = WAT(st, i);
     // ---- phase 1
     double acc = 0.0;
-    lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
     // The per-step scalars are formed by thread 0 and broadcast through shared
     // memory: a division or square root costs about ten dependent FP64
     // instructions, which every warp would otherwise repeat on the critical
     // path after each grid barrier.  What does not depend on this step's sums
-    // (c2, and s_i = 1 / (2^k ||w_i||) from the previous step) is formed before
-    // the barrier.
+    // (c2, and s_i = 1 / (2^k ||W_i||) of the previous step) is formed at the
+    // start of the SpMV phase, where the other warps' work hides it.
     if (threadIdx.x == 0) {
       if (i > i_begin) {
         sc = 1.0 / ldexp(wn_prev, k2_prev);
@@ -355,8 +354,9 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       sm.scal[0] = sc;
       sm.scal[1] = (i >= 2) ? beta_i * sprev / sc : 0.0;
     }
+    lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
     block_sum_store(acc, sm.red, &st.partials[bid]);
-    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i - 1) * (unsigned)G, &c->err)) return;
     {
       const double S = partials_sum_to0(st.partials, G, sm.red);
       if (threadIdx.x == 0) {
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       wo[r] = scale_pow2(w, k2);
     }
     block_sum_store(acc2, sm.red, &st.partials[G + bid]);
-    if (!grid_barrier(&c->bar_count, &c->bar_gen, &c->err)) return;
+    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i) * (unsigned)G, &c->err)) return;
     {
       const double S = partials_sum_to0(st.partials + G, G, sm.red);
       if (threadIdx.x == 0) {

@@ -119,11 +119,26 @@ PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, in
   spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
 }
 
+// Up to N entries of a row, starting at buffer entry k: all gathers first,
+// then the FMAs in entry order.  `cnt` is this lane's count of entries left.
+template <int N>
+PSF_DEVINL double spmv_batch(const SpmvTile& tb, int k, int cnt, int dj, const double* __restrict__ x, double s) {
+  double xv[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    if (q < cnt) xv[q] = __ldg(x + tb.ja[k + q + dj]);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    if (q < cnt) s = fma(tb.val[k + q], xv[q], s);
+  return s;
+}
+
 // Row sum of a staged tile: up to 8 gathers are issued before their FMAs.
-// The batch is cut at the longest row of the warp (a warp-uniform bound), so
-// that slots no lane of the warp needs are skipped by a uniform branch
-// instead of being evaluated and discarded: with 7 entries per row the eighth
-// FMA would otherwise cost one FP64 instruction per row.
+// Each batch is sized to the longest remaining row of the warp, chosen by a
+// warp-uniform switch: a predicated-off FP64 instruction still occupies the
+// FP64 pipe for the whole warp, so with 7 entries per row a fixed batch of 8
+// would cost one wasted FMA per row.  Entries are summed in order, so the
+// result does not depend on the batching.
 PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x) {
   const int dj = ti.kv0 - ti.kj0;  // ja index = val index + dj
   const int di = ti.r0 - ti.ki0;
@@ -133,21 +148,16 @@ PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const
   double s = 0.0;
   for (int kk = 0; kk < wmax; kk += 8) {
     const int k = kb + kk;
-    const int cnt = ke - k;   // this lane's entries left (may be <= 0)
-    const int wc = wmax - kk;  // the warp's
-    double xv[8], vv[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (q < wc && q < cnt) {
-        xv[q] = __ldg(x + tb.ja[k + q + dj]);
-        vv[q] = tb.val[k + q];
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (q < wc) {
-        if (q < cnt) s = fma(vv[q], xv[q], s);
-      }
+    const int cnt = ke - k;
+    switch (min(wmax - kk, 8)) {
+      case 1: s = spmv_batch<1>(tb, k, cnt, dj, x, s); break;
+      case 2: s = spmv_batch<2>(tb, k, cnt, dj, x, s); break;
+      case 3: s = spmv_batch<3>(tb, k, cnt, dj, x, s); break;
+      case 4: s = spmv_batch<4>(tb, k, cnt, dj, x, s); break;
+      case 5: s = spmv_batch<5>(tb, k, cnt, dj, x, s); break;
+      case 6: s = spmv_batch<6>(tb, k, cnt, dj, x, s); break;
+      case 7: s = spmv_batch<7>(tb, k, cnt, dj, x, s); break;
+      default: s = spmv_batch<8>(tb, k, cnt, dj, x, s); break;
     }
   }
   return s;
