@@ -214,9 +214,11 @@ struct __align__(128) LzSmem {
   uint64_t bar[kLzStages];    // "full": TMA transaction barriers
   uint64_t empty[kLzStages];  // "empty": one arrival per consumer warp
   double red[kSpmvThreads / 32];
+  double vals[kSpmvThreads];  // per-thread partials of a block reduction
   double scal[4];             // per-step scalars computed by thread 0: alpha, c2, beta, s_{i+1}
 };
 constexpr size_t kLzSmemBytes = sizeof(LzSmem);
+static_assert(kSpmvThreads == 512, "k_lz_persist reduces with block_sum_store_512");
 static_assert(kLzSmemBytes <= 227 * 1024, "persistent Lanczos stages exceed the shared memory of a CTA");
 
 PSF_DEVINL void lz_smem_init(LzSmem& sm) {
@@ -355,7 +357,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       sm.scal[1] = (i >= 2) ? beta_i * sprev / sc : 0.0;
     }
     lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
-    block_sum_store(acc, sm.red, &st.partials[bid]);
+    block_sum_store_512(acc, sm.vals, sm.red, &st.partials[bid]);
     if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i - 1) * (unsigned)G, &c->err)) return;
     {
       const double S = partials_sum_to0(st.partials, G, sm.red);
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       acc2 = fma(w, w, acc2);
       wo[r] = scale_pow2(w, k2);
     }
-    block_sum_store(acc2, sm.red, &st.partials[G + bid]);
+    block_sum_store_512(acc2, sm.vals, sm.red, &st.partials[G + bid]);
     if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i) * (unsigned)G, &c->err)) return;
     {
       const double S = partials_sum_to0(st.partials + G, G, sm.red);
