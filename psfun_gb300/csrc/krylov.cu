@@ -193,13 +193,14 @@ __global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) 
 // CTA 0 records H, s and itx for the estimate / final kernels.
 // ---------------------------------------------------------------------------
 // Warp-specialised tile pipeline of the persistent Lanczos kernel.  The last
-// warp produces: its lane 0 stages every regular tile of the CTA's range by
-// TMA into one of kLzStages buffers, after the consumer warps have released it
-// ("empty" mbarrier, one arrival per consumer warp).  The other warps consume:
-// they wait on the buffer's "full" transaction barrier, form their rows and
-// release the buffer -- no block-wide barrier per tile.  Staged tiles are
-// counted from the start of the kernel; the n-th staged tile uses buffer
-// n % kLzStages and phase parity (n / kLzStages) & 1 on both barriers.  With
+// warp produces: its lane 0 stages every tile of the CTA's range by TMA into
+// one of kLzStages slots, after the consumer warps have released it ("empty"
+// mbarrier, one arrival per consumer warp); the slot also carries the tile's
+// geometry.  The other warps consume: they wait on the slot's "full"
+// transaction barrier, form their rows and release the slot -- no block-wide
+// barrier per tile.  Tiles are counted from the start of the kernel; the n-th
+// tile uses slot n % kLzStages and phase parity (n / kLzStages) & 1 on both
+// barriers.  With
 // four 50 KB stages about 150 KB of matrix is in flight per SM, enough to
 // cover the HBM latency at this SM's share of the bandwidth.  Because the
 // matrix does not change between steps, the producer stages the first tiles
@@ -213,6 +214,7 @@ struct __align__(128) LzSmem {
   SpmvTile buf[kLzStages];
   uint64_t bar[kLzStages];    // "full": TMA transaction barriers
   uint64_t empty[kLzStages];  // "empty": one arrival per consumer warp
+  TileInfo info[kLzStages];   // geometry of the staged tile, written by the producer
   double red[kSpmvThreads / 32];
   double vals[kSpmvThreads];  // per-thread partials of a block reduction
   double scal[4];             // per-step scalars computed by thread 0: alpha, c2, beta, s_{i+1}
@@ -236,27 +238,21 @@ struct PipeCounters {
   unsigned consumed;  // consumers: tiles consumed so far
 };
 
-PSF_DEVINL bool is_regular(const CsrDev& A, int t) {
-  const int2 d0 = A.tile_desc[t], d1 = A.tile_desc[t + 1];
-  return d1.y - d0.y <= kTileNnz;
-}
-
-// First tile index past the first `count` regular tiles of [tb, te).
-PSF_DEVINL int skip_regular(const CsrDev& A, int tb, int te, int count) {
-  int t = tb;
-  for (int c = 0; t < te && c < count; ++t)
-    if (is_regular(A, t)) ++c;
-  return t;
-}
-
-// Producer: stage regular tiles of [tb, te); returns false on timeout.
+// Producer: stage tiles [tb, te) in order, one slot each.  The slot also
+// carries the tile's geometry, so that consumers read no tile descriptor from
+// global memory.  A tile that is one long row is not copied: its slot holds
+// only the geometry and its full barrier completes with a plain arrive.  The
+// arrive (plain or expect_tx) releases the write of the geometry.  Returns
+// false on timeout.
 PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, LzSmem& sm, unsigned& issued) {
   for (int t = tb; t < te; ++t) {
-    if (!is_regular(A, t)) continue;
     const unsigned b = issued % kLzStages;
     const unsigned use = issued / kLzStages;
     if (use >= 1u && !mbar_wait(&sm.empty[b], (use + 1u) & 1u)) return false;
-    spmv_issue_to(A, tile_info(A, t), sm.buf[b], &sm.bar[b]);
+    const TileInfo ti = tile_info(A, t);
+    sm.info[b] = ti;
+    if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
+    else mbar_arrive(&sm.bar[b]);
     ++issued;
   }
   return true;
@@ -265,21 +261,27 @@ PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, LzSmem& sm, unsign
 PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int t0, int t1, LzSmem& sm,
                              double* __restrict__ u, double& acc, int* err, PipeCounters& pc, bool prefetch_next) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tpre = t0 + min(kLzStages, t1 - t0);  // tiles staged ahead of each step
   bool ok = true;
   if (warp == kConsumerWarps) {
     if (lane == 0) {
-      // the first kLzStages regular tiles were staged ahead (previous step or prologue)
-      ok = pipe_produce(A, skip_regular(A, t0, t1, kLzStages), t1, sm, pc.issued);
-      if (ok && prefetch_next) ok = pipe_produce(A, t0, skip_regular(A, t0, t1, kLzStages), sm, pc.issued);
+      ok = pipe_produce(A, tpre, t1, sm, pc.issued);
+      if (ok && prefetch_next) ok = pipe_produce(A, t0, tpre, sm, pc.issued);
       if (!ok) atomicOr(err, DEVERR_TIMEOUT);
     }
     return ok;
   }
   const int ctid = threadIdx.x;  // 0 .. kConsumerWarps*32-1
   for (int t = t0; t < t1; ++t) {
-    const TileInfo ti = tile_info(A, t);
+    const unsigned b = pc.consumed % kLzStages;
+    if (!mbar_wait(&sm.bar[b], (pc.consumed / kLzStages) & 1u)) {
+      atomicOr(err, DEVERR_TIMEOUT);
+      return false;
+    }
+    ++pc.consumed;
+    const TileInfo ti = sm.info[b];
     if (ti.k1 - ti.k0 > kTileNnz) {
-      if (warp == 0) {
+      if (warp == 0) {  // one long row, from global memory
         double s = 0.0;
         for (int k = ti.k0 + lane; k < ti.k1; k += 32) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
         s = warp_sum(s);
@@ -288,21 +290,15 @@ PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int 
           acc = fma(s, x[ti.r0], acc);
         }
       }
-      continue;
-    }
-    const unsigned b = pc.consumed % kLzStages;
-    if (!mbar_wait(&sm.bar[b], (pc.consumed / kLzStages) & 1u)) {
-      atomicOr(err, DEVERR_TIMEOUT);
-      return false;
-    }
-    ++pc.consumed;
-    const SpmvTile& tb = sm.buf[b];
-    const int nr = ti.r1 - ti.r0;
-    for (int lr = ctid; lr < nr; lr += kConsumerWarps * 32) {
-      const int r = ti.r0 + lr;
-      const double s = spmv_row(tb, ti, lr, x);
-      u[r] = s;
-      acc = fma(s, __ldg(x + r), acc);
+    } else {
+      const SpmvTile& tb = sm.buf[b];
+      const int nr = ti.r1 - ti.r0;
+      for (int lr = ctid; lr < nr; lr += kConsumerWarps * 32) {
+        const int r = ti.r0 + lr;
+        const double s = spmv_row(tb, ti, lr, x);
+        u[r] = s;
+        acc = fma(s, __ldg(x + r), acc);
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&sm.empty[b]);
@@ -330,7 +326,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
   PipeCounters pc{0u, 0u};
   if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first tiles
-    if (!pipe_produce(A, t0, skip_regular(A, t0, t1, kLzStages), sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
+    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
   }
   double sc = st.s[i_begin];       // s_i (thread 0 keeps it current; others read it after each barrier)
   double wn_prev = 0.0;            // thread 0: ||W_i|| and k of the previous step
