@@ -65,7 +65,7 @@ def persist_bytes(n: int, nnz: int, steps: int) -> int:
     return steps * b["step"] - 8 * n
 
 
-def dgemm_fma_rate(torch, size: int = 4096, reps: int = 3) -> float:
+def dgemm_fma_rate(torch, size: int = 2048, reps: int = 5) -> float:
     """FP64 multiply-adds per second of cuBLAS DGEMM on this GPU (the FP64 peak
     the Lanczos step is held against)."""
     a = torch.randn(size, size, dtype=torch.float64, device="cuda")
@@ -500,7 +500,7 @@ def main():
                      "fp64": {"fma_per_launch": fma_launch, "achieved_gfma_s": fma_launch / (launch_ms * 1e-3) / 1e9,
                               "peak_gfma_s": fp64_peak / 1e9,
                               "frac": fma_launch / (launch_ms * 1e-3) / fp64_peak,
-                              "peak_source": "measured in this run: cuBLAS DGEMM (torch.matmul, 4096^3 float64)"}},
+                              "peak_source": "measured in this run: cuBLAS DGEMM (torch.matmul, 2048^3 float64)"}},
         "lanczos_step": {"step_ms": step_ms, "step_algorithmic_bytes": nbytes["step"],
                          "step_GBs": nbytes["step"] / (step_ms * 1e-3) / 1e9,
                          "solve_GBs": (bytes_launch + 8 * n * (M_KRYLOV + 1)) / (ms_per_step * 1e-3) / 1e9},
