@@ -507,6 +507,113 @@ __global__ void __launch_bounds__(kMgsThreads) k_ar_mgs(KState st, int i) {
   }
 }
 
+// The same modified Gram-Schmidt with the block's rows of w held in shared
+// memory for the whole step (used when they fit, n <= ~4.3M rows on 152 SMs):
+// per sweep only W_k and W_{k+1} stream from HBM, and w never leaves the SM
+// until it is written back at the end.  512 threads; the grid barriers count
+// on a counter that grows across the steps of a solve (bar_base = barriers
+// run by the earlier steps), per-block partials are reduced through shared
+// memory and the scalars of a sweep are formed by thread 0.
+constexpr int kMgsSmThreads = 512;
+constexpr size_t kMgsSmFixed = sizeof(double) * (kMgsSmThreads + 32 + 8);
+
+__global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base) {
+  extern __shared__ __align__(16) double mgs_sm[];
+  double* vals = mgs_sm;               // kMgsSmThreads
+  double* red = vals + kMgsSmThreads;  // 32
+  double* scal = red + 32;             // 8
+  double* wl = scal + 8;               // chunk
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  if (c->breakdown) {  // the previous step found h(i-1,i-2) == 0 (istop = 2)
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->done = 1;
+    return;
+  }
+  const int G = gridDim.x;
+  const int b = blockIdx.x;
+  const int bd = blockDim.x;
+  const int64_t r0 = (int64_t)b * chunk;
+  const int nloc = (int)max((int64_t)0, min(r0 + chunk, st.n) - r0);
+  double* __restrict__ w = WAT(st, i) + r0;
+  double* part = st.partials;
+  unsigned nb = bar_base;
+  {  // load the rows of w; dot with v_1
+    const double* __restrict__ wk = WAT(st, 1) + r0;
+    double acc = 0.0;
+    for (int l = threadIdx.x; l < nloc; l += bd) {
+      const double v = w[l];
+      wl[l] = v;
+      acc = fma(wk[l], v, acc);
+    }
+    block_sum_store_512(acc, vals, red, &part[b]);
+  }
+  if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
+  for (int k = 1; k <= i - 1; ++k) {
+    const double tot = partials_sum_to0(part + (size_t)((k - 1) & 1) * G, G, red);
+    if (threadIdx.x == 0) {
+      const double h = st.s[k] * tot;  // h(k,i-1) = v_k . w
+      if (b == 0) HAT(st, k, i - 1) = h;
+      scal[0] = h * st.s[k];
+    }
+    __syncthreads();
+    const double cc = scal[0];
+    const double* __restrict__ wk = WAT(st, k) + r0;
+    double acc = 0.0;
+    int l = threadIdx.x;
+    if (k + 1 <= i - 1) {  // update with v_k fused with the dot of v_{k+1}
+      const double* __restrict__ wn = WAT(st, k + 1) + r0;
+      for (; l + 3 * bd < nloc; l += 4 * bd) {
+        double a[4], nx[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          a[q] = wk[l + q * bd];
+          nx[q] = wn[l + q * bd];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double v = fma(-cc, a[q], wl[l + q * bd]);
+          wl[l + q * bd] = v;
+          acc = fma(nx[q], v, acc);
+        }
+      }
+      for (; l < nloc; l += bd) {
+        const double v = fma(-cc, wk[l], wl[l]);
+        wl[l] = v;
+        acc = fma(wn[l], v, acc);
+      }
+    } else {  // last update fused with the norm
+      for (; l + 3 * bd < nloc; l += 4 * bd) {
+        double a[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = wk[l + q * bd];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double v = fma(-cc, a[q], wl[l + q * bd]);
+          wl[l + q * bd] = v;
+          acc = fma(v, v, acc);
+        }
+      }
+      for (; l < nloc; l += bd) {
+        const double v = fma(-cc, wk[l], wl[l]);
+        wl[l] = v;
+        acc = fma(v, v, acc);
+      }
+    }
+    block_sum_store_512(acc, vals, red, &part[(size_t)(k & 1) * G + b]);
+    if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
+  }
+  for (int l = threadIdx.x; l < nloc; l += bd) w[l] = wl[l];
+  const double tot = partials_sum_to0(part + (size_t)((i - 1) & 1) * G, G, red);
+  if (b == 0 && threadIdx.x == 0) {
+    const double beta = sqrt(tot);
+    HAT(st, i, i - 1) = beta;
+    st.s[i] = 1.0 / beta;
+    c->itx = i - 1;
+    if (beta == 0.0) c->breakdown = 1;
+    if (st.host_flag) st.host_flag[1] = i;
+  }
+}
+
 // A posteriori estimate of iteration i (psfun_d_arnoldi.f90:222-276,
 // psfun_d_lanczos.f90:271-324): yk = f(H(1:i-1,1:i-1)) e1,
 // rs(i) = beta0 * h(i,i-1) * |yk(i-1)| / ||yk||; stop when rs(i) < eps.
@@ -755,6 +862,28 @@ static int grid_for(int64_t items, int threads, int per_sm) {
   return (int)g;
 }
 
+// Grid and rows per block of k_ar_mgs_sm for n rows, or 0 when the rows of a
+// block do not fit in shared memory.
+static int mgs_sm_plan(int64_t n, int* chunk) {
+  const int G = sm_count();
+  int64_t ch = (n + G - 1) / G;
+  ch = (ch + 1) & ~(int64_t)1;
+  const size_t bytes = kMgsSmFixed + sizeof(double) * (size_t)ch;
+  if (bytes + 1024 > 227 * 1024) return 0;  // room for the static shared memory
+  static size_t attr = 0;
+  if (attr < bytes) {
+    if (cudaFuncSetAttribute(k_ar_mgs_sm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      return 0;
+    attr = bytes;
+  }
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ar_mgs_sm, kMgsSmThreads, bytes) != cudaSuccess ||
+      per < 1)
+    return 0;
+  *chunk = (int)ch;
+  return G;
+}
+
 static int mgs_grid() {
   static int g = 0;
   if (g == 0) {
@@ -843,6 +972,8 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
   const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
   const int gm = mgs_grid();
+  int mgs_chunk = 0;
+  const int gms = arnoldi ? mgs_sm_plan(n, &mgs_chunk) : 0;
   const int tridiag = arnoldi ? 0 : 1;
   const size_t small_doubles = meth->small.bytes / sizeof(double);
 
@@ -865,9 +996,16 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       prof_begin(PROF_AR_SPMV, s);
       k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
       prof_end(PROF_AR_SPMV, s);
-      void* args[] = {(void*)&st, (void*)&i};
       prof_begin(PROF_AR_MGS, s);
-      PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
+      if (gms > 0) {
+        unsigned bar_base = (unsigned)((int64_t)(i - 1) * i / 2 - 1);  // barriers of steps 2..i-1
+        void* args[] = {(void*)&st, (void*)&i, (void*)&mgs_chunk, (void*)&bar_base};
+        const size_t smem = kMgsSmFixed + sizeof(double) * (size_t)mgs_chunk;
+        PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs_sm, dim3(gms), dim3(kMgsSmThreads), args, smem, s));
+      } else {
+        void* args[] = {(void*)&st, (void*)&i};
+        PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
+      }
       prof_end(PROF_AR_MGS, s);
       count_launch(2);
     } else {
@@ -1070,46 +1208,57 @@ struct MsParams {
   double* resid;  // N
 };
 
-__global__ void k_ms_monitor(KState st, MsParams mp, int i) {
+// Shifted residuals of Lanczos steps i0..i1-1 (in order; each step's LDL^T
+// update of every shift depends on the previous one).  Stops at the first
+// step at which every shift has converged, or at a breakdown: c->itx is that
+// step and the Lanczos steps computed after it are ignored.
+__global__ void k_ms_monitor(KState st, MsParams mp, int i0, int i1) {
   __shared__ double red[32];
   KCtrl* c = st.ctrl;
   if (c->done) return;
-  const double alpha = HAT(st, i, i);
-  const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
-  const double bnext = HAT(st, i + 1, i);
-  double worst = 0.0;
-  for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
-    const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
-    const zc a = zadd(xi, zmk(mp.sign * alpha, 0.0));
-    zc d, phi;
-    if (i == 1) {
-      d = a;
-      phi = zdiv(zmk(1.0, 0.0), d);
-    } else {
-      const zc dprev = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
-      const zc phiprev = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
-      const double b = mp.sign * bi;
-      d = zsub(a, zdiv(zmk(b * b, 0.0), dprev));
-      phi = zdiv(zmul(phiprev, zmk(-b, 0.0)), d);
+  const int ibd = c->breakdown ? c->itx : i1;  // a breakdown found at step itx ends the basis there
+  for (int i = i0; i < i1; ++i) {
+    const bool last_valid = i >= ibd;
+    const double alpha = HAT(st, i, i);
+    const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
+    const double bnext = HAT(st, i + 1, i);
+    double worst = 0.0;
+    for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
+      const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
+      const zc a = zadd(xi, zmk(mp.sign * alpha, 0.0));
+      zc d, phi;
+      if (i == 1) {
+        d = a;
+        phi = zdiv(zmk(1.0, 0.0), d);
+      } else {
+        const zc dprev = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
+        const zc phiprev = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
+        const double b = mp.sign * bi;
+        d = zsub(a, zdiv(zmk(b * b, 0.0), dprev));
+        phi = zdiv(zmul(phiprev, zmk(-b, 0.0)), d);
+      }
+      mp.d[2 * j] = cuCreal(d);
+      mp.d[2 * j + 1] = cuCimag(d);
+      mp.phi[2 * j] = cuCreal(phi);
+      mp.phi[2 * j + 1] = cuCimag(phi);
+      const double r = bnext * zabs(phi);
+      mp.resid[j] = r;
+      worst = fmax(worst, r);
     }
-    mp.d[2 * j] = cuCreal(d);
-    mp.d[2 * j + 1] = cuCimag(d);
-    mp.phi[2 * j] = cuCreal(phi);
-    mp.phi[2 * j + 1] = cuCimag(phi);
-    const double r = bnext * zabs(phi);
-    mp.resid[j] = r;
-    worst = fmax(worst, r);
-  }
-  worst = block_max(worst, red);
-  if (threadIdx.x == 0) {
-    c->itx = i;
-    c->errnum = worst;
-    c->errden = 1.0;
-    if (worst < mp.eps || c->breakdown) {
-      c->done = 1;
-      c->conv = 1;
-      if (st.host_flag) st.host_flag[0] = 1;
+    worst = block_max(worst, red);  // ends with a block barrier: d, phi visible
+    bool stop = false;
+    if (threadIdx.x == 0) {
+      c->itx = i;
+      c->errnum = worst;
+      c->errden = 1.0;
+      if (worst < mp.eps || last_valid) {
+        c->done = 1;
+        c->conv = 1;
+        if (st.host_flag) st.host_flag[0] = 1;
+      }
     }
+    stop = worst < mp.eps || last_valid;
+    if (stop) return;
   }
 }
 
@@ -1262,18 +1411,21 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   st.host_flag = dflag;
   const CsrDev A = a->dev();
   spmv_kernel_attrs();
-  const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
   const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
   k_init<<<gv, kVecThreads, 0, s>>>(st, b);
   count_launch();
-  for (int i = 1; i <= nl; ++i) {
+  // Lanczos steps in chunks of kMsChunk, each one persistent cooperative
+  // launch, followed by the shifted-residual monitor of the chunk; at most
+  // kMsChunk - 1 steps run past convergence.
+  constexpr int kMsChunk = 8;
+  for (int i = 1; i <= nl; i += kMsChunk) {
     if (hflag[0]) break;
-    k_lz_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i);
-    k_lz_update<<<gv, kVecThreads, 0, s>>>(st, i);
-    k_ms_monitor<<<1, 256, 0, s>>>(st, mp, i);
-    count_launch(3);
+    const int i1 = std::min(i + kMsChunk, nl + 1);
+    PSF_TRY(launch_lz_persist(st, A, i, i1, s));
+    k_ms_monitor<<<1, 256, 0, s>>>(st, mp, i, i1);
+    count_launch();
     PSF_CUDA(cudaGetLastError());
-    for (long spin = 0; i - hflag[1] > 24 && !hflag[0]; ++spin) {
+    for (long spin = 0; i - hflag[1] > 32 && !hflag[0]; ++spin) {
       if (cudaStreamQuery(s) == cudaSuccess) break;
       if (spin > 200000000L) break;
     }

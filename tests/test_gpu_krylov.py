@@ -215,3 +215,18 @@ def test_semigroup_property_3d(lib):
     assert r1.info == r2.info == r3.info == 0
     assert rel(r2.y, r3.y) < 1e-10
     assert np.linalg.norm(r1.y) < 1.0
+
+
+@pytest.mark.parametrize("side", [300, 2100])
+def test_arnoldi_both_mgs_paths(lib, orc, side):
+    """Arnoldi keeps a block's rows of w in shared memory while they fit
+    (n <= ~4.3M rows on 152 SMs) and in global memory beyond: 2-D Laplacians
+    with n = 90,000 and n = 4,410,000 exercise both MGS kernels against the
+    oracle (fixed Krylov dimension 12)."""
+    A = matrices.laplacian_2d(side)
+    x = matrices.unit(np.random.default_rng(side).standard_normal(A.shape[0]))
+    g = run_gpu("ARNOLDI", "EXP", "GENPADE", -0.01, A, x, 1e-12, itmax=12, istop=2)
+    orc.set_threads(0)
+    o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", -0.01, A, x, 1e-12, itmax=12, istop=2)
+    assert g.info == 0 and o["info"] == 0 and g.iter == o["iter"]
+    assert rel(g.y, o["y"]) <= TOL
