@@ -421,8 +421,8 @@ PSF_DEVINL void cram_accumulate(int m, const double* x, const zc* sols, double* 
   for (int j = threadIdx.x; j < m; j += blockDim.x) {
     double acc = x[j] * kCramAlpha0;
     for (int p = 0; p < 7; ++p) {
-      const zc a = zmk(kCramAlpha[p][0], kCramAlpha[p][1]);
-      acc = acc + cuCreal(zmul(a, sols[(size_t)p * m + j]));
+      const zc sp = sols[(size_t)p * m + j];
+      acc = acc + (kCramAlpha[p][0] * cuCreal(sp) - kCramAlpha[p][1] * cuCimag(sp));
     }
     y[j] = acc;
   }
@@ -557,45 +557,69 @@ PSF_DEVINL bool cta_cram_full(int m, double t, const double* H, int ldh, const d
 // to the nonzeros (a row swap fills one extra super-diagonal).
 PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, const double* x, double* y,
                                  double* scratch) {
-  zc* sols = (zc*)scratch;                      // 7*m
-  zc* band = (zc*)(scratch + 2 * 7 * (size_t)m);  // 7 * 4 * m : d, du, du2, dl
+  // One thread per pole: banded GEPP of (-t T - theta_p I) u = x with the
+  // first-max row rule (swap when the subdiagonal entry is larger), the
+  // elimination of dnchbv.f:78-108 specialised to a tridiagonal T.  The active
+  // rows live in registers, so the forward sweep's dependent chain has no
+  // memory round trip; the finished U rows go to scratch (written in the
+  // forward sweep, read back in the backward one).  Magnitudes are compared
+  // squared, and a division is one reciprocal of |p|^2 and products: on this
+  // part each dependent FP64 instruction costs tens of cycles.
+  zc* sols = (zc*)scratch;                        // 7*m
+  zc* urow = (zc*)(scratch + 2 * 7 * (size_t)m);  // 7 * 4 * m : u0, u1, u2, rhs per row
   int bad = 0;
   if (threadIdx.x < 7) {
     const int p = threadIdx.x;
     const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
-    zc* d = band + (size_t)p * 4 * m;
-    zc* du = d + m;
-    zc* du2 = du + m;
-    zc* dl = du2 + m;
+    zc* U = urow + (size_t)p * 4 * m;
     zc* b = sols + (size_t)p * m;
-    for (int i = 0; i < m; ++i) {
-      d[i] = zsub(zmk(-t * H[i + (size_t)i * ldh], 0.0), theta);
-      du[i] = (i + 1 < m) ? zmk(-t * H[i + (size_t)(i + 1) * ldh], 0.0) : zmk(0.0, 0.0);
-      dl[i] = (i + 1 < m) ? zmk(-t * H[i + 1 + (size_t)i * ldh], 0.0) : zmk(0.0, 0.0);
-      du2[i] = zmk(0.0, 0.0);
-      b[i] = zmk(x[i], 0.0);
-    }
-    for (int k = 0; k < m - 1 && !bad; ++k) {
-      if (zabs(d[k]) < zabs(dl[k])) {  // swap rows k, k+1 (first max rule)
+    auto diag = [&](int i) { return zmk(-t * H[i + (size_t)i * ldh] - cuCreal(theta), -cuCimag(theta)); };
+    auto sup = [&](int i) { return zmk(i + 1 < m ? -t * H[i + (size_t)(i + 1) * ldh] : 0.0, 0.0); };
+    auto sub = [&](int i) { return zmk(i + 1 < m ? -t * H[i + 1 + (size_t)i * ldh] : 0.0, 0.0); };
+    // pivot row (columns k, k+1, k+2) and its right-hand side
+    zc a0 = diag(0), a1 = sup(0), a2 = zmk(0.0, 0.0), bk = zmk(x[0], 0.0);
+    for (int k = 0; k < m - 1; ++k) {
+      // original row k+1: columns k, k+1, k+2
+      zc q0 = sub(k), q1 = diag(k + 1), q2 = sup(k + 1), qb = zmk(x[k + 1], 0.0);
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      const double nq = cuCreal(q0) * cuCreal(q0) + cuCimag(q0) * cuCimag(q0);
+      if (na < nq) {
         zc tt;
-        tt = d[k]; d[k] = dl[k]; dl[k] = tt;
-        tt = du[k]; du[k] = d[k + 1]; d[k + 1] = tt;
-        if (k + 1 < m - 1) { tt = du2[k]; du2[k] = du[k + 1]; du[k + 1] = tt; }
-        tt = b[k]; b[k] = b[k + 1]; b[k + 1] = tt;
+        tt = a0; a0 = q0; q0 = tt;
+        tt = a1; a1 = q1; q1 = tt;
+        tt = a2; a2 = q2; q2 = tt;
+        tt = bk; bk = qb; qb = tt;
       }
-      if (zabs(d[k]) == 0.0) { bad = 1; break; }
-      const zc l = zdiv(dl[k], d[k]);
-      d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
-      if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
-      b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+      const double np = (na < nq) ? nq : na;
+      if (np == 0.0) { bad = 1; break; }
+      const double inv = 1.0 / np;
+      // l = q0 / a0 = q0 conj(a0) / |a0|^2
+      const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
+                       (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
+      U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      a0 = zsub(q1, zmul(l, a1));
+      a1 = zsub(q2, zmul(l, a2));
+      a2 = zmk(0.0, 0.0);
+      bk = zsub(qb, zmul(l, bk));
     }
-    if (!bad && zabs(d[m - 1]) == 0.0) bad = 1;
     if (!bad) {
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      if (na == 0.0) bad = 1;
+      U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
+    }
+    if (!bad) {
+      zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);  // solution at i+1, i+2
       for (int i = m - 1; i >= 0; --i) {
-        zc s = b[i];
-        if (i + 1 < m) s = zsub(s, zmul(du[i], b[i + 1]));
-        if (i + 2 < m) s = zsub(s, zmul(du2[i], b[i + 2]));
-        b[i] = zdiv(s, d[i]);
+        const zc u0 = U[4 * i], u1 = U[4 * i + 1], u2 = U[4 * i + 2];
+        zc s = U[4 * i + 3];
+        s = zsub(s, zmul(u1, x1));
+        s = zsub(s, zmul(u2, x2));
+        const double inv = 1.0 / (cuCreal(u0) * cuCreal(u0) + cuCimag(u0) * cuCimag(u0));
+        const zc xi = zmk((cuCreal(s) * cuCreal(u0) + cuCimag(s) * cuCimag(u0)) * inv,
+                          (cuCimag(s) * cuCreal(u0) - cuCreal(s) * cuCimag(u0)) * inv);
+        b[i] = xi;
+        x2 = x1;
+        x1 = xi;
       }
     }
   }
