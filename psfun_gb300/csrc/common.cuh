@@ -289,6 +289,23 @@ PSF_DEVINL void bulk_g2s(void* dst_smem, const void* src_gmem, unsigned bytes, u
       : "memory");
 }
 
+// The same copy with an L2 eviction-priority policy (createpolicy): used for
+// data streamed once per pass (matrix tiles larger than L2), so that the
+// vectors the other phases re-read stay resident in L2.
+PSF_DEVINL uint64_t l2_policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+PSF_DEVINL void bulk_g2s_hint(void* dst_smem, const void* src_gmem, unsigned bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
+}
+
 PSF_DEVINL void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // v * 2^k, exact.  For a normal v whose scaled value stays normal the scaling

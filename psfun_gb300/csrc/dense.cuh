@@ -571,16 +571,20 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
   if (threadIdx.x < 7) {
     const int p = threadIdx.x;
     const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
-    zc* U = urow + (size_t)p * 4 * m;
-    zc* b = sols + (size_t)p * m;
+    zc* __restrict__ U = urow + (size_t)p * 4 * m;
+    zc* __restrict__ b = sols + (size_t)p * m;
     auto diag = [&](int i) { return zmk(-t * H[i + (size_t)i * ldh] - cuCreal(theta), -cuCimag(theta)); };
     auto sup = [&](int i) { return zmk(i + 1 < m ? -t * H[i + (size_t)(i + 1) * ldh] : 0.0, 0.0); };
     auto sub = [&](int i) { return zmk(i + 1 < m ? -t * H[i + 1 + (size_t)i * ldh] : 0.0, 0.0); };
     // pivot row (columns k, k+1, k+2) and its right-hand side
     zc a0 = diag(0), a1 = sup(0), a2 = zmk(0.0, 0.0), bk = zmk(x[0], 0.0);
+    // original row k+1 (columns k, k+1, k+2), loaded one iteration ahead so
+    // that the loads stay off the dependent chain
+    zc q0 = zmk(0.0, 0.0), q1 = q0, q2 = q0, qb = q0;
+    if (m > 1) { q0 = sub(0); q1 = diag(1); q2 = sup(1); qb = zmk(x[1], 0.0); }
     for (int k = 0; k < m - 1; ++k) {
-      // original row k+1: columns k, k+1, k+2
-      zc q0 = sub(k), q1 = diag(k + 1), q2 = sup(k + 1), qb = zmk(x[k + 1], 0.0);
+      zc n0 = zmk(0.0, 0.0), n1 = n0, n2 = n0, nb = n0;
+      if (k + 2 < m) { n0 = sub(k + 1); n1 = diag(k + 2); n2 = sup(k + 2); nb = zmk(x[k + 2], 0.0); }
       const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
       const double nq = cuCreal(q0) * cuCreal(q0) + cuCimag(q0) * cuCimag(q0);
       if (na < nq) {
@@ -601,6 +605,7 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
       a1 = zsub(q2, zmul(l, a2));
       a2 = zmk(0.0, 0.0);
       bk = zsub(qb, zmul(l, bk));
+      q0 = n0; q1 = n1; q2 = n2; qb = nb;
     }
     if (!bad) {
       const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
@@ -609,14 +614,16 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
     }
     if (!bad) {
       zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);  // solution at i+1, i+2
+      // U row i, loaded one iteration ahead
+      zc u0 = U[4 * (m - 1)], u1 = U[4 * (m - 1) + 1], u2 = U[4 * (m - 1) + 2], ub = U[4 * (m - 1) + 3];
       for (int i = m - 1; i >= 0; --i) {
-        const zc u0 = U[4 * i], u1 = U[4 * i + 1], u2 = U[4 * i + 2];
-        zc s = U[4 * i + 3];
-        s = zsub(s, zmul(u1, x1));
-        s = zsub(s, zmul(u2, x2));
-        const double inv = 1.0 / (cuCreal(u0) * cuCreal(u0) + cuCimag(u0) * cuCimag(u0));
-        const zc xi = zmk((cuCreal(s) * cuCreal(u0) + cuCimag(s) * cuCimag(u0)) * inv,
-                          (cuCimag(s) * cuCreal(u0) - cuCreal(s) * cuCimag(u0)) * inv);
+        zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
+        if (i > 0) { u0 = U[4 * (i - 1)]; u1 = U[4 * (i - 1) + 1]; u2 = U[4 * (i - 1) + 2]; ub = U[4 * (i - 1) + 3]; }
+        const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+        zc sv = zsub(vb, zmul(v1, x1));
+        sv = zsub(sv, zmul(v2, x2));
+        const zc xi = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
+                          (cuCimag(sv) * cuCreal(v0) - cuCreal(sv) * cuCimag(v0)) * inv);
         b[i] = xi;
         x2 = x1;
         x1 = xi;

@@ -244,29 +244,32 @@ struct PipeCounters {
 // only the geometry and its full barrier completes with a plain arrive.  The
 // arrive (plain or expect_tx) releases the write of the geometry.  Returns
 // false on timeout.
-PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, LzSmem& sm, unsigned& issued) {
+PSF_DEVINL bool pipe_produce(const CsrDev& A, int tb, int te, LzSmem& sm, unsigned& issued, bool stream) {
+  const uint64_t pol = l2_policy_evict_first();
   for (int t = tb; t < te; ++t) {
     const unsigned b = issued % kLzStages;
     const unsigned use = issued / kLzStages;
     if (use >= 1u && !mbar_wait(&sm.empty[b], (use + 1u) & 1u)) return false;
     const TileInfo ti = tile_info(A, t);
     sm.info[b] = ti;
-    if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
-    else mbar_arrive(&sm.bar[b]);
+    if (ti.k1 - ti.k0 > kTileNnz) mbar_arrive(&sm.bar[b]);
+    else if (stream) spmv_issue_hint(A, ti, sm.buf[b], &sm.bar[b], pol);
+    else spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
     ++issued;
   }
   return true;
 }
 
 PSF_DEVINL bool lz_phase1_ws(const CsrDev& A, const double* __restrict__ x, int t0, int t1, LzSmem& sm,
-                             double* __restrict__ u, double& acc, int* err, PipeCounters& pc, bool prefetch_next) {
+                             double* __restrict__ u, double& acc, int* err, PipeCounters& pc, bool prefetch_next,
+                             bool stream) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tpre = t0 + min(kLzStages, t1 - t0);  // tiles staged ahead of each step
   bool ok = true;
   if (warp == kConsumerWarps) {
     if (lane == 0) {
-      ok = pipe_produce(A, tpre, t1, sm, pc.issued);
-      if (ok && prefetch_next) ok = pipe_produce(A, t0, tpre, sm, pc.issued);
+      ok = pipe_produce(A, tpre, t1, sm, pc.issued, stream);
+      if (ok && prefetch_next) ok = pipe_produce(A, t0, tpre, sm, pc.issued, stream);
       if (!ok) atomicOr(err, DEVERR_TIMEOUT);
     }
     return ok;
@@ -324,9 +327,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
   const int t0 = min(A.ntiles, bid * tiles_per_cta);
   const int t1 = min(A.ntiles, t0 + tiles_per_cta);
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
+  // A matrix larger than half of L2 is streamed with evict-first priority, so
+  // that u and the basis vectors the update phase re-reads stay in L2.
+  const bool stream = (A.nnz * 12 + A.n * 4) > (int64_t)(64 << 20);
   PipeCounters pc{0u, 0u};
   if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first tiles
-    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued)) atomicOr(&c->err, DEVERR_TIMEOUT);
+    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued, stream))
+      atomicOr(&c->err, DEVERR_TIMEOUT);
   }
   double sc = st.s[i_begin];       // s_i (thread 0 keeps it current; others read it after each barrier)
   double wn_prev = 0.0;            // thread 0: ||W_i|| and k of the previous step
@@ -352,7 +359,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       sm.scal[0] = sc;
       sm.scal[1] = (i >= 2) ? beta_i * sprev / sc : 0.0;
     }
-    lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end);
+    lz_phase1_ws(A, wi, t0, t1, sm, u, acc, &c->err, pc, i + 1 < i_end, stream);
     block_sum_store_512(acc, sm.vals, sm.red, &st.partials[bid]);
     if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i - 1) * (unsigned)G, &c->err)) return;
     {

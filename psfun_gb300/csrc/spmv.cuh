@@ -114,6 +114,20 @@ PSF_DEVINL void spmv_issue_to(const CsrDev& A, const TileInfo& ti, SpmvTile& buf
   bulk_g2s(buf.irp, A.irp + ti.ki0, bi, bar);
 }
 
+// The same with an L2 policy on the three copies (see bulk_g2s_hint).
+PSF_DEVINL void spmv_issue_hint(const CsrDev& A, const TileInfo& ti, SpmvTile& buf, uint64_t* bar, uint64_t pol) {
+  const unsigned bv = (unsigned)(((ti.k1 - ti.kv0) + 1) & ~1) * 8u;
+  const unsigned bj = (unsigned)(((ti.k1 - ti.kj0) + 3) & ~3) * 4u;
+  const unsigned bi = (unsigned)(((ti.r1 + 1 - ti.ki0) + 3) & ~3) * 4u;
+  fence_proxy_async();
+  mbar_expect_tx(bar, (ti.k1 > ti.k0 ? bv + bj : 0u) + bi);
+  if (ti.k1 > ti.k0) {
+    bulk_g2s_hint(buf.val, A.val + ti.kv0, bv, bar, pol);
+    bulk_g2s_hint(buf.ja, A.ja + ti.kj0, bj, bar, pol);
+  }
+  bulk_g2s_hint(buf.irp, A.irp + ti.ki0, bi, bar, pol);
+}
+
 // Thread 0: stage tile t into buffer b.
 PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, int b) {
   spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
