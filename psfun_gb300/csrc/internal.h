@@ -86,6 +86,7 @@ struct psfun_csr {
     d.n = n; d.nnz = nnz; d.irp = irp; d.ja = ja; d.val = val; d.tile_row = tile_row; d.ntiles = ntiles;
     d.sched = sched;
     d.tile_desc = tile_desc;
+    d.stream = (nnz * 12 + n * 4) > ((int64_t)64 << 20) ? 1 : 0;
     return d;
   }
 };

@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
   // A matrix larger than half of L2 is streamed with evict-first priority, so
   // that u and the basis vectors the update phase re-reads stay in L2.
-  const bool stream = (A.nnz * 12 + A.n * 4) > (int64_t)(64 << 20);
+  const bool stream = A.stream != 0;
   PipeCounters pc{0u, 0u};
   if (threadIdx.x == kConsumerWarps * 32) {  // prologue: stage the first tiles
     if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued, stream))

@@ -34,6 +34,7 @@ struct CsrDev {
   int32_t ntiles;
   unsigned* sched;  // [0] next tile, [1] blocks done: zero between launches
   const int2* __restrict__ tile_desc;  // {first row, first stored entry} per tile (+1 sentinel)
+  int stream;  // matrix larger than half of L2: stage tiles with an L2 evict-first policy
 };
 
 // One staged tile: values, column indices and the row pointers of its rows.
@@ -128,10 +129,14 @@ PSF_DEVINL void spmv_issue_hint(const CsrDev& A, const TileInfo& ti, SpmvTile& b
   bulk_g2s_hint(buf.irp, A.irp + ti.ki0, bi, bar, pol);
 }
 
-// Thread 0: stage tile t into buffer b.
+// Thread 0: stage tile t into buffer b; a matrix streamed once per pass and
+// larger than half of L2 goes with evict-first priority, so that the vectors
+// the caller re-reads stay in L2.
 PSF_DEVINL void spmv_issue(const CsrDev& A, const TileInfo& ti, SpmvSmem& sm, int b) {
-  spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
+  if (A.stream) spmv_issue_hint(A, ti, sm.buf[b], &sm.bar[b], l2_policy_evict_first());
+  else spmv_issue_to(A, ti, sm.buf[b], &sm.bar[b]);
 }
+
 
 // Up to N entries of a row, starting at buffer entry k: all gathers first,
 // then the FMAs in entry order.  `cnt` is this lane's count of entries left.
