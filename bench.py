@@ -303,6 +303,32 @@ def bench_multishift(torch, pg, peak_gbs: float, reps: int = 3):
             "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs}
 
 
+def bench_cg(torch, pg, peak_gbs: float, reps: int = 3):
+    """Shifted CG (psfun_dcg_vect) on (eta A + zeta I) x = b with eta = 1,
+    zeta = 0.5, A the 3-D 7-point Laplacian 128^3, Jacobi preconditioner,
+    relative residual 1e-10 (istop 2).  Bytes per iteration: one SpMV
+    (B_spmv) plus the vector updates of PCG (x, r, p, q, z: 7 reads and 4
+    writes of n doubles, 88 n)."""
+    A, _ = make_problem(N1)
+    n, nnz = A.shape[0], A.nnz
+    b = torch.tensor(np.random.default_rng(7).standard_normal(n), device="cuda")
+    a = pg.CsrMatrix.from_scipy(A)
+    x0 = torch.zeros_like(b)
+
+    def solve():
+        x0.zero_()
+        return pg.psb_krylov("CG", a, "DIAG", b, 1.0, 0.5, x0, 1e-10, itmax=5000, istop=2)
+
+    dt, (xs, info, it, err) = _time_dev(torch, solve, reps)
+    assert info == 0, info
+    b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    nbytes = it * (b_spmv + 88 * n)
+    return {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152), (A + 0.5 I) x = b, CG with DIAG, eps 1e-10",
+            "ms_per_solve": 1e3 * dt, "iterations": int(it), "relative_residual": float(err),
+            "us_per_iteration": 1e6 * dt / max(it, 1), "algorithmic_bytes_per_solve": nbytes,
+            "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs}
+
+
 def bench_adjoint(torch, pg, reps: int = 3):
     """Gradient of L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2 on the 512 x 512
     grid-graph Laplacian (n = 262,144, 523,264 edge weights theta): the cost of
@@ -513,6 +539,7 @@ def main():
         torch.cuda.empty_cache()
         line["multishift"] = bench_multishift(torch, pg, peak)
         line["adjoint"] = bench_adjoint(torch, pg)
+        line["cg"] = bench_cg(torch, pg, peak)
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_secondary:
         line["batched"] = bench_batched(torch, pg)
