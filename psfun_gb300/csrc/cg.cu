@@ -9,12 +9,14 @@
 // and the iteration also ends once itx >= itmax.  Preconditioners: NONE and
 // DIAG (Jacobi from the diagonal of A, the shifted.inp:8 choice).
 //
-// Per iteration three launches: p = z + beta p; q = eta A p + zeta p with the
+// Per iteration three kernels: p = z + beta p; q = eta A p + zeta p with the
 // fused p.q (SpMV epilogue); x += alpha p, r -= alpha q, z = D r with the fused
 // r.z and the norms of the stopping rule.  Scalars (rho, sigma, alpha, beta,
-// the stop test) are finalised on the device by the last block.
+// the stop test) are finalised on the device by the last block.  Iterations
+// are replayed from a CUDA graph in chunks of eight.
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "internal.h"
 
@@ -297,20 +299,47 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   k_cg_bnorm_fin<<<1, kCgThreads, 0, s>>>(st, gv);
   count_launch(2);
   const CsrDev A = a->dev();
+  // kCgChunk iterations (three kernels each) captured once per launch key in
+  // a CUDA graph and replayed: the launch cost of the host loop is paid once
+  // per chunk.  Kernels of iterations past the end return at their top.
+  constexpr int kCgChunk = 8;
+  struct Key {
+    CgState st; CsrDev A; int gs, gv;
+  } key;
+  memset(&key, 0, sizeof key);
+  key.st = st; key.A = A; key.gs = gs; key.gv = gv;
+  static cudaGraphExec_t graph = nullptr;
+  static std::vector<unsigned char> graph_key;
+  const unsigned char* kb = reinterpret_cast<const unsigned char*>(&key);
+  std::vector<unsigned char> kv(kb, kb + sizeof key);
+  if (!graph || graph_key != kv) {
+    if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kCgChunk; ++k) {
+      k_cg_p<<<gv, kCgThreads, 0, s>>>(st);
+      k_cg_q<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
+      k_cg_xr<<<gv, kCgThreads, 0, s>>>(st);
+    }
+    cudaError_t ec = cudaStreamEndCapture(s, &g);
+    PSF_CUDA(ec);
+    cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    PSF_CUDA(ei);
+    graph_key = kv;
+  }
   int itx_host = 0;
   while (itx_host < itmax) {  // restart loop (:252-253)
     hflag[2] = 0;
     k_cg_restart<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
     count_launch();
     PSF_CUDA(cudaGetLastError());
-    // enqueue iterations ahead of the device; device flags end them
-    for (int k = itx_host; k <= itmax + 1; ++k) {
+    // enqueue chunks ahead of the device; device flags end them
+    for (int k = itx_host; k <= itmax + 1; k += kCgChunk) {
       if (hflag[0] || hflag[2]) break;
-      k_cg_p<<<gv, kCgThreads, 0, s>>>(st);
-      k_cg_q<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
-      k_cg_xr<<<gv, kCgThreads, 0, s>>>(st);
-      count_launch(3);
-      for (long spin = 0; k - hflag[1] > 32 && !hflag[0] && !hflag[2]; ++spin) {
+      PSF_CUDA(cudaGraphLaunch(graph, s));
+      count_launch(3 * kCgChunk);
+      for (long spin = 0; k - hflag[1] > 4 * kCgChunk && !hflag[0] && !hflag[2]; ++spin) {
         if (cudaStreamQuery(s) == cudaSuccess) break;
         if (spin > 200000000L) break;
       }
