@@ -9,22 +9,21 @@
 // and the iteration also ends once itx >= itmax.  Preconditioners: NONE and
 // DIAG (Jacobi from the diagonal of A, the shifted.inp:8 choice).
 //
-// Per iteration three kernels: p = z + beta p; q = eta A p + zeta p with the
-// fused p.q (SpMV epilogue); x += alpha p, r -= alpha q, z = D r with the fused
-// r.z and the norms of the stopping rule.  Scalars (rho, sigma, alpha, beta,
-// the stop test) are finalised on the device by the last block.  Iterations
-// are replayed from a CUDA graph in chunks of eight.
+// The restart and all iterations run in one persistent cooperative kernel
+// (k_cg_persist below); the host only relaunches it after a breakdown.
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "internal.h"
+#include "persist.cuh"
 
 namespace psf {
 
 struct CgCtrl {
   int done, brk, itx, it, err, pad0;
   unsigned cnt0, cnt1;
+  unsigned bar, pad1;  // grid-barrier arrivals of the persistent kernel (zeroed before each launch)
   double rho, rho_old, sigma, alpha, beta;
   double errnum, errden;
   double bnorm_inf, bnorm2, anorm_inf;
@@ -56,149 +55,6 @@ struct EpiResid {
     acc = fma(v, zz, acc);
   }
 };
-
-__global__ void __launch_bounds__(kSpmvThreads) k_cg_restart(CgState st, CsrDev A) {
-  PSF_SPMV_SMEM();
-  CgCtrl* c = st.c;
-  if (c->done) return;
-  spmv_smem_init(sm);
-  EpiResid epi{&st, 0.0};
-  spmv_tiles(A, st.x, epi, sm, &c->err);
-  spmv_sched_done(A);
-  const double acc = block_sum(epi.acc, sm.red);
-  last_block_reduce(acc, st.part, &c->cnt0, sm.red, [&](double tot) {
-    c->brk = 0;
-    c->it = 0;
-    c->rho_old = 0.0;
-    c->rho = tot;  // rho of the first iteration (r.z)
-  });
-}
-
-// it += 1, itx += 1 ; p = z (it == 1) or p = z + beta p  (:267-285)
-__global__ void __launch_bounds__(kCgThreads) k_cg_p(CgState st) {
-  CgCtrl* c = st.c;
-  if (c->done || c->brk) return;
-  const int first = (c->it == 0);
-  const double beta = c->beta;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < st.n; r += stride)
-    st.p[r] = first ? st.z[r] : fma(beta, st.p[r], st.z[r]);
-}
-
-// q = eta A p + zeta p ; sigma = p.q ; alpha = rho/sigma  (:302-310)
-__global__ void __launch_bounds__(kSpmvThreads) k_cg_q(CgState st, CsrDev A) {
-  PSF_SPMV_SMEM();
-  CgCtrl* c = st.c;
-  if (c->done || c->brk) return;
-  spmv_smem_init(sm);
-  EpiShiftDot epi{st.eta, st.zeta, st.p, st.q, 0.0};
-  spmv_tiles(A, st.p, epi, sm, &c->err);
-  spmv_sched_done(A);
-  const double acc = block_sum(epi.acc, sm.red);
-  last_block_reduce(acc, st.part, &c->cnt0, sm.red, [&](double tot) {
-    c->it += 1;
-    c->itx += 1;
-    c->sigma = tot;
-    if (tot == 0.0) {
-      c->brk = 1;  // sigma breakdown: exit iteration, restart
-      if (st.host_flag) st.host_flag[2] = 1;
-    } else {
-      c->alpha = c->rho / tot;
-    }
-  });
-}
-
-// x += alpha p ; r -= alpha q ; z = D r ; rho' = r.z ; stop test  (:320-333)
-__global__ void __launch_bounds__(kCgThreads) k_cg_xr(CgState st) {
-  __shared__ double red[32];
-  CgCtrl* c = st.c;
-  if (c->done || c->brk) return;
-  const double alpha = c->alpha;
-  double a_rz = 0.0, a_r = 0.0, a_x = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < st.n; r += stride) {
-    const double xv = fma(alpha, st.p[r], st.x[r]);
-    st.x[r] = xv;
-    const double rv = fma(-alpha, st.q[r], st.r[r]);
-    st.r[r] = rv;
-    const double zv = st.dinv ? st.dinv[r] * rv : rv;
-    st.z[r] = zv;
-    a_rz = fma(rv, zv, a_rz);
-    if (st.istop == 1) {
-      a_r = fmax(a_r, fabs(rv));
-      a_x = fmax(a_x, fabs(xv));
-    } else {
-      a_r = fma(rv, rv, a_r);
-    }
-  }
-  a_rz = block_sum(a_rz, red);
-  if (st.istop == 1) {
-    a_r = block_max(a_r, red);
-    a_x = block_max(a_x, red);
-  } else {
-    a_r = block_sum(a_r, red);
-  }
-  __shared__ bool am_last;
-  if (threadIdx.x == 0) {
-    st.part[3 * blockIdx.x + 0] = a_rz;
-    st.part[3 * blockIdx.x + 1] = a_r;
-    st.part[3 * blockIdx.x + 2] = a_x;
-    __threadfence();
-    am_last = (atomicAdd(&c->cnt1, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!am_last) return;
-  __threadfence();
-  double s_rz = 0.0, s_r = 0.0, s_x = 0.0;
-  const volatile double* pv = st.part;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-    s_rz += pv[3 * b];
-    if (st.istop == 1) {
-      s_r = fmax(s_r, pv[3 * b + 1]);
-      s_x = fmax(s_x, pv[3 * b + 2]);
-    } else {
-      s_r += pv[3 * b + 1];
-    }
-  }
-  s_rz = block_sum(s_rz, red);
-  if (st.istop == 1) {
-    s_r = block_max(s_r, red);
-    s_x = block_max(s_x, red);
-  } else {
-    s_r = block_sum(s_r, red);
-  }
-  if (threadIdx.x == 0) {
-    c->cnt1 = 0u;
-    double errnum, errden;
-    if (st.istop == 1) {
-      errnum = s_r;
-      errden = c->anorm_inf * s_x + c->bnorm_inf;
-    } else {
-      errnum = sqrt(s_r);
-      errden = c->bnorm2;
-    }
-    c->errnum = errnum;
-    c->errden = errden;
-    const bool ok = (errden == 0.0) ? (errnum <= st.eps) : (errnum <= st.eps * errden);
-    if (ok || c->itx >= st.itmax) {
-      c->done = 1;
-      if (st.host_flag) st.host_flag[0] = 1;
-    } else {
-      // next iteration's rho and beta (:278-285)
-      c->rho_old = c->rho;
-      c->rho = s_rz;
-      if (c->rho_old == 0.0) {
-        c->brk = 1;  // rho breakdown at the top of the next iteration: exit it, restart
-        c->itx += 1;
-        if (st.host_flag) st.host_flag[2] = 1;
-      } else {
-        c->beta = c->rho / c->rho_old;
-      }
-    }
-    if (st.host_flag) st.host_flag[1] = c->itx;
-    __threadfence();
-  }
-}
 
 // ||b||_inf, ||b||_2
 __global__ void __launch_bounds__(kCgThreads) k_cg_bnorm(CgState st) {
@@ -234,6 +90,230 @@ __global__ void k_cg_bnorm_fin(CgState st, int nblocks) {
 __global__ void k_diag_inv(int64_t n, const double* d, double* out) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
     out[r] = (d[r] != 0.0) ? 1.0 / d[r] : 1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent CG: the restart and every iteration of psfun_dcg_vect in one
+// cooperative launch, with the SpMV through the TMA tile pipeline of the
+// persistent Lanczos kernel (matrix tiles staged with an L2 evict-first
+// policy, so x, r, p, q, z stay in L2).  Each block owns the rows of its
+// tile range for the vector updates.  Per iteration three grid barriers:
+//   p = z (first) or z + beta p                        -> barrier (p complete)
+//   q = eta A p + zeta p, partial p.q                  -> barrier -> alpha
+//   x += alpha p, r -= alpha q, z = D r, partial r.z and the norms of the
+//   stopping rule                                      -> barrier -> stop, beta
+// Thread 0 of every block forms the same scalars from the per-block partials
+// in the same order; block 0 records them in the control block.  The kernel
+// returns when the stopping rule holds, itx reaches itmax, or a breakdown
+// (sigma = 0 or rho_old = 0) asks the host to restart.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev A, int tiles_per_cta) {
+  extern __shared__ __align__(128) unsigned char cg_smem_raw[];
+  LzSmem& sm = *reinterpret_cast<LzSmem*>(cg_smem_raw);
+  CgCtrl* c = st.c;
+  if (c->done) return;
+  lz_smem_init(sm);
+  const int G = gridDim.x, bid = blockIdx.x;
+  const int t0 = min(A.ntiles, bid * tiles_per_cta);
+  const int t1 = min(A.ntiles, t0 + tiles_per_cta);
+  const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
+  const bool stream = A.stream != 0;
+  PipeCounters pc{0u, 0u};
+  if (threadIdx.x == kConsumerWarps * 32) {
+    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued, stream)) atomicOr(&c->err, DEVERR_TIMEOUT);
+  }
+  double* part = st.part;  // [5][G]
+  unsigned nb = 0;
+  unsigned passes = 0;  // SpMV passes completed (each consumes t1 - t0 tiles)
+  auto drain = [&]() { pipe_drain(sm, pc, passes * (unsigned)(t1 - t0)); };
+  auto gsync = [&]() -> bool { return grid_sync_to(&c->bar, (++nb) * (unsigned)G, &c->err); };
+  const int bd = blockDim.x;
+  // ---- restart: r = b - eta A x - zeta x ; z = D r ; rho = r.z (:256-260)
+  {
+    EpiResid epi{&st, 0.0};
+    if (__syncthreads_or(!pipe_spmv(A, st.x, t0, t1, sm, epi, &c->err, pc, true, stream))) {
+      drain();
+      return;
+    }
+    ++passes;
+    block_sum_store_512(epi.acc, sm.vals, sm.red, &part[bid]);
+  }
+  if (!gsync()) { drain(); return; }
+  {
+    const double S = partials_sum_to0(part, G, sm.red);
+    if (threadIdx.x == 0) {
+      sm.scal[0] = S;
+      if (bid == 0) {
+        c->brk = 0;
+        c->it = 0;
+        c->rho_old = 0.0;
+        c->rho = S;
+      }
+    }
+    __syncthreads();
+  }
+  double rho = sm.scal[0], beta = 0.0;
+  int itx = c->itx;  // iterations before this launch
+  bool first = true;
+  for (;;) {
+    // ---- p = z (it == 1) or p = z + beta p (:267-285); four rows per thread
+    // in flight (loads of a group before its arithmetic)
+    {
+      int r = rb + threadIdx.x;
+      if (first) {
+        for (; r < re; r += bd) st.p[r] = st.z[r];
+      } else {
+        for (; r + 3 * bd < re; r += 4 * bd) {
+          double zz[4], pp[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            zz[q] = st.z[r + q * bd];
+            pp[q] = st.p[r + q * bd];
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) st.p[r + q * bd] = fma(beta, pp[q], zz[q]);
+        }
+        for (; r < re; r += bd) st.p[r] = fma(beta, st.p[r], st.z[r]);
+      }
+    }
+    first = false;
+    if (!gsync()) { drain(); return; }
+    // ---- q = eta A p + zeta p ; sigma = p.q ; alpha = rho / sigma (:302-310)
+    {
+      EpiShiftDot epi{st.eta, st.zeta, st.p, st.q, 0.0};
+      if (__syncthreads_or(!pipe_spmv(A, st.p, t0, t1, sm, epi, &c->err, pc, true, stream))) {
+        drain();
+        return;
+      }
+      ++passes;
+      block_sum_store_512(epi.acc, sm.vals, sm.red, &part[G + bid]);
+    }
+    if (!gsync()) { drain(); return; }
+    ++itx;
+    {
+      const double sigma = partials_sum_to0(part + G, G, sm.red);
+      if (threadIdx.x == 0) {
+        sm.scal[1] = (sigma == 0.0) ? 0.0 : rho / sigma;
+        sm.scal[2] = (sigma == 0.0) ? 1.0 : 0.0;
+        if (bid == 0) {
+          c->it += 1;
+          c->itx = itx;
+          c->sigma = sigma;
+          if (sigma == 0.0) {
+            c->brk = 1;  // sigma breakdown: exit the iteration, restart
+            if (st.host_flag) st.host_flag[2] = 1;
+          } else {
+            c->alpha = sm.scal[1];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (sm.scal[2] != 0.0) { drain(); return; }
+    const double alpha = sm.scal[1];
+    // ---- x += alpha p ; r -= alpha q ; z = D r ; rho' = r.z ; norms (:320-333)
+    double a_rz = 0.0, a_r = 0.0, a_x = 0.0;
+    auto upd = [&](int r, double pv, double xo, double qv, double ro, double dv) {
+      const double xv = fma(alpha, pv, xo);
+      st.x[r] = xv;
+      const double rv = fma(-alpha, qv, ro);
+      st.r[r] = rv;
+      const double zv = st.dinv ? dv * rv : rv;
+      st.z[r] = zv;
+      a_rz = fma(rv, zv, a_rz);
+      if (st.istop == 1) {
+        a_r = fmax(a_r, fabs(rv));
+        a_x = fmax(a_x, fabs(xv));
+      } else {
+        a_r = fma(rv, rv, a_r);
+      }
+    };
+    {
+      int r = rb + threadIdx.x;
+      for (; r + 2 * bd < re; r += 3 * bd) {  // three rows per thread in flight
+        double pv[3], xo[3], qv[3], ro[3], dv[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const int rr = r + q * bd;
+          pv[q] = st.p[rr];
+          xo[q] = st.x[rr];
+          qv[q] = st.q[rr];
+          ro[q] = st.r[rr];
+          dv[q] = st.dinv ? st.dinv[rr] : 1.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) upd(r + q * bd, pv[q], xo[q], qv[q], ro[q], dv[q]);
+      }
+      for (; r < re; r += bd) upd(r, st.p[r], st.x[r], st.q[r], st.r[r], st.dinv ? st.dinv[r] : 1.0);
+    }
+    block_sum_store_512(a_rz, sm.vals, sm.red, &part[2 * G + bid]);
+    if (st.istop == 1) {
+      block_max_store_512(a_r, sm.vals, sm.red, &part[3 * G + bid]);
+      block_max_store_512(a_x, sm.vals, sm.red, &part[4 * G + bid]);
+    } else {
+      block_sum_store_512(a_r, sm.vals, sm.red, &part[3 * G + bid]);
+    }
+    if (!gsync()) { drain(); return; }
+    {
+      const double s_rz = partials_sum_to0(part + 2 * G, G, sm.red);
+      double s_r, s_x = 0.0;
+      __syncthreads();  // red is reused below
+      if (st.istop == 1) {
+        s_r = partials_max_to0(part + 3 * G, G, sm.red);
+        __syncthreads();
+        s_x = partials_max_to0(part + 4 * G, G, sm.red);
+      } else {
+        s_r = partials_sum_to0(part + 3 * G, G, sm.red);
+      }
+      if (threadIdx.x == 0) {
+        double errnum, errden;
+        if (st.istop == 1) {
+          errnum = s_r;
+          errden = c->anorm_inf * s_x + c->bnorm_inf;
+        } else {
+          errnum = sqrt(s_r);
+          errden = c->bnorm2;
+        }
+        const bool ok = (errden == 0.0) ? (errnum <= st.eps) : (errnum <= st.eps * errden);
+        int state = 0;  // 0 continue, 1 done, 2 rho breakdown
+        double bnext = 0.0;
+        if (ok || itx >= st.itmax) {
+          state = 1;
+        } else if (rho == 0.0) {
+          state = 2;  // rho breakdown at the top of the next iteration: exit it, restart
+        } else {
+          bnext = s_rz / rho;
+        }
+        sm.scal[3] = (double)state;
+        sm.scal[4] = bnext;
+        sm.scal[0] = s_rz;
+        if (bid == 0) {
+          c->errnum = errnum;
+          c->errden = errden;
+          if (state == 1) {
+            c->done = 1;
+            if (st.host_flag) st.host_flag[0] = 1;
+          } else {
+            c->rho_old = rho;
+            c->rho = s_rz;
+            if (state == 2) {
+              c->brk = 1;
+              c->itx = itx + 1;
+              if (st.host_flag) st.host_flag[2] = 1;
+            } else {
+              c->beta = bnext;
+            }
+          }
+          if (st.host_flag) st.host_flag[1] = c->itx;
+        }
+      }
+      __syncthreads();
+    }
+    const int state = (int)sm.scal[3];
+    if (state != 0) { drain(); return; }
+    beta = sm.scal[4];
+    rho = sm.scal[0];
+  }
 }
 
 int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
@@ -292,58 +372,24 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   h0.errden = 1.0;
   PSF_CUDA(cudaMemcpyAsync(st.c, &h0, sizeof h0, cudaMemcpyHostToDevice, s));
   const int gv = std::max(1, std::min<int>((int)((n + kCgThreads - 1) / kCgThreads), sm_count() * 8));
-  static bool attr = false;
-  if (!attr) { spmv_smem_attr(k_cg_restart); spmv_smem_attr(k_cg_q); attr = true; }
-  const int gs = std::max(1, std::min<int>(a->ntiles, sm_count() * 4));
   k_cg_bnorm<<<gv, kCgThreads, 0, s>>>(st);
   k_cg_bnorm_fin<<<1, kCgThreads, 0, s>>>(st, gv);
   count_launch(2);
   const CsrDev A = a->dev();
-  // kCgChunk iterations (three kernels each) captured once per launch key in
-  // a CUDA graph and replayed: the launch cost of the host loop is paid once
-  // per chunk.  Kernels of iterations past the end return at their top.
-  constexpr int kCgChunk = 8;
-  struct Key {
-    CgState st; CsrDev A; int gs, gv;
-  } key;
-  memset(&key, 0, sizeof key);
-  key.st = st; key.A = A; key.gs = gs; key.gv = gv;
-  static cudaGraphExec_t graph = nullptr;
-  static std::vector<unsigned char> graph_key;
-  const unsigned char* kb = reinterpret_cast<const unsigned char*>(&key);
-  std::vector<unsigned char> kv(kb, kb + sizeof key);
-  if (!graph || graph_key != kv) {
-    if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
-    cudaGraph_t g = nullptr;
-    PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kCgChunk; ++k) {
-      k_cg_p<<<gv, kCgThreads, 0, s>>>(st);
-      k_cg_q<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
-      k_cg_xr<<<gv, kCgThreads, 0, s>>>(st);
-    }
-    cudaError_t ec = cudaStreamEndCapture(s, &g);
-    PSF_CUDA(ec);
-    cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
-    cudaGraphDestroy(g);
-    PSF_CUDA(ei);
-    graph_key = kv;
-  }
+  // persistent grid: one block per SM, each owning a contiguous tile range
+  static int gp = 0;
+  if (!gp) gp = persist_grid_for(k_cg_persist);
+  int tpc = (A.ntiles + gp - 1) / gp;
+  if (tpc < 1) tpc = 1;
+  int G = (A.ntiles + tpc - 1) / tpc;
+  if (G < 1) G = 1;
   int itx_host = 0;
-  while (itx_host < itmax) {  // restart loop (:252-253)
+  while (itx_host < itmax) {  // restart loop (:252-253): a launch per restart
     hflag[2] = 0;
-    k_cg_restart<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A);
+    PSF_CUDA(cudaMemsetAsync(&st.c->bar, 0, sizeof(unsigned), s));
+    void* args[] = {(void*)&st, (void*)&A, (void*)&tpc};
+    PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_persist, dim3(G), dim3(kSpmvThreads), args, kLzSmemBytes, s));
     count_launch();
-    PSF_CUDA(cudaGetLastError());
-    // enqueue chunks ahead of the device; device flags end them
-    for (int k = itx_host; k <= itmax + 1; k += kCgChunk) {
-      if (hflag[0] || hflag[2]) break;
-      PSF_CUDA(cudaGraphLaunch(graph, s));
-      count_launch(3 * kCgChunk);
-      for (long spin = 0; k - hflag[1] > 4 * kCgChunk && !hflag[0] && !hflag[2]; ++spin) {
-        if (cudaStreamQuery(s) == cudaSuccess) break;
-        if (spin > 200000000L) break;
-      }
-    }
     PSF_CUDA(cudaGetLastError());
     CgCtrl hc;
     PSF_CUDA(cudaMemcpyAsync(&hc, st.c, sizeof hc, cudaMemcpyDeviceToHost, s));

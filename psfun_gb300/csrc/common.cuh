@@ -113,6 +113,39 @@ PSF_DEVINL void block_sum_store_512(double v, double* vals, double* red, double*
   if (threadIdx.x == 0) *out = (red[0] + red[1]) + (red[2] + red[3]);
 }
 
+// Thread 0 stores the maximum of the block's values to *out (blockDim.x == 512),
+// the counterpart of block_sum_store_512.
+PSF_DEVINL void block_max_store_512(double v, double* vals, double* red, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  vals[threadIdx.x] = v;
+  __syncthreads();
+  if (wid < 4) {
+    const double* p = vals + 128 * wid + lane;
+    double t = fmax(fmax(p[0], p[32]), fmax(p[64], p[96]));
+    t = warp_max(t);
+    if (lane == 0) red[wid] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *out = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
+}
+
+// Maximum of p[0..count) (count <= 256) for thread 0, the counterpart of
+// partials_sum_to0 (warps 0..7 reduce one chunk each).
+PSF_DEVINL double partials_max_to0(const volatile double* p, int count, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nch = (count + 31) >> 5;
+  if (wid < nch) {
+    double v = (32 * wid + lane < count) ? p[32 * wid + lane] : 0.0;
+    v = warp_max(v);
+    if (lane == 0) red[wid] = v;
+  }
+  __syncthreads();
+  double m = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < nch; ++w) m = fmax(m, red[w]);
+  return m;
+}
+
 // Sum of p[0..count) (count <= 256), bit-identical to block_sum_array(p,
 // count) run by a block of at least `count` threads, formed with less latency:
 // warps 0..7 reduce one chunk of 32 partials each in parallel, and thread 0
