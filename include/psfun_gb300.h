@@ -138,6 +138,15 @@ int psfun_gpu_krylov_destroy(psfun_krylov* meth);
  * last one as the reference does (psfun_d_arnoldi.f90:325-328). */
 int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char* val);
 int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val);
+/* The shift-and-invert method's parameters, which the reference keeps in the
+ * public components meth%tau and meth%prec (:45, :43-44) and builds the
+ * preconditioner with precinit/precbuild (:326-403): set_real("TAU", tau);
+ * set_string("PREC", "NONE" | "DIAG") (the Jacobi preconditioner of
+ * shifted.inp:8; AMG4PSBLAS's other types are not available) and
+ * set_string("KMETHD", ...) (only "CG" solves).  KNAME 'SAIARNOLDI' runs
+ * psfun_d_saiarnoldi (krylov/rational/psfun_d_sai.f90:37-419) with the inner
+ * CG on (A + tau I) w = v, inner itmax = ITMAX and istop = ISTOPC. */
+int psfun_gpu_krylov_set_real(psfun_krylov* meth, const char* what, double val);
 /* kmethd%apply(fun,a,desc_a,y,x,eps,info,itmax,itrace,istop,iter,err,res):
  * psfun_d_parallel_apply (:225-269).  itmax/itrace/istop are the optional
  * arguments with the reference defaults 200/0/1 supplied by the caller.

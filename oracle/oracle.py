@@ -72,6 +72,9 @@ def lib():
         for f in (L.orc_arnoldi, L.orc_lanczos):
             f.argtypes = [C.POINTER(OrcSerial), C.POINTER(OrcCsr), _dp, _dp, C.c_double, C.c_int, C.c_int,
                           C.c_int, C.POINTER(C.c_int), _dp, _dp, C.c_int, C.POINTER(C.c_int)]
+        L.orc_saiarnoldi.argtypes = [C.POINTER(OrcSerial), C.POINTER(OrcCsr), _dp, C.c_double, C.c_int, C.c_int, _dp,
+                                     _dp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double), _dp, C.c_int, C.POINTER(C.c_int)]
         L.orc_dcg.argtypes = [C.POINTER(OrcCsr), _dp, _dp, C.c_double, C.c_double, _dp, C.c_double, C.c_int,
                               C.c_int, C.POINTER(C.c_int), _dp]
         L.orc_horner.argtypes = [_dp, C.c_int, C.c_double]
@@ -160,17 +163,37 @@ def krylov(method, fun, A: Csr, x, eps, itmax=200, istop=1, drop_last=True):
     return dict(y=y, info=info, iter=it.value, err=err.value, res=res[: nres.value].copy())
 
 
+def diag_inv(A: Csr):
+    """Inverse diagonal of A for the DIAG preconditioner (a zero entry -> 1)."""
+    n = len(A.irp) - 1
+    d = np.zeros(n)
+    for i in range(n):
+        lo, hi = A.irp[i], A.irp[i + 1]
+        sel = A.ja[lo:hi] == i
+        d[i] = A.val[lo:hi][sel].sum()
+    return np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 1.0)
+
+
+def saiarnoldi(fun, A: Csr, x, eps, tau=0.0, prec="NONE", initmax=200, inistop=1, itmax=200, istop=1,
+               drop_last=True):
+    """psfun_d_saiarnoldi with kmethd 'CG' (krylov/rational/psfun_d_sai.f90)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    it = C.c_int(0)
+    err = C.c_double(0.0)
+    res = np.zeros(itmax + 2)
+    nres = C.c_int(0)
+    dinv = diag_inv(A) if prec.upper() == "DIAG" else None
+    info = lib().orc_saiarnoldi(C.byref(fun), C.byref(A.s), _p(dinv) if dinv is not None else None, float(tau),
+                                int(initmax), int(inistop), _p(y), _p(x), eps, itmax, istop, 1 if drop_last else 0,
+                                C.byref(it), C.byref(err), _p(res), len(res), C.byref(nres))
+    return dict(y=y, info=info, iter=it.value, err=err.value, res=res[: nres.value].copy())
+
+
 def dcg(A: Csr, b, eta, zeta, x0=None, eps=1e-7, itmax=1000, istop=2, prec="NONE"):
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
-    dinv = None
-    if prec.upper() == "DIAG":
-        d = np.zeros(len(b))
-        for i in range(len(b)):
-            lo, hi = A.irp[i], A.irp[i + 1]
-            sel = A.ja[lo:hi] == i
-            d[i] = A.val[lo:hi][sel].sum()
-        dinv = np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 1.0)
+    dinv = diag_inv(A) if prec.upper() == "DIAG" else None
     it = C.c_int(0)
     err = C.c_double(0.0)
     info = lib().orc_dcg(C.byref(A.s), _p(dinv) if dinv is not None else None, _p(b), eta, zeta, _p(x), eps,

@@ -199,10 +199,15 @@ class PsfunDKrylov:
         self.handle = h
 
     def set(self, what: str, val) -> int:
+        """set(what, val): KNAME, KMETHD, PREC ('NONE' / 'DIAG') as strings;
+        ITMAX, ITRACE, ISTOPC, IRST, KEEPLAST as integers; TAU (the public
+        component meth%tau of the reference) as a real."""
         if isinstance(val, str):
             return _lib().psfun_gpu_krylov_set_string(self.handle, what.encode(), val.encode())
         if isinstance(val, (bool, int, np.integer)):
             return _lib().psfun_gpu_krylov_set_integer(self.handle, what.encode(), int(val))
+        if isinstance(val, (float, np.floating)):
+            return _lib().psfun_gpu_krylov_set_real(self.handle, what.encode(), float(val))
         return ERR_INVALID_ARGS_COMBINATION
 
     def apply(self, fun: PsfunDSerial, a: CsrMatrix, x, eps: float, itmax: int | None = None,

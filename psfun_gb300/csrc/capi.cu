@@ -529,6 +529,20 @@ int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char
   if (!meth || !val) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   const std::string k = upper_key(what);
   if (k == "KNAME") { set_fstr(meth->kname, val); return PSFUN_SUCCESS; }
+  if (k == "KMETHD") { set_fstr(meth->kmethd, val); return PSFUN_SUCCESS; }
+  if (k == "PREC") {
+    const std::string v = upper_key(val);
+    if (v == "NONE" || v == "NOPREC") meth->prec = 0;
+    else if (v == "DIAG") meth->prec = 1;
+    else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    return PSFUN_SUCCESS;
+  }
+  return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+}
+int psfun_gpu_krylov_set_real(psfun_krylov* meth, const char* what, double val) {
+  if (!meth) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string k = upper_key(what);
+  if (k == "TAU") { meth->tau = val; return PSFUN_SUCCESS; }
   return PSFUN_ERR_INVALID_ARGS_COMBINATION;
 }
 int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val) {

@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(kVecThreads) k_init(KState st, const double* _
     if (b == 0.0) {
       c->done = 1;
       c->itx = 0;
+      if (st.host_flag) st.host_flag[0] = 1;
     } else {
       st.s[1] = 1.0 / b;
     }
@@ -571,6 +572,59 @@ __global__ void k_estimate_tail(KState st, int i, double eps) {
   estimate_tail(st, i, eps, red);
 }
 
+// Shift-and-invert Arnoldi (psfun_d_saiarnoldi, krylov/rational/psfun_d_sai.f90):
+// the right-hand side of the inner solve, b = v_{i-1} = s_{i-1} W_{i-1}, into
+// u, and its initial guess into slot i: the w of the previous step after its
+// Gram-Schmidt sweep (slot i-1, unnormalised), zero at the first step (:204-205).
+__global__ void __launch_bounds__(kVecThreads) k_sai_rhs(KState st, int i) {
+  if (st.ctrl->done) return;
+  const double sc = st.s[i - 1];
+  const double* __restrict__ w = WAT(st, i - 1);
+  double* __restrict__ x0 = WAT(st, i);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < st.n; r += stride) {
+    const double v = w[r];
+    st.u[r] = sc * v;
+    x0[r] = (i == 2) ? 0.0 : v;
+  }
+}
+
+// Shift-and-invert estimate of step i (:222-276): yk = f(hcomp) e1 with
+// hcomp = inv(H(1:i-1,1:i-1)) and, as in the reference's loop
+// `do j=1,i-1,i`, only hcomp(1,1) shifted by -tau; then the residual estimate
+// of the Arnoldi method.
+__global__ void __launch_bounds__(kDenseThreads) k_sai_estimate(KState st, FunParams fp, int i, double eps,
+                                                                double tau) {
+  __shared__ DenseSmem sm;
+  KCtrl* c = st.ctrl;
+  if (c->done) return;
+  const int m = i - 1;
+  double* Aw = st.ework;
+  double* Bi = st.ework + (size_t)m * m;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int col = t / m, r = t - col * m;
+    Aw[t] = HAT(st, r + 1, col + 1);
+    Bi[t] = (r == col) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  int rc = cta_gesv(m, m, Aw, m, Bi, m, sm) ? 0 : DEVERR_SINGULAR;
+  if (!rc) {
+    if (threadIdx.x == 0) Bi[0] -= tau;
+    __syncthreads();
+    rc = fh_apply_cta(fp, m, Bi, m, st.e1, st.yk, st.fscratch, false, sm);
+  }
+  if (rc) {
+    if (threadIdx.x == 0) {
+      atomicOr(&c->err, rc);
+      c->info = PSFUN_ERR_FROM_SUBROUTINE_NON;
+      c->done = 1;
+      if (st.host_flag) st.host_flag[0] = 1;
+    }
+    return;
+  }
+  estimate_tail(st, i, eps, sm.red);
+}
+
 // Final f(H) e1 when no estimate converged, and the assembly coefficients
 // (psfun_d_arnoldi.f90:282-329, psfun_d_lanczos.f90:330-377).
 // mode: 0 = compute f on the device, 1 = yk already computed (USERF).
@@ -807,9 +861,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   (void)itrace;
   char kn[32];
   upper_trim(meth->kname, kn, sizeof kn);
-  int arnoldi;
+  int arnoldi, sai = 0;
   if (!strcmp(kn, "ARNOLDI")) arnoldi = 1;
   else if (!strcmp(kn, "LANCZOS")) arnoldi = 0;
+  else if (!strcmp(kn, "SAIARNOLDI")) arnoldi = sai = 1;
   else {
     set_last_error(std::string("kname not available: ") + kn);
     return PSFUN_ERR_INVALID_ARGS_COMBINATION;  // psfun_d_krylov_mod.F90:265-266
@@ -828,6 +883,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   }
   const bool userf = (fp.fname == FN_USERF);
   if (userf && !fun->f_ptr) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+  if (userf && sai) {
+    set_last_error("SAIARNOLDI: USERF functions are not available with the shift-and-invert method");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
   const int64_t n = a->n;
   PSF_TRY(ensure_workspace(meth, n, nl, fp.phiorder));
   cudaStream_t s = stream();
@@ -899,9 +958,24 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   };
   auto enqueue_step = [&](int i) -> int {
     if (arnoldi) {
-      prof_begin(PROF_AR_SPMV, s);
-      k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
-      prof_end(PROF_AR_SPMV, s);
+      if (sai) {
+        // w = (A + tau I)^{-1} v_{i-1} by the inner CG (kmethd), with the
+        // outer eps and the method's itmax / istopc (:204-205)
+        k_sai_rhs<<<gv, kVecThreads, 0, s>>>(st, i);
+        count_launch();
+        int cit = 0;
+        double cerr = 0.0;
+        const int rc = cg_device(a, meth->prec, st.u, 1.0, meth->tau, WAT(st, i), eps, meth->itmax, meth->istopc,
+                                 &cit, &cerr);
+        if (rc != PSFUN_SUCCESS) {
+          set_last_error("SAIARNOLDI: inner CG failed");
+          return PSFUN_ERR_FROM_SUBROUTINE_NON;
+        }
+      } else {
+        prof_begin(PROF_AR_SPMV, s);
+        k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
+        prof_end(PROF_AR_SPMV, s);
+      }
       prof_begin(PROF_AR_MGS, s);
       if (gms > 0) {
         unsigned bar_base = (unsigned)((int64_t)(i - 1) * i / 2 - 1);  // barriers of steps 2..i-1
@@ -913,7 +987,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
         PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
       }
       prof_end(PROF_AR_MGS, s);
-      count_launch(2);
+      count_launch(sai ? 1 : 2);
     } else {
       prof_begin(PROF_LZ_SPMV, s);
       PSF_TRY(launch_lz_persist(st, A, i, i + 1, s));
@@ -934,7 +1008,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     return PSFUN_SUCCESS;
   };
 
-  if (istop == 2 && !userf && !prof_enabled()) {
+  if (istop == 2 && !userf && !prof_enabled() && !sai) {
     // fixed-length solve: one CUDA graph, captured once per launch key
     struct Key {
       const void* a; const void* x; void* y; const void* V; int64_t n; int nl, arnoldi, keeplast, gs, gv, gm;
@@ -979,12 +1053,19 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     PSF_TRY(enqueue_epilogue(0));
   } else {
     PSF_TRY(enqueue_prologue(true));
+    if (sai) {  // the inner solves run host-synchronously: stop at once on a zero x
+      PSF_CUDA(cudaStreamSynchronize(s));
+    }
     const int max_ahead = 24;
     for (int i = 2; i <= nl; ++i) {
-      if (istop == 1 && hflag[0]) break;
+      if ((istop == 1 || sai) && hflag[0]) break;
       PSF_TRY(enqueue_step(i));
       if (istop == 1) {
-        if (userf) {
+        if (sai) {
+          k_sai_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, meth->tau);
+          count_launch();
+          PSF_CUDA(cudaStreamSynchronize(s));  // the next inner solve waits for the verdict
+        } else if (userf) {
           // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
           PSF_CUDA(cudaStreamSynchronize(s));
           KCtrl hc;

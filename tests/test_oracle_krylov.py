@@ -145,3 +145,34 @@ def test_arnoldi_other_functions(orc, fname, variant, k):
     assert r["info"] == 0
     ref = orc.dense_phi1_times(A.toarray(), x, t) if fname == "PHI" else orc.dense_expm_times(A.toarray(), x, t)
     assert np.linalg.norm(r["y"] - ref) / np.linalg.norm(ref) < 1e-9
+
+
+def test_oracle_saiarnoldi_tau0_matches_dense_expm(orc):
+    """psfun_d_saiarnoldi restated (krylov/rational/psfun_d_sai.f90): with
+    tau = 0 the shift quirk is void and a converged estimate gives exp(A)x on a
+    negative definite A (the inner CG solves A w = v)."""
+    import scipy.linalg as sl
+    A = -matrices.laplacian_2d(20)
+    x = matrices.unit(np.random.default_rng(3).standard_normal(A.shape[0]))
+    ref = sl.expm(A.toarray()) @ x
+    for prec in ("NONE", "DIAG"):
+        r = orc.saiarnoldi(orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-10, tau=0.0,
+                           prec=prec, istop=1, itmax=40)
+        assert r["info"] == 0 and r["err"] < 1e-10
+        assert np.linalg.norm(r["y"] - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def test_oracle_saiarnoldi_reference_quirks(orc):
+    """Only hcomp(1,1) is shifted (`do j=1,i-1,i`, :296-298), so tau != 0 does
+    not converge to exp(A)x; without a converged estimate the assembly applies f
+    to H itself (:346-368).  The restatement keeps both."""
+    import scipy.linalg as sl
+    A = -matrices.laplacian_2d(20)
+    x = matrices.unit(np.random.default_rng(3).standard_normal(A.shape[0]))
+    ref = sl.expm(A.toarray()) @ x
+    r = orc.saiarnoldi(orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-10, tau=-1.0, istop=1,
+                       itmax=40)
+    assert r["info"] == 0 and np.linalg.norm(r["y"] - ref) > 0.1 * np.linalg.norm(ref)
+    r2 = orc.saiarnoldi(orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-10, tau=0.0, istop=2,
+                        itmax=40)
+    assert r2["info"] == 0 and r2["iter"] == 39
