@@ -170,11 +170,11 @@ def cpu_baseline(A, x, budget_s: float = 20.0, max_solves: int = 5):
 
 
 def bench_batched(torch, pg, scale: float = 1.0, reps: int = 2):
-    """Config 4: 64 uneven instances x 4 right-hand sides, exp(-t_k A_k) X_k,
+    """64 uneven instances x 4 right-hand sides, exp(-t_k A_k) X_k,
     Lanczos m <= 60, eps 1e-8.  Batched (one persistent launch) against the
     plain path (one drop-in call per instance and right-hand side)."""
     from psfun_gb300 import matrices
-    probs = matrices.config4(scale=scale)
+    probs = matrices.uneven_batch(scale=scale)
     fun = pg.PsfunDSerial()
     fun.set("FNAME", "EXP")
     fun.set("VARIANT", "CHBSYM")
@@ -249,7 +249,7 @@ def bench_arnoldi_phi(torch, pg, peak_gbs: float, reps: int = 3):
     one-pass modified Gram-Schmidt of the new vector against the i previous
     ones, B_spmv + 8 n i + 16 n."""
     from psfun_gb300 import matrices
-    p = matrices.config2b()
+    p = matrices.convdiff_phi1()
     A, x = p.A, p.x
     n, nnz, m = A.shape[0], A.nnz, 60
     a = pg.CsrMatrix.from_scipy(A)
@@ -282,7 +282,7 @@ def bench_multishift(torch, pg, peak_gbs: float, reps: int = 3):
     B_spmv + 32 n (the Lanczos step), plus 8 n per basis vector for the final
     recombination."""
     from psfun_gb300 import matrices
-    p = matrices.config3()
+    p = matrices.laplace3d_invsqrt()
     A, x = p.A, p.x
     n, nnz = A.shape[0], A.nnz
     q = pg.PsfunZQuadrature()
@@ -335,7 +335,7 @@ def bench_adjoint(torch, pg, reps: int = 3):
     the forward exp(tA)x against forward plus all gradients (x, t, and every
     stored entry of A, from which dL/dtheta follows by the chain rule)."""
     from psfun_gb300 import matrices
-    cfg = matrices.config5()
+    cfg = matrices.grid_graph_adjoint()
     N, ei, ej = cfg["N"], cfg["ei"], cfg["ej"]
     n = N * N
     a = pg.CsrMatrix.from_scipy(matrices.graph_laplacian(n, ei, ej, cfg["theta"]))

@@ -4,16 +4,16 @@ The reference's drivers read MatrixMarket files (examples/polynomial/arnolditest
 and ship one fixture, a 50 x 50 1-D Laplacian (examples/polynomial/laplacian.mtx).
 The benchmark problems are synthetic and seeded (numpy default_rng):
 
-  config1   2-D 5-point Dirichlet Laplacian 100 x 100, stencil [-1,-1,4,-1,-1],
-            x ~ U[-1,1]^n (seed 0) normalised; y = exp(-A) x
-  config2a  3-D 7-point Laplacian 128^3 (unscaled), x ~ N(0,1) (seed 1) normalised;
-            y = exp(-0.05 A) x by Lanczos, m = 80
-  config2b  2-D convection-diffusion 2048^2, -Lap u + beta.grad u, beta = (50, 25),
-            first-order upwind, h = 1/2049, scaled by h^-2 / h^-1; y = phi_1(-1e-3 A) x
-  config3   3-D 7-point Laplacian 96^3, x ~ N(0,1) (seed 2); y = A^{-1/2} x by the
-            HHT rule with N = 24 and the analytic spectrum bounds
-  config4   64 uneven instances (seed 3), 4 right-hand sides each
-  config5   512^2 grid-graph Laplacian with lognormal(0,0.7) conductivities (seed 4)
+  laplace2d_expm      2-D 5-point Dirichlet Laplacian 100 x 100, stencil [-1,-1,4,-1,-1],
+                      x ~ U[-1,1]^n (seed 0) normalised; y = exp(-A) x
+  laplace3d_lanczos   3-D 7-point Laplacian 128^3 (unscaled), x ~ N(0,1) (seed 1) normalised;
+                      y = exp(-0.05 A) x by Lanczos, m = 80
+  convdiff_phi1       2-D convection-diffusion 2048^2, -Lap u + beta.grad u, beta = (50, 25),
+                      first-order upwind, h = 1/2049, scaled by h^-2 / h^-1; y = phi_1(-1e-3 A) x
+  laplace3d_invsqrt   3-D 7-point Laplacian 96^3, x ~ N(0,1) (seed 2); y = A^{-1/2} x by the
+                      HHT rule with N = 24 and the analytic spectrum bounds
+  uneven_batch        64 uneven instances (seed 3), 4 right-hand sides each
+  grid_graph_adjoint  512^2 grid-graph Laplacian with lognormal(0,0.7) conductivities (seed 4)
 """
 from __future__ import annotations
 
@@ -148,33 +148,33 @@ class Problem:
     params: dict
 
 
-def config1() -> Problem:
+def laplace2d_expm() -> Problem:
     A = laplacian_2d(100)
     x = unit(np.random.default_rng(0).uniform(-1.0, 1.0, A.shape[0]))
     return Problem("laplace2d-100x100 exp(-A)x m<=50 eps=1e-10", A, x,
                    dict(t=1.0, itmax=50, eps=1e-10))
 
 
-def config2a(n1: int = 128) -> Problem:
+def laplace3d_lanczos(n1: int = 128) -> Problem:
     A = laplacian_3d(n1)
     x = unit(np.random.default_rng(1).standard_normal(A.shape[0]))
     return Problem(f"laplace3d-{n1}^3 exp(-0.05A)x lanczos m=80", A, x, dict(t=0.05, m=80))
 
 
-def config2b(N: int = 2048) -> Problem:
+def convdiff_phi1(N: int = 2048) -> Problem:
     A = convdiff_2d(N)
     x = unit(np.random.default_rng(1).standard_normal(A.shape[0]))
     return Problem(f"convdiff2d-{N}^2 phi1(-1e-3A)x arnoldi m=60", A, x, dict(t=1e-3, m=60))
 
 
-def config3(n1: int = 96) -> Problem:
+def laplace3d_invsqrt(n1: int = 96) -> Problem:
     A = laplacian_3d(n1)
     x = np.random.default_rng(2).standard_normal(A.shape[0])
     return Problem(f"laplace3d-{n1}^3 A^-1/2 x HHT N=24", A, x,
                    dict(N=24, bounds=laplacian_3d_bounds(n1), eps=1e-10))
 
 
-def config4(count: int = 64, nrhs: int = 4, scale: float = 1.0):
+def uneven_batch(count: int = 64, nrhs: int = 4, scale: float = 1.0):
     """64 uneven instances: 32 2-D Laplacians (side ~ U{64..512}) and 32 kNN
     random-geometric-graph Laplacians (n log-uniform in [4096, 262144]);
     `scale` < 1 shrinks the sizes for tests."""
@@ -197,7 +197,7 @@ def config4(count: int = 64, nrhs: int = 4, scale: float = 1.0):
     return out
 
 
-def config5(N: int = 512):
+def grid_graph_adjoint(N: int = 512):
     rng = np.random.default_rng(4)
     ei, ej = grid_edges(N)
     theta = rng.lognormal(0.0, 0.7, size=ei.shape[0])

@@ -8,8 +8,8 @@ does not need to).
    examples/polynomial/laplacian.mtx (checked equal to tridiag(1,-2,1), n=50).
 3. driver_scenarios.npz  -- oracle outputs for the reference's driver
    scenarios on that matrix (arnolditest / lanczostest / serialtest with the
-   driver's eps 1e-6, itmax 100, istop 1, x = ones) and for config 1
-   (100 x 100 5-point Laplacian, exp(-A)x, m <= 50, eps 1e-10).
+   driver's eps 1e-6, itmax 100, istop 1, x = ones) and for the
+   100 x 100 5-point Laplacian problem (exp(-A)x, m <= 50, eps 1e-10).
 """
 from __future__ import annotations
 
@@ -71,17 +71,17 @@ def main():
     y, info = orc.serial_apply(orc.serial("EXP", "GENPADE", 1.0), T.toarray(), ones)
     fix.update(serial_y=y)
 
-    # config 1: 100x100 5-point Laplacian, exp(-A)x, m <= 50, eps 1e-10
-    p = matrices.config1()
+    # 100x100 5-point Laplacian, exp(-A)x, m <= 50, eps 1e-10
+    p = matrices.laplace2d_expm()
     C1 = orc.Csr.from_scipy(p.A)
     r = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", -1.0), C1, p.x, 1e-10, itmax=50, istop=1)
-    fix.update(c1_arn_y=r["y"], c1_arn_iter=r["iter"], c1_arn_err=r["err"], c1_arn_res=r["res"])
+    fix.update(lap2d_arn_y=r["y"], lap2d_arn_iter=r["iter"], lap2d_arn_err=r["err"], lap2d_arn_res=r["res"])
     Cm = orc.Csr.from_scipy(-p.A)
     r = orc.krylov("LANCZOS", orc.serial("EXP", "CHBSYM", 1.0), Cm, p.x, 1e-10, itmax=50, istop=1)
-    fix.update(c1_lz_y=r["y"], c1_lz_iter=r["iter"], c1_lz_err=r["err"], c1_lz_res=r["res"])
+    fix.update(lap2d_lz_y=r["y"], lap2d_lz_iter=r["iter"], lap2d_lz_err=r["err"], lap2d_lz_res=r["res"])
     # dense oracle: exp(-A) = exp(-T) (x) exp(-T) for the Kronecker sum
     X = p.x.reshape(100, 100)
-    fix["c1_dense_y"] = orc.kron_expm_2d_times(matrices.laplacian_1d(100).toarray(), X).ravel()
+    fix["lap2d_dense_y"] = orc.kron_expm_2d_times(matrices.laplacian_1d(100).toarray(), X).ravel()
     np.savez_compressed(HERE / "driver_scenarios.npz", **{k: np.asarray(v) for k, v in fix.items()})
     print({k: (v if np.ndim(v) == 0 else np.shape(v)) for k, v in fix.items()})
 

@@ -1,4 +1,4 @@
-"""Adjoint of y = exp(tA(theta)) x on grid-graph Laplacians (config 5).
+"""Adjoint of y = exp(tA(theta)) x on grid-graph Laplacians.
 
 Oracles: the dense FP64 Frechet derivative (expm of the block matrix
 [[M, E], [0, M]], and the equivalent eigen divided differences) on a 32 x 32
@@ -130,7 +130,7 @@ class ExpmAction:
 
 
 def test_autograd_full_size_vs_finite_differences(lib):
-    """Config 5: 512 x 512 grid, L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2.
+    """512 x 512 grid, L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2.
 
     Central differences with h = 1e-6 carry their own FP64 rounding floor of
     about eps * L / h (L ~ 4.5e3 here, i.e. ~5e-6 on each derivative), so a
@@ -139,7 +139,7 @@ def test_autograd_full_size_vs_finite_differences(lib):
     above that floor and are held to 1e-6 relative."""
     torch = pytest.importorskip("torch")
     import psfun_gb300 as pg
-    cfg = matrices.config5()
+    cfg = matrices.grid_graph_adjoint()
     N, ei, ej = cfg["N"], cfg["ei"], cfg["ej"]
     n = N * N
     Fn = ExpmAction.make(ei, ej, n)

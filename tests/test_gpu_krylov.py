@@ -38,23 +38,23 @@ def run_orc(orc, kname, fname, variant, scaling, A, x, eps, itmax=200, istop=1, 
                       eps, itmax=itmax, istop=istop, drop_last=not keeplast)
 
 
-def test_config1_arnoldi(lib):
-    p = matrices.config1()
+def test_laplace2d_100_arnoldi(lib):
+    p = matrices.laplace2d_expm()
     r = run_gpu("ARNOLDI", "EXP", "GENPADE", -1.0, p.A, p.x, 1e-10, itmax=50)
     assert r.info == 0
-    assert r.iter == int(FIX["c1_arn_iter"]) == 18
-    assert rel(r.y, FIX["c1_arn_y"]) <= TOL
-    assert rel(r.y, FIX["c1_dense_y"]) <= 1e-10
-    assert abs(r.err - float(FIX["c1_arn_err"])) <= 1e-6 * float(FIX["c1_arn_err"])
-    assert np.allclose(r.res, FIX["c1_arn_res"], rtol=1e-6, atol=0)
+    assert r.iter == int(FIX["lap2d_arn_iter"]) == 18
+    assert rel(r.y, FIX["lap2d_arn_y"]) <= TOL
+    assert rel(r.y, FIX["lap2d_dense_y"]) <= 1e-10
+    assert abs(r.err - float(FIX["lap2d_arn_err"])) <= 1e-6 * float(FIX["lap2d_arn_err"])
+    assert np.allclose(r.res, FIX["lap2d_arn_res"], rtol=1e-6, atol=0)
 
 
-def test_config1_lanczos(lib):
-    p = matrices.config1()
+def test_laplace2d_100_lanczos(lib):
+    p = matrices.laplace2d_expm()
     r = run_gpu("LANCZOS", "EXP", "CHBSYM", 1.0, -p.A, p.x, 1e-10, itmax=50)
-    assert r.info == 0 and r.iter == int(FIX["c1_lz_iter"])
-    assert rel(r.y, FIX["c1_lz_y"]) <= TOL
-    assert rel(r.y, FIX["c1_dense_y"]) <= 1e-10
+    assert r.info == 0 and r.iter == int(FIX["lap2d_lz_iter"])
+    assert rel(r.y, FIX["lap2d_lz_y"]) <= TOL
+    assert rel(r.y, FIX["lap2d_dense_y"]) <= 1e-10
 
 
 @pytest.mark.parametrize("kname,variant,fix", [("ARNOLDI", "GENPADE", "arn"), ("LANCZOS", "CHBSYM", "lz")])
@@ -105,11 +105,11 @@ def test_lanczos_ignores_scaling(lib, orc):
 
 
 def test_keeplast(lib, orc):
-    p = matrices.config1()
+    p = matrices.laplace2d_expm()
     g = run_gpu("ARNOLDI", "EXP", "GENPADE", -1.0, p.A, p.x, 1e-10, itmax=50, keeplast=True)
     o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", -1.0, p.A, p.x, 1e-10, itmax=50, keeplast=True)
     assert g.info == 0 and g.iter == o["iter"] and rel(g.y, o["y"]) <= TOL
-    assert rel(g.y, FIX["c1_dense_y"]) < rel(FIX["c1_arn_y"], FIX["c1_dense_y"])
+    assert rel(g.y, FIX["lap2d_dense_y"]) < rel(FIX["lap2d_arn_y"], FIX["lap2d_dense_y"])
 
 
 @pytest.mark.parametrize("kname", ["ARNOLDI", "LANCZOS"])
@@ -181,7 +181,7 @@ def test_null_projected_matrix_is_error(lib):
 def test_device_api_matches_host_api(lib):
     torch = pytest.importorskip("torch")
     import psfun_gb300 as pg
-    p = matrices.config1()
+    p = matrices.laplace2d_expm()
     fun = pg.PsfunDSerial()
     fun.set("FNAME", "EXP"); fun.set("VARIANT", "GENPADE"); fun.set("SCALING", -1.0)
     meth = pg.PsfunDKrylov()
@@ -194,7 +194,7 @@ def test_device_api_matches_host_api(lib):
 
 
 def test_repeatable_bitwise(lib):
-    p = matrices.config1()
+    p = matrices.laplace2d_expm()
     r1 = run_gpu("ARNOLDI", "EXP", "GENPADE", -1.0, p.A, p.x, 1e-10, itmax=50)
     r2 = run_gpu("ARNOLDI", "EXP", "GENPADE", -1.0, p.A, p.x, 1e-10, itmax=50)
     assert np.array_equal(r1.y, r2.y)

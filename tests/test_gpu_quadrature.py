@@ -48,11 +48,11 @@ def test_quadrature_matches_its_rule(lib, n1):
     assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-9
 
 
-def test_config3_full_size(lib):
-    """96^3, N = 24 (config 3).  Solver error: the GPU sum equals the HHT rule
+def test_laplace3d_96_full_size(lib):
+    """A^{-1/2} x on the 96^3 Laplacian, N = 24.  Solver error: the GPU sum equals the HHT rule
     evaluated exactly in the eigenbasis.  The rule itself is only accurate to
     ~1.6e-6 at kappa ~ 3800 with 24 poles (a property of the published rule)."""
-    p = matrices.config3()
+    p = matrices.laplace3d_invsqrt()
     q, (y, info, it, err) = run(96, 24, p.x, eps=1e-13)
     assert info == 0 and err < 1e-13
 
@@ -65,10 +65,10 @@ def test_config3_full_size(lib):
     assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 2e-6
 
 
-def test_config3_48_poles(lib):
+def test_laplace3d_96_48_poles(lib):
     """The shifts share one Lanczos basis, so 48 poles cost the same Krylov steps:
     A^{-1/2} x on 96^3 to ~1e-12."""
-    p = matrices.config3()
+    p = matrices.laplace3d_invsqrt()
     q, (y, info, it, err) = run(96, 48, p.x, eps=1e-13)
     assert info == 0
     ref = apply_fun_3d(96, p.x, lambda L: L ** -0.5)

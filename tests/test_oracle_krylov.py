@@ -11,32 +11,32 @@ from psfun_gb300 import matrices
 FIX = np.load(Path(__file__).parent / "golden" / "driver_scenarios.npz")
 
 
-def test_config1_arnoldi_vs_dense(orc):
-    p = matrices.config1()
+def test_laplace2d_100_arnoldi_vs_dense(orc):
+    p = matrices.laplace2d_expm()
     r = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", -1.0), orc.Csr.from_scipy(p.A), p.x, 1e-10, itmax=50)
     assert r["info"] == 0 and r["iter"] == 18
-    dense = FIX["c1_dense_y"]
+    dense = FIX["lap2d_dense_y"]
     rel = np.linalg.norm(r["y"] - dense) / np.linalg.norm(dense)
     assert rel < 1e-10
-    assert np.array_equal(r["y"], FIX["c1_arn_y"]) or np.linalg.norm(r["y"] - FIX["c1_arn_y"]) < 1e-13
+    assert np.array_equal(r["y"], FIX["lap2d_arn_y"]) or np.linalg.norm(r["y"] - FIX["lap2d_arn_y"]) < 1e-13
 
 
-def test_config1_lanczos_vs_dense(orc):
-    p = matrices.config1()
+def test_laplace2d_100_lanczos_vs_dense(orc):
+    p = matrices.laplace2d_expm()
     r = orc.krylov("LANCZOS", orc.serial("EXP", "CHBSYM", 1.0), orc.Csr.from_scipy(-p.A), p.x, 1e-10, itmax=50)
     assert r["info"] == 0
-    dense = FIX["c1_dense_y"]
+    dense = FIX["lap2d_dense_y"]
     assert np.linalg.norm(r["y"] - dense) / np.linalg.norm(dense) < 1e-10
 
 
 def test_drop_last_quirk(orc):
     """Assembly sums yk(1..itx-1) while yk has itx entries (psfun_d_arnoldi.f90:325-328):
     keeping every term is more accurate."""
-    p = matrices.config1()
+    p = matrices.laplace2d_expm()
     A = orc.Csr.from_scipy(p.A)
     r1 = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", -1.0), A, p.x, 1e-10, itmax=50, drop_last=True)
     r2 = orc.krylov("ARNOLDI", orc.serial("EXP", "GENPADE", -1.0), A, p.x, 1e-10, itmax=50, drop_last=False)
-    d = FIX["c1_dense_y"]
+    d = FIX["lap2d_dense_y"]
     e1 = np.linalg.norm(r1["y"] - d) / np.linalg.norm(d)
     e2 = np.linalg.norm(r2["y"] - d) / np.linalg.norm(d)
     assert e2 < e1

@@ -39,7 +39,7 @@ def _worker(rank, world, port, q):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     orc.set_threads(1)  # fixed reduction order
-    probs = matrices.config4(count=6, nrhs=1, scale=0.02)
+    probs = matrices.uneven_batch(count=6, nrhs=1, scale=0.02)
     costs = [p.A.nnz for p in probs]
     local = {}
     for k in my_instances(costs, rank, world):
@@ -68,7 +68,7 @@ def test_two_rank_gloo_matches_single_rank():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    probs = matrices.config4(count=6, nrhs=1, scale=0.02)
+    probs = matrices.uneven_batch(count=6, nrhs=1, scale=0.02)
     assert sorted(res) == list(range(6))
     orc.set_threads(1)
     for k, p in enumerate(probs):
