@@ -147,6 +147,14 @@ int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val);
  * psfun_d_saiarnoldi (krylov/rational/psfun_d_sai.f90:37-419) with the inner
  * CG on (A + tau I) w = v, inner itmax = ITMAX and istop = ISTOPC. */
 int psfun_gpu_krylov_set_real(psfun_krylov* meth, const char* what, double val);
+/* meth%precinit(ctxt, ptype, info): psfun_d_prec_init (:326-361).  ptype
+ * 'NOPREC' / 'NONE' or 'DIAG'; AMG4PSBLAS's other types (BJAC, AS, ML, ...)
+ * return PSFUN_ERR_FROM_SUBROUTINE.  There is one process, so no context. */
+int psfun_gpu_krylov_precinit(psfun_krylov* meth, const char* ptype);
+/* meth%precbuild(a, desc_a, info): psfun_d_prec_build (:363-403).  For DIAG
+ * it builds the inverse diagonal of a on the device now, cached on the matrix
+ * handle, instead of on the first inner solve that needs it. */
+int psfun_gpu_krylov_precbuild(psfun_krylov* meth, psfun_csr* a);
 /* kmethd%apply(fun,a,desc_a,y,x,eps,info,itmax,itrace,istop,iter,err,res):
  * psfun_d_parallel_apply (:225-269).  itmax/itrace/istop are the optional
  * arguments with the reference defaults 200/0/1 supplied by the caller.

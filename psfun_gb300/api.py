@@ -197,18 +197,38 @@ class PsfunDKrylov:
         h = C.c_void_p()
         _lib().psfun_gpu_krylov_create(C.byref(h))
         self.handle = h
+        self.kname = "ARNOLDI"
 
     def set(self, what: str, val) -> int:
         """set(what, val): KNAME, KMETHD, PREC ('NONE' / 'DIAG') as strings;
         ITMAX, ITRACE, ISTOPC, IRST, KEEPLAST as integers; TAU (the public
         component meth%tau of the reference) as a real."""
         if isinstance(val, str):
-            return _lib().psfun_gpu_krylov_set_string(self.handle, what.encode(), val.encode())
+            info = _lib().psfun_gpu_krylov_set_string(self.handle, what.encode(), val.encode())
+            if info == 0 and what.strip().upper() == "KNAME":
+                self.kname = val
+            return info
         if isinstance(val, (bool, int, np.integer)):
             return _lib().psfun_gpu_krylov_set_integer(self.handle, what.encode(), int(val))
         if isinstance(val, (float, np.floating)):
             return _lib().psfun_gpu_krylov_set_real(self.handle, what.encode(), float(val))
         return ERR_INVALID_ARGS_COMBINATION
+
+    def precinit(self, ptype: str) -> int:
+        """meth%precinit(ctxt, ptype, info) (psfun_d_prec_init,
+        krylov/psfun_d_krylov_mod.F90:326-361): 'NOPREC'/'NONE' or 'DIAG'."""
+        return _lib().psfun_gpu_krylov_precinit(self.handle, ptype.encode())
+
+    def precbuild(self, a: CsrMatrix) -> int:
+        """meth%precbuild(a, desc_a, info) (psfun_d_prec_build, :363-403)."""
+        return _lib().psfun_gpu_krylov_precbuild(self.handle, a.handle)
+
+    def plot(self, fun: PsfunDSerial, iter: int, res, directory: str = ".") -> int:
+        """meth%plot(fun, iter, res, info) (psfun_d_plot_info, :271-324): the
+        residual history res(1:min(size(res), iter+1)) on a log scale, written
+        to '<KNAME>-<FNAME>-<VARIANT>-Residual'.  The reference drives gnuplot
+        to a PDF; this writes an SVG of the same plot with no external tool."""
+        return plot_residual(self.kname, fun, iter, res, directory)
 
     def apply(self, fun: PsfunDSerial, a: CsrMatrix, x, eps: float, itmax: int | None = None,
               itrace: int | None = None, istop: int | None = None, y=None) -> KrylovResult:
@@ -242,6 +262,66 @@ class PsfunDKrylov:
             _lib().psfun_gpu_krylov_destroy(self.handle)
         except Exception:
             pass
+
+
+def plot_residual(kname: str, fun: PsfunDSerial, iter: int, res, directory: str = ".") -> int:
+    """Residual history plot of psfun_d_plot_info (krylov/psfun_d_krylov_mod.F90:271-324):
+    points (j, res(j)) for j = 1..indplot, indplot = size(res) if size(res) <= iter+1
+    else iter+1 (:289-296), y on a log scale, lines with points, file and title
+    '<kname>-<fname>-<variant>-Residual' (:300-304).  Written as SVG by hand
+    (gnuplot is not a dependency); non-positive residuals are left out, as a
+    log axis cannot show them.  Returns 0, or PSFUN_ERR_FROM_SUBROUTINE when
+    the file cannot be written."""
+    import math
+    import os
+    res = np.asarray(res, dtype=np.float64).ravel()
+    n = res.size
+    indplot = n if n <= iter + 1 else iter + 1
+    st = fun.get()
+    tag = f"{kname.strip()}-{st['fname'].strip()}-{st['variant'].strip()}"
+    pts = [(j + 1, float(res[j])) for j in range(indplot) if res[j] > 0 and math.isfinite(res[j])]
+    W, H, L, R, T, B = 640, 480, 80, 20, 40, 50
+    if pts:
+        lo = math.floor(math.log10(min(v for _, v in pts)))
+        hi = math.ceil(math.log10(max(v for _, v in pts)))
+    else:
+        lo, hi = -16, 0
+    hi = max(hi, lo + 1)
+    xmax = max(indplot, 2)
+
+    def px(j):
+        return L + (W - L - R) * (j - 1) / (xmax - 1)
+
+    def py(v):
+        return T + (H - T - B) * (hi - math.log10(v)) / (hi - lo)
+
+    out = [f'<svg xmlns="http://www.w3.org/2000/svg" width="{W}" height="{H}" font-family="sans-serif" font-size="12">',
+           f'<text x="{W / 2}" y="20" text-anchor="middle" font-size="14">Residual history {tag}</text>',
+           f'<rect x="{L}" y="{T}" width="{W - L - R}" height="{H - T - B}" fill="none" stroke="black"/>',
+           f'<text x="{(W + L - R) / 2}" y="{H - 12}" text-anchor="middle">Iteration</text>',
+           f'<text x="18" y="{(H + T - B) / 2}" text-anchor="middle" transform="rotate(-90 18 {(H + T - B) / 2})">'
+           'Relative Residual</text>']
+    step = max(1, (hi - lo) // 8)
+    for e in range(lo, hi + 1, step):
+        y = py(10.0 ** e)
+        out.append(f'<line x1="{L - 4}" y1="{y:.1f}" x2="{L}" y2="{y:.1f}" stroke="black"/>'
+                   f'<text x="{L - 8}" y="{y + 4:.1f}" text-anchor="end">10^{e}</text>')
+    xstep = max(1, int(math.ceil((xmax - 1) / 10)))
+    for j in range(1, xmax + 1, xstep):
+        x = px(j)
+        out.append(f'<line x1="{x:.1f}" y1="{H - B}" x2="{x:.1f}" y2="{H - B + 4}" stroke="black"/>'
+                   f'<text x="{x:.1f}" y="{H - B + 18}" text-anchor="middle">{j}</text>')
+    if pts:
+        poly = " ".join(f"{px(j):.1f},{py(v):.1f}" for j, v in pts)
+        out.append(f'<polyline points="{poly}" fill="none" stroke="#d62728"/>')
+        out.extend(f'<circle cx="{px(j):.1f}" cy="{py(v):.1f}" r="3" fill="#d62728"/>' for j, v in pts)
+    out.append("</svg>")
+    try:
+        with open(os.path.join(directory, tag + "-Residual.svg"), "w") as f:
+            f.write("\n".join(out) + "\n")
+    except OSError:
+        return ERR_FROM_SUBROUTINE
+    return 0
 
 
 def krylov_batch(meth: "PsfunDKrylov", fun: "PsfunDSerial", items, eps: float, itmax: int = 200,

@@ -539,6 +539,22 @@ int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char
   }
   return PSFUN_ERR_INVALID_ARGS_COMBINATION;
 }
+int psfun_gpu_krylov_precinit(psfun_krylov* meth, const char* ptype) {
+  if (!meth || !ptype) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const std::string v = upper_key(ptype);
+  if (v == "NONE" || v == "NOPREC") meth->prec = 0;
+  else if (v == "DIAG") meth->prec = 1;
+  else {
+    psf::set_last_error("precinit: preconditioner type '" + v + "' is not available (NOPREC, NONE and DIAG are)");
+    return PSFUN_ERR_FROM_SUBROUTINE;
+  }
+  return PSFUN_SUCCESS;
+}
+int psfun_gpu_krylov_precbuild(psfun_krylov* meth, psfun_csr* a) {
+  if (!meth || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (meth->prec == 1) PSF_TRY(psf::csr_build_diag_inv(a));
+  return PSFUN_SUCCESS;
+}
 int psfun_gpu_krylov_set_real(psfun_krylov* meth, const char* what, double val) {
   if (!meth) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   const std::string k = upper_key(what);

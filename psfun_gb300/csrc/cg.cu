@@ -316,6 +316,36 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
   }
 }
 
+int csr_build_diag_inv(psfun_csr* a) {
+  if (a->diag_inv) return PSFUN_SUCCESS;
+  // DIAG: inverse diagonal of A (a zero diagonal entry is left as 1), cached
+  // on the matrix handle until the handle is destroyed
+  const int64_t n = a->n;
+  cudaStream_t s = stream();
+  double* inv = nullptr;
+  double* dtmp = nullptr;
+  PSF_CUDA(cudaMalloc(&inv, sizeof(double) * (n + 1)));
+  if (cudaMalloc(&dtmp, sizeof(double) * (n + 1)) != cudaSuccess) {
+    cudaFree(inv);
+    set_last_error("csr_build_diag_inv: cudaMalloc failed");
+    return PSFUN_ERR_ALLOC_DEALLOC;
+  }
+  cudaError_t e = cudaMemcpyAsync(dtmp, a->h_diag.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_diag_inv<<<256, 256, 0, s>>>(n, dtmp, inv);
+    count_launch();
+    e = cudaStreamSynchronize(s);
+  }
+  cudaFree(dtmp);
+  if (e != cudaSuccess) {
+    cudaFree(inv);
+    set_last_error(std::string("csr_build_diag_inv: ") + cudaGetErrorString(e));
+    return PSFUN_ERR_CUDA;
+  }
+  a->diag_inv = inv;
+  return PSFUN_SUCCESS;
+}
+
 int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
               int istop, int* iter, double* err) {
   if (istop < 1 || istop > 2) return PSFUN_ERR_INVALID_ISTOP;
@@ -327,17 +357,7 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   PSF_TRY(work.ensure(sizeof(double) * 4 * ld + 64));
   PSF_TRY(ctrlb.ensure(sizeof(CgCtrl) + 64));
   PSF_TRY(partb.ensure(sizeof(double) * 3 * 4096));
-  if (prec == 1 && !a->diag_inv) {
-    // DIAG: inverse diagonal of A (a zero diagonal entry is left as 1)
-    double* dtmp = nullptr;
-    PSF_CUDA(cudaMalloc(&a->diag_inv, sizeof(double) * (n + 1)));
-    PSF_CUDA(cudaMalloc(&dtmp, sizeof(double) * (n + 1)));
-    PSF_CUDA(cudaMemcpyAsync(dtmp, a->h_diag.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    k_diag_inv<<<256, 256, 0, s>>>(n, dtmp, a->diag_inv);
-    count_launch();
-    PSF_CUDA(cudaStreamSynchronize(s));
-    cudaFree(dtmp);
-  }
+  if (prec == 1) PSF_TRY(csr_build_diag_inv(a));
   CgState st;
   st.n = n;
   st.istop = istop;

@@ -3,6 +3,8 @@ include/*.h declares."""
 import re
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent.parent
 
 
@@ -44,3 +46,32 @@ def test_setters_without_gpu(lib):
     k = pg.PsfunDKrylov()
     assert k.set("kname", "LANCZOS") == 0 and k.set("itmax", 10) == 0 and k.set("BAD", 1) == 111
     assert k.set("ITMAX", "x") == 111
+
+
+def test_precinit_types_without_gpu(lib):
+    """precinit (psfun_d_prec_init) accepts the preconditioners that exist here
+    and reports the AMG4PSBLAS-only types as a failed subroutine."""
+    import psfun_gb300 as pg
+    k = pg.PsfunDKrylov()
+    assert k.precinit("NOPREC") == 0 and k.precinit("diag") == 0 and k.precinit("NONE") == 0
+    assert k.precinit("BJAC") == pg.api.ERR_FROM_SUBROUTINE
+    assert b"BJAC" in lib.psfun_gpu_last_error()
+
+
+def test_plot_residual_history(lib, tmp_path):
+    """plot (psfun_d_plot_info): min(size(res), iter+1) points, file named
+    <kname>-<fname>-<variant>-Residual, log axis skipping non-positive values."""
+    import psfun_gb300 as pg
+    f = pg.PsfunDSerial()
+    assert f.set("VARIANT", "GENPADE") == 0
+    k = pg.PsfunDKrylov()
+    assert k.set("KNAME", "Lanczos") == 0
+    res = np.array([1.0, 1e-3, 1e-6, 0.0, 1e-9, 5.0])
+    assert k.plot(f, 4, res, directory=str(tmp_path)) == 0
+    svg = (tmp_path / "Lanczos-EXP-GENPADE-Residual.svg").read_text()
+    assert "Residual history Lanczos-EXP-GENPADE" in svg
+    # iter = 4: the first 5 entries, of which the zero is left out
+    assert svg.count("<circle") == 4
+    assert k.plot(f, 10, res, directory=str(tmp_path)) == 0
+    assert (tmp_path / "Lanczos-EXP-GENPADE-Residual.svg").read_text().count("<circle") == 5
+    assert k.plot(f, 1, res, directory=str(tmp_path / "missing")) == pg.api.ERR_FROM_SUBROUTINE

@@ -59,3 +59,22 @@ def test_sai_errors(lib):
     assert meth.apply(fun, pg.CsrMatrix.from_scipy(A), x, 1e-8, itmax=10).info == 111
     fun2 = pg.PsfunDSerial(); fun2.set("VARIANT", "GENPADE")
     assert meth.apply(fun2, pg.CsrMatrix.from_scipy(A), x, 1e-8, itmax=10, istop=3).info == 5001
+
+
+def test_precinit_precbuild_diag(lib):
+    """precinit('DIAG') + precbuild(a) (psfun_d_prec_init / psfun_d_prec_build)
+    builds the Jacobi preconditioner before apply; the result is identical to
+    building it lazily on the first inner solve."""
+    import psfun_gb300 as pg
+    A = -matrices.laplacian_2d(20)
+    x = matrices.unit(np.random.default_rng(5).standard_normal(A.shape[0]))
+    lazy = run_gpu(A, x, 1e-10, 0.0, 1, 40, "DIAG")
+    fun = pg.PsfunDSerial()
+    assert fun.set("VARIANT", "GENPADE") == 0
+    meth = pg.PsfunDKrylov()
+    a = pg.CsrMatrix.from_scipy(A)
+    assert meth.set("KNAME", "SAIARNOLDI") == 0
+    assert meth.precinit("DIAG") == 0 and meth.precbuild(a) == 0
+    r = meth.apply(fun, a, x, 1e-10, itmax=40, istop=1)
+    assert r.info == 0 and lazy.info == 0 and r.iter == lazy.iter
+    assert np.array_equal(r.y, lazy.y)
