@@ -469,18 +469,35 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
     int l = threadIdx.x;
     if (k + 1 <= i - 1) {  // update with v_k fused with the dot of v_{k+1}
       const double* __restrict__ wn = WAT(st, k + 1) + r0;
-      for (; l + 3 * bd < nloc; l += 4 * bd) {
+      // the next group's loads are issued before this group's arithmetic
+      if (l + 3 * bd < nloc) {
         double a[4], nx[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           a[q] = wk[l + q * bd];
           nx[q] = wn[l + q * bd];
         }
+        for (;;) {
+          const int ln = l + 4 * bd;
+          const bool more = ln + 3 * bd < nloc;
+          double a2[4], nx2[4];
+          if (more) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const double v = fma(-cc, a[q], wl[l + q * bd]);
-          wl[l + q * bd] = v;
-          acc = fma(nx[q], v, acc);
+            for (int q = 0; q < 4; ++q) {
+              a2[q] = wk[ln + q * bd];
+              nx2[q] = wn[ln + q * bd];
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const double v = fma(-cc, a[q], wl[l + q * bd]);
+            wl[l + q * bd] = v;
+            acc = fma(nx[q], v, acc);
+          }
+          l = ln;
+          if (!more) break;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) { a[q] = a2[q]; nx[q] = nx2[q]; }
         }
       }
       for (; l < nloc; l += bd) {
@@ -1010,11 +1027,15 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
 
   if (istop == 2 && !userf && !prof_enabled() && !sai) {
     // fixed-length solve: one CUDA graph, captured once per launch key
+    // the device arrays of the matrix are part of the key: a handle can be
+    // destroyed and another created at the same address
     struct Key {
       const void* a; const void* x; void* y; const void* V; int64_t n; int nl, arnoldi, keeplast, gs, gv, gm;
       FunParams fp; double scaling;
+      const void *irp, *ja, *val, *tiles;
     } key;
     memset(&key, 0, sizeof key);
+    key.irp = A.irp; key.ja = A.ja; key.val = A.val; key.tiles = A.tile_desc;
     key.a = a; key.x = x; key.y = y; key.V = st.V; key.n = n; key.nl = nl; key.arnoldi = arnoldi;
     key.keeplast = meth->keeplast; key.gs = gs; key.gv = gv; key.gm = gm; key.fp = fpk; key.scaling = scaling;
     const unsigned char* kb = reinterpret_cast<const unsigned char*>(&key);

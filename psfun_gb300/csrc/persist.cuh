@@ -31,7 +31,7 @@ struct __align__(128) LzSmem {
   TileInfo info[kLzStages];   // geometry of the staged tile, written by the producer
   double red[kSpmvThreads / 32];
   double vals[kSpmvThreads];  // per-thread partials of a block reduction
-  double scal[4];             // per-step scalars computed by thread 0: alpha, c2, beta, s_{i+1}
+  double scal[8];             // per-step scalars formed by one thread and broadcast to the block
 };
 constexpr size_t kLzSmemBytes = sizeof(LzSmem);
 static_assert(kSpmvThreads == 512, "the persistent kernels reduce with block_sum_store_512");
