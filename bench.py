@@ -381,6 +381,24 @@ def run_reference(args):
     return 0
 
 
+def run_only(name: str) -> int:
+    """One secondary workload on cuda:0, its result as one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import psfun_gb300 as pg
+    from psfun_gb300 import _capi
+    _capi.load()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    fn = {"arnoldi_phi1": lambda: bench_arnoldi_phi(torch, pg, peak),
+          "multishift": lambda: bench_multishift(torch, pg, peak),
+          "adjoint": lambda: bench_adjoint(torch, pg),
+          "cg": lambda: bench_cg(torch, pg, peak),
+          "batched": lambda: bench_batched(torch, pg)}[name]
+    print(json.dumps({name: fn()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -391,9 +409,13 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batched (64-instance) comparison")
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
+    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched"],
+                    help="run one secondary workload alone and print its result (for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args.only)
 
     import torch
     rank, world, local = dist_info()
