@@ -31,6 +31,12 @@ extern "C" {
 #endif
 
 /* ---- status codes: PSBLAS psb_const_mod values used by the reference ---- */
+/* Concurrency: the library keeps per-process state (the current stream set by
+ * psfun_gpu_set_stream, workspaces cached per handle and per entry point,
+ * mapped progress flags).  Calls must not overlap: call it from one host
+ * thread at a time, as the reference's procedures are called by one thread
+ * per MPI rank. */
+
 #define PSFUN_SUCCESS 0
 #define PSFUN_ERR_INVALID_ARGS_COMBINATION 111 /* psb_err_invalid_args_combination_ */
 #define PSFUN_ERR_INVALID_VECT_STATE 1124      /* psb_err_invalid_vect_state_ */
@@ -76,6 +82,12 @@ void* psfun_gpu_get_stream(void);
  * 3 Arnoldi MGS, 4 final f(H), 5 recombination.  Enabling resets the totals. */
 int psfun_gpu_profile_enable(int on);
 int psfun_gpu_profile_read(int kernel, long long* launches, double* total_ms);
+/* No counterpart in the reference.  Runs a device wait that nothing completes
+ * (which 0: a grid barrier short of one arrival; 1: an mbarrier phase nobody
+ * completes) through the same bounded-wait code as the solvers, so that a
+ * test can see the limit expire: returns PSFUN_ERR_DEVICE_TIMEOUT after about
+ * two seconds, with the CUDA context still usable. */
+int psfun_gpu_selftest_wait(int which);
 
 /* ------------------------------------------------------------------------ */
 /* Sparse matrix: replaces the psb_dspmat_type the reference passes to       */
@@ -158,6 +170,8 @@ int psfun_gpu_krylov_precbuild(psfun_krylov* meth, psfun_csr* a);
 /* kmethd%apply(fun,a,desc_a,y,x,eps,info,itmax,itrace,istop,iter,err,res):
  * psfun_d_parallel_apply (:225-269).  itmax/itrace/istop are the optional
  * arguments with the reference defaults 200/0/1 supplied by the caller.
+ * itrace > 0 writes the convergence log to stdout (header, every itrace-th
+ * error estimate, end line) after the solve, not while it runs.
  * res (capacity res_cap, may be NULL) receives the residual history of
  * length iter+1 (psfun_d_arnoldi.f90:319-323); *res_len its length.
  * Host vectors x (in) and y (out) of length n. */

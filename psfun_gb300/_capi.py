@@ -53,6 +53,7 @@ PROTOS = {
     "psfun_gpu_krylov_set_integer": (C.c_int, [vp, C.c_char_p, C.c_int]),
     "psfun_gpu_krylov_set_real": (C.c_int, [vp, C.c_char_p, C.c_double]),
     "psfun_gpu_krylov_precinit": (C.c_int, [vp, C.c_char_p]),
+    "psfun_gpu_selftest_wait": (C.c_int, [C.c_int]),
     "psfun_gpu_krylov_precbuild": (C.c_int, [vp, vp]),
     "psfun_gpu_d_krylov_apply": (C.c_int, [vp, vp, vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_int,
                                            C.POINTER(C.c_int), dp, dp, C.c_int, C.POINTER(C.c_int)]),

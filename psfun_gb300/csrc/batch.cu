@@ -637,6 +637,7 @@ using namespace psf;
 extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count,
                                         const psfun_batch_item* items, double eps, int itmax, int istop,
                                         int* iters, double* errs, int* infos) {
+  psf::NvtxRange nvtx_range("psfun_gpu_d_krylov_batch");
   if (!meth || !fun || count < 1 || !items) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   char kn[32];
   {

@@ -43,6 +43,7 @@ int DevBuf::ensure(size_t need) {
   release();
   cudaError_t e = cudaMalloc(&ptr, need);
   if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // recoverable: keep it out of later launch checks
     ptr = nullptr;
     bytes = 0;
     set_last_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -154,12 +155,58 @@ bool parse_fun(const psfun_serial* fun, FunParams* fp) {
   return false;
 }
 
+// Self-test of the bounded device waits: a wait that nothing completes.
+// which 0: a grid barrier of a 2-CTA cooperative grid whose target is one
+// arrival more than the grid makes; which 1: an mbarrier wait for a phase
+// that no thread or copy completes.  Both give up after kWaitLimitNs and
+// record DEVERR_TIMEOUT, as every wait of the solvers does.
+__global__ void k_selftest_wait(int which, unsigned* counter, int* err) {
+  __shared__ uint64_t bar;
+  if (which == 0) {
+    if (grid_sync_to(counter, gridDim.x + 1u, err)) atomicOr(err, 0x100);  // completed: not expected
+    return;
+  }
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (mbar_wait(&bar, 0u)) atomicOr(err, 0x100);
+    else atomicOr(err, DEVERR_TIMEOUT);
+  }
+}
+
 }  // namespace psf
 
 using namespace psf;
 
 // ---------------------------------------------------------------------------
 extern "C" {
+
+int psfun_gpu_selftest_wait(int which) {
+  if (which < 0 || which > 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  static DevBuf buf;
+  PSF_TRY(buf.ensure(64));
+  cudaStream_t s = stream();
+  PSF_CUDA(cudaMemsetAsync(buf.ptr, 0, 64, s));
+  unsigned* counter = buf.as<unsigned>();
+  int* err = reinterpret_cast<int*>(counter + 4);
+  if (which == 0) {
+    void* args[] = {(void*)&which, (void*)&counter, (void*)&err};
+    PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_selftest_wait, dim3(2), dim3(32), args, 0, s));
+  } else {
+    k_selftest_wait<<<1, 32, 0, s>>>(which, counter, err);
+  }
+  count_launch();
+  PSF_CUDA(cudaGetLastError());
+  int h = 0;
+  PSF_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (h & DEVERR_TIMEOUT) {
+    set_last_error("self-test: the bounded device wait expired and reported it");
+    return PSFUN_ERR_DEVICE_TIMEOUT;
+  }
+  set_last_error("self-test: the wait completed or reported nothing");
+  return PSFUN_ERR_INTERNAL;
+}
 
 const char* psfun_gpu_version(void) { return "psfun_gb300 0.1 (sm_103a)"; }
 const char* psfun_gpu_last_error(void) { return g_last_error.c_str(); }
@@ -270,6 +317,7 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
   a->norm_inf = ninf;
   cudaStream_t s = stream();
   auto fail = [&](cudaError_t e) {
+    (void)cudaGetLastError();
     set_last_error(std::string("csr_create: ") + cudaGetErrorString(e));
     psfun_gpu_csr_destroy(a);
     return PSFUN_ERR_CUDA;
@@ -364,11 +412,13 @@ int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double
 extern "C" {
 
 int psfun_gpu_csr_spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
+  psf::NvtxRange nvtx_range("psfun_gpu_csr_spmv_device");
   if (!a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   return spmv_device(a, alpha, x, beta, y);
 }
 
 int psfun_gpu_csr_spmv(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
+  psf::NvtxRange nvtx_range("psfun_gpu_csr_spmv");
   if (!a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   const size_t nb = sizeof(double) * (a->n + 1);
   DevBuf dx, dy;
@@ -441,6 +491,7 @@ int psfun_gpu_serial_get(const psfun_serial* fun, char* fname, char* variant, do
 }
 
 int psfun_gpu_serial_apply(psfun_serial* fun, int n, const double* a, int lda, double* y, const double* x) {
+  psf::NvtxRange nvtx_range("psfun_gpu_serial_apply");
   if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   if (n < 1 || lda < n) return PSFUN_ERR_FROM_SUBROUTINE;
   DevBuf da, dx, dy;
@@ -478,6 +529,7 @@ __global__ void k_csr_to_dense(CsrDev A, double* D) {
 extern "C" {
 
 int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, const double* x) {
+  psf::NvtxRange nvtx_range("psfun_gpu_serial_apply_sparse");
   if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;
   if (n < 1 || n > 8192) return PSFUN_ERR_FROM_SUBROUTINE;
@@ -551,6 +603,7 @@ int psfun_gpu_krylov_precinit(psfun_krylov* meth, const char* ptype) {
   return PSFUN_SUCCESS;
 }
 int psfun_gpu_krylov_precbuild(psfun_krylov* meth, psfun_csr* a) {
+  psf::NvtxRange nvtx_range("psfun_gpu_krylov_precbuild");
   if (!meth || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (meth->prec == 1) PSF_TRY(psf::csr_build_diag_inv(a));
   return PSFUN_SUCCESS;
@@ -576,6 +629,7 @@ int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val) 
 int psfun_gpu_d_krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y,
                                     const double* x, double eps, int itmax, int itrace, int istop, int* iter,
                                     double* err, double* res, int res_cap, int* res_len) {
+  psf::NvtxRange nvtx_range("psfun_gpu_d_krylov_apply_device");
   if (!meth || !fun || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   return krylov_apply_device(meth, fun, a, y, x, eps, itmax, itrace, istop, iter, err, res, res_cap, res_len);
 }
@@ -583,6 +637,7 @@ int psfun_gpu_d_krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun
 int psfun_gpu_d_krylov_apply(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x,
                              double eps, int itmax, int itrace, int istop, int* iter, double* err, double* res,
                              int res_cap, int* res_len) {
+  psf::NvtxRange nvtx_range("psfun_gpu_d_krylov_apply");
   if (!meth || !fun || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;

@@ -326,6 +326,7 @@ int csr_build_diag_inv(psfun_csr* a) {
   double* dtmp = nullptr;
   PSF_CUDA(cudaMalloc(&inv, sizeof(double) * (n + 1)));
   if (cudaMalloc(&dtmp, sizeof(double) * (n + 1)) != cudaSuccess) {
+    (void)cudaGetLastError();
     cudaFree(inv);
     set_last_error("csr_build_diag_inv: cudaMalloc failed");
     return PSFUN_ERR_ALLOC_DEALLOC;
@@ -338,6 +339,7 @@ int csr_build_diag_inv(psfun_csr* a) {
   }
   cudaFree(dtmp);
   if (e != cudaSuccess) {
+    (void)cudaGetLastError();
     cudaFree(inv);
     set_last_error(std::string("csr_build_diag_inv: ") + cudaGetErrorString(e));
     return PSFUN_ERR_CUDA;
@@ -441,6 +443,7 @@ static int parse_prec(const char* ptype, int* prec) {
 
 int psfun_gpu_dcg_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
                          double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err) {
+  psf::NvtxRange nvtx_range("psfun_gpu_dcg_device");
   (void)method;  // only CG exists; unknown methods default to CG (psfun_krylov_mod.f90:120-125)
   if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   int prec = 0;
@@ -450,6 +453,7 @@ int psfun_gpu_dcg_device(const char* method, psfun_csr* a, const char* ptype, co
 
 int psfun_gpu_dcg(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta, double zeta,
                   double* x, double eps, int itmax, int istop, int* iter, double* err) {
+  psf::NvtxRange nvtx_range("psfun_gpu_dcg");
   if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (!b || !x) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/psfun_gb300.h"
+#include <nvtx3/nvToolsExt.h>
 #include "dense.cuh"
 #include "spmv.cuh"
 
@@ -19,11 +20,15 @@ void count_launch(int n = 1);
 long long launch_count();
 int sm_count();
 
-// CUDA call -> status code, recording the message.
+// CUDA call -> status code, recording the message.  A failed call's error is
+// also taken off the runtime's last-error slot (cudaGetLastError), so that a
+// recoverable failure (an allocation the device cannot satisfy) is not
+// reported again by the next call's launch checks.
 #define PSF_CUDA(call)                                                          \
   do {                                                                          \
     cudaError_t e_ = (call);                                                    \
     if (e_ != cudaSuccess) {                                                    \
+      (void)cudaGetLastError();                                                 \
       ::psf::set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
       return PSFUN_ERR_CUDA;                                                    \
     }                                                                           \
@@ -43,6 +48,15 @@ struct DevBuf {
   void release();
   template <class T>
   T* as() const { return static_cast<T*>(ptr); }
+};
+
+// An NVTX range over one C-ABI call (named after the entry point), for
+// profilers; without a tool attached it costs a null check.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // Control block of one Krylov solve, in device memory.

@@ -22,6 +22,7 @@
 // estimate (istop = 1) is a one-CTA kernel in the same stream.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -875,7 +876,6 @@ static int mgs_grid() {
 int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x, double eps,
                         int itmax, int itrace, int istop, int* iter, double* err, double* res, int res_cap,
                         int* res_len) {
-  (void)itrace;
   char kn[32];
   upper_trim(meth->kname, kn, sizeof kn);
   int arnoldi, sai = 0;
@@ -1142,6 +1142,26 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     if (res_len) *res_len = cnt;
   } else if (res_len) {
     *res_len = 0;
+  }
+  if (itrace > 0) {
+    // The convergence log the reference writes through log_header, log_conv
+    // every itrace iterations and log_end (psfun_d_arnoldi.f90:181, 255-256,
+    // 317), method name KNAME+FNAME+VARIANT (:93).  The solve runs on the
+    // device without host round trips, so the lines are written after it from
+    // the recorded estimates rs(2:itx).
+    auto trimmed = [](const char* v) {
+      std::string t(v);
+      while (!t.empty() && t.back() == ' ') t.pop_back();
+      return t;
+    };
+    const std::string mname = std::string(kn) + "+" + trimmed(fun->fname) + "+" + trimmed(fun->variant);
+    std::printf("%s: %9s %16s %16s\n", mname.c_str(), "iteration", "error estimate", "tolerance");
+    if (istop == 1)
+      for (int l = 1; l < hc.itx; ++l)
+        if (l % itrace == 0) std::printf("%s: %9d %16.8e %16.8e\n", mname.c_str(), l, hrs[l], eps);
+    std::printf("%s: %s after %d iterations, error estimate %.8e\n", mname.c_str(),
+                hc.conv ? "converged" : "stopped", hc.itx, hc.derr);
+    std::fflush(stdout);
   }
   return PSFUN_SUCCESS;
 }
@@ -1775,17 +1795,20 @@ extern "C" {
 int psfun_gpu_z_quadrature_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta,
                                         double sign, const double* x, double* y, double eps, int itmax, int* iter,
                                         double* err) {
+  psf::NvtxRange nvtx_range("psfun_gpu_z_quadrature_apply_device");
   return psf::quad_apply_device(a, N, xi, c, eta, sign, x, y, eps, itmax, iter, err);
 }
 
 int psfun_gpu_d_expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps,
                                     int itmax, int recompute, double* y, double* grad_x, double* grad_t,
                                     double* grad_vals, int* iters) {
+  psf::NvtxRange nvtx_range("psfun_gpu_d_expm_adjoint_device");
   return psf::expm_adjoint_device(a, t, x, g, nquad, eps, itmax, recompute, y, grad_x, grad_t, grad_vals, iters);
 }
 
 int psfun_gpu_z_quadrature_apply(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                                  const double* x, double* y, double eps, int itmax, int* iter, double* err) {
+  psf::NvtxRange nvtx_range("psfun_gpu_z_quadrature_apply");
   if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;

@@ -230,3 +230,30 @@ def test_arnoldi_both_mgs_paths(lib, orc, side):
     o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", -0.01, A, x, 1e-12, itmax=12, istop=2)
     assert g.info == 0 and o["info"] == 0 and g.iter == o["iter"]
     assert rel(g.y, o["y"]) <= TOL
+
+
+def test_itrace_log(lib, capfd):
+    """itrace > 0: the convergence log (header, every itrace-th estimate, end
+    line) under the reference's method name KNAME+FNAME+VARIANT."""
+    import psfun_gb300 as pg
+    A = -matrices.laplacian_2d(30)
+    x = matrices.unit(np.random.default_rng(4).standard_normal(A.shape[0]))
+    fun = pg.PsfunDSerial()
+    assert fun.set("VARIANT", "GENPADE") == 0
+    meth = pg.PsfunDKrylov()
+    assert meth.set("KNAME", "arnoldi") == 0
+    capfd.readouterr()
+    r = meth.apply(fun, pg.CsrMatrix.from_scipy(A), x, 1e-10, itmax=80, itrace=3, istop=1)
+    out = capfd.readouterr().out.splitlines()
+    assert r.info == 0
+    lines = [l for l in out if l.startswith("ARNOLDI+EXP+GENPADE:")]
+    assert "error estimate" in lines[0]
+    its = [int(l.split()[1]) for l in lines[1:-1]]
+    assert its == list(range(3, r.iter, 3))
+    for l in lines[1:-1]:
+        it = int(l.split()[1])
+        assert float(l.split()[2]) == pytest.approx(r.res[it], rel=1e-7)
+    assert f"converged after {r.iter} iterations" in lines[-1]
+    # itrace 0: silent
+    meth.apply(fun, pg.CsrMatrix.from_scipy(A), x, 1e-10, itmax=80, istop=1)
+    assert "ARNOLDI+" not in capfd.readouterr().out
