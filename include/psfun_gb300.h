@@ -193,6 +193,19 @@ int psfun_gpu_dcg(const char* method, psfun_csr* a, const char* ptype, const dou
                   double* x, double eps, int itmax, int istop, int* iter, double* err);
 int psfun_gpu_dcg_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
                          double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err);
+/* The same with the reference's optional itrace and cond (psfun_dcg.F90:146-148):
+ * itrace > 0 writes the stopping-test value of every itrace-th iteration to
+ * stdout after the solve; cond (may be NULL) receives eig_max / eig_min of
+ * the CG tridiagonal (td = 1/alpha + beta/alpha_old, tu = sqrt(beta)/alpha_old,
+ * :312-320, :336-347), the reference's estimate of the preconditioned
+ * operator's condition number (eigenvalues by Sturm bisection here, DSTEBZ
+ * there), 0 when no iteration formed alpha. */
+int psfun_gpu_dcg_ex(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
+                     double zeta, double* x, double eps, int itmax, int itrace, int istop, int* iter, double* err,
+                     double* cond);
+int psfun_gpu_dcg_ex_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
+                            double zeta, double* x, double eps, int itmax, int itrace, int istop, int* iter,
+                            double* err, double* cond);
 
 /* ------------------------------------------------------------------------ */
 /* Quadrature rules (host side): hhtmethod1 and the elliptic utilities        */

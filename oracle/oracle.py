@@ -77,6 +77,8 @@ def lib():
                                      C.POINTER(C.c_double), _dp, C.c_int, C.POINTER(C.c_int)]
         L.orc_dcg.argtypes = [C.POINTER(OrcCsr), _dp, _dp, C.c_double, C.c_double, _dp, C.c_double, C.c_int,
                               C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_dcg_hist.argtypes = [C.POINTER(OrcCsr), _dp, _dp, C.c_double, C.c_double, _dp, C.c_double, C.c_int,
+                                   C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
         L.orc_horner.argtypes = [_dp, C.c_int, C.c_double]
         L.orc_horner.restype = C.c_double
         L.orc_ellipkkp.argtypes = [C.c_double, _dp]
@@ -199,6 +201,32 @@ def dcg(A: Csr, b, eta, zeta, x0=None, eps=1e-7, itmax=1000, istop=2, prec="NONE
     info = lib().orc_dcg(C.byref(A.s), _p(dinv) if dinv is not None else None, _p(b), eta, zeta, _p(x), eps,
                          itmax, istop, C.byref(it), C.byref(err))
     return dict(x=x, info=info, iter=it.value, err=err.value)
+
+
+def dcg_cond(A: Csr, b, eta, zeta, x0=None, eps=1e-7, itmax=1000, istop=2, prec="NONE"):
+    """dcg with the reference's optional cond (psfun_dcg.F90:237-246, 312-320,
+    336-353): the CG tridiagonal td/tu, its extreme eigenvalues by LAPACK's
+    symmetric tridiagonal solver (scipy), cond = eig(max) / eig(min); and the
+    per-iteration errnum/errden."""
+    import scipy.linalg as sla
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+    dinv = diag_inv(A) if prec.upper() == "DIAG" else None
+    it = C.c_int(0)
+    err = C.c_double(0.0)
+    nt = C.c_int(0)
+    td = np.zeros(max(itmax, 1))
+    tu = np.zeros(max(itmax, 1))
+    eh = np.zeros(max(itmax, 1))
+    info = lib().orc_dcg_hist(C.byref(A.s), _p(dinv) if dinv is not None else None, _p(b), eta, zeta, _p(x), eps,
+                              itmax, istop, C.byref(it), C.byref(err), _p(td), _p(tu), C.byref(nt), _p(eh))
+    m = nt.value
+    cond = 0.0
+    if m > 0:
+        ev = sla.eigvalsh_tridiagonal(td[:m], tu[:m - 1]) if m > 1 else td[:1]
+        cond = float(ev[-1] / ev[0])
+    return dict(x=x, info=info, iter=it.value, err=err.value, cond=cond, td=td[:m].copy(), tu=tu[:max(m - 1, 0)].copy(),
+                errh=eh[: it.value].copy())
 
 
 def spmv(A: Csr, x, alpha=1.0, beta=0.0, y=None):

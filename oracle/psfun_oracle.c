@@ -781,8 +781,24 @@ done:
 /* and check_conv also returning true once itx >= itmax.                     */
 /* prec_diag_inv == NULL is the NONE preconditioner; otherwise z = d .* r.   */
 /* ------------------------------------------------------------------------ */
+/* orc_dcg_hist also returns what the optional argument cond of the reference
+ * needs (:237-246, :312-320): the tridiagonal td(1:nt), tu(1:nt-1) built from
+ * alpha and beta (td = 1/alpha + beta/alpha_old, tu = sqrt(beta)/alpha_old,
+ * the variables keeping their values across restarts), and errnum/errden of
+ * every iteration's stopping test (errh, NaN where none ran).  td, tu, errh
+ * (capacity itmax) and nt may be NULL. */
+int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
+                 double* x, double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu,
+                 int* nt, double* errh);
+
 int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
             double* x, double eps, int itmax, int istop, int* iter, double* err) {
+  return orc_dcg_hist(A, prec_diag_inv, b, eta, zeta, x, eps, itmax, istop, iter, err, NULL, NULL, NULL, NULL);
+}
+
+int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
+                 double* x, double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu,
+                 int* nt, double* errh) {
   if (istop < 1 || istop > 2) return ORC_ERR_INVALID_ISTOP;
   if (!b || !x) return ORC_ERR_INVALID_VECT_STATE;
   int64_t n = A->n;
@@ -801,8 +817,10 @@ int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, doub
   double bni = vamax(n, b), bn2 = vnrm2(n, b);
   int itx = 0;
   double errnum = 0.0, errden = 1.0;
-  double alpha = 0.0, beta = 0.0, rho = 0.0, rho_old, sigma;
-  int conv = 0;
+  double alpha = 0.0, beta = 0.0, rho = 0.0, rho_old, sigma, alpha_old;
+  int conv = 0, istebz = 0;
+  if (errh)
+    for (int j = 0; j < itmax; ++j) errh[j] = NAN;
   while (!conv) { /* restart :252 */
     if (itx >= itmax) break;
     int it = 0;
@@ -831,7 +849,17 @@ int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, doub
       vaxpby(n, zeta, p, 1.0, q);
       sigma = vdot(n, p, q);
       if (sigma == 0.0) break;
+      alpha_old = alpha;
       alpha = rho / sigma;
+      if (td) { /* :312-320 */
+        istebz = istebz + 1;
+        if (istebz == 1) {
+          td[0] = 1.0 / alpha;
+        } else {
+          td[istebz - 1] = 1.0 / alpha + beta / alpha_old;
+          tu[istebz - 2] = sqrt(beta) / alpha_old;
+        }
+      }
       vaxpby(n, alpha, p, 1.0, x);
       vaxpby(n, -alpha, q, 1.0, r);
       if (istop == 1) {
@@ -842,9 +870,11 @@ int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, doub
         errden = bn2;
       }
       int ok = (errden == 0.0) ? (errnum <= eps) : (errnum <= eps * errden);
+      if (errh) errh[itx - 1] = log_end_err(errnum, errden);
       if (ok || itx >= itmax) { conv = 1; break; }
     }
   }
+  if (nt) *nt = istebz;
   if (iter) *iter = itx;
   if (err) *err = log_end_err(errnum, errden);
   free(p); free(q); free(r); free(z);

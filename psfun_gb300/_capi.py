@@ -68,6 +68,10 @@ PROTOS = {
                                 C.c_int, C.POINTER(C.c_int), dp]),
     "psfun_gpu_dcg_device": (C.c_int, [C.c_char_p, vp, C.c_char_p, vp, C.c_double, C.c_double, vp, C.c_double,
                                        C.c_int, C.c_int, C.POINTER(C.c_int), dp]),
+    "psfun_gpu_dcg_ex": (C.c_int, [C.c_char_p, vp, C.c_char_p, dp, C.c_double, C.c_double, dp, C.c_double, C.c_int,
+                                   C.c_int, C.c_int, C.POINTER(C.c_int), dp, dp]),
+    "psfun_gpu_dcg_ex_device": (C.c_int, [C.c_char_p, vp, C.c_char_p, vp, C.c_double, C.c_double, vp, C.c_double,
+                                          C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), dp, dp]),
     "psfun_gpu_hhtmethod1": (C.c_int, [ZFUN, C.c_void_p, C.c_int, dp, dp, dp, dp, dp]),
     "psfun_gpu_ellipkkp": (C.c_int, [C.c_double, dp]),
     "psfun_gpu_d_ellipj": (C.c_int, [C.c_double, C.c_double, dp, dp, dp]),

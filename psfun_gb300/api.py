@@ -386,23 +386,29 @@ def expm_adjoint(a: CsrMatrix, t: float, x, g=None, nquad: int = 32, eps: float 
 
 # ---------------------------------------------------------------------------
 def psb_krylov(method: str, a: CsrMatrix, prec: str, b, eta: float, zeta: float, x, eps: float,
-               itmax: int = 1000, istop: int = 2):
-    """psb_krylov(method,a,prec,b,eta,zeta,x,eps,desc_a,info,itmax,iter,err,...)
+               itmax: int = 1000, istop: int = 2, itrace: int = 0, cond: bool = False):
+    """psb_krylov(method,a,prec,b,eta,zeta,x,eps,desc_a,info,itmax,iter,err,itrace,istop,cond)
     for (eta A + zeta I) x = b (psfun_dkrylov_vect).  prec is 'NONE' or 'DIAG'.
-    x is the initial guess.  Returns (x, info, iter, err)."""
+    x is the initial guess.  Returns (x, info, iter, err), and cond as a fifth
+    element when cond=True (the reference's optional condition estimate)."""
     it = C.c_int(0)
     err = C.c_double(0.0)
+    cv = C.c_double(0.0)
+    pc = C.byref(cv) if cond else None
     if _is_device(b):
         _sync_stream()
-        info = _lib().psfun_gpu_dcg_device(method.encode(), a.handle, prec.encode(), C.c_void_p(b.data_ptr()),
-                                           eta, zeta, C.c_void_p(x.data_ptr()), eps, itmax, istop, C.byref(it),
-                                           C.byref(err))
-        return x, info, it.value, err.value
-    bb = np.ascontiguousarray(b, dtype=np.float64)
-    xx = np.ascontiguousarray(x, dtype=np.float64).copy()
-    info = _lib().psfun_gpu_dcg(method.encode(), a.handle, prec.encode(), _dp(bb), eta, zeta, _dp(xx), eps,
-                                itmax, istop, C.byref(it), C.byref(err))
-    return xx, info, it.value, err.value
+        info = _lib().psfun_gpu_dcg_ex_device(method.encode(), a.handle, prec.encode(), C.c_void_p(b.data_ptr()),
+                                              eta, zeta, C.c_void_p(x.data_ptr()), eps, itmax, itrace, istop,
+                                              C.byref(it), C.byref(err), pc)
+        out = x
+    else:
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        out = np.ascontiguousarray(x, dtype=np.float64).copy()
+        info = _lib().psfun_gpu_dcg_ex(method.encode(), a.handle, prec.encode(), _dp(bb), eta, zeta, _dp(out), eps,
+                                       itmax, itrace, istop, C.byref(it), C.byref(err), pc)
+    if cond:
+        return out, info, it.value, err.value, cv.value
+    return out, info, it.value, err.value
 
 
 # ---------------------------------------------------------------------------

@@ -11,7 +11,9 @@
 //
 // The restart and all iterations run in one persistent cooperative kernel
 // (k_cg_persist below); the host only relaunches it after a breakdown.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -39,6 +41,10 @@ struct CgState {
   double* part;   // partial sums (3 per block)
   CgCtrl* c;
   volatile int* host_flag;
+  // Optional per-iteration record (3 doubles per iteration, NaN where none
+  // was formed): alpha, the beta it follows, errnum / errden.  For the
+  // reference's optional outputs cond and the itrace log.
+  double* hist;
 };
 
 constexpr int kCgThreads = 256;
@@ -155,6 +161,8 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
   double rho = sm.scal[0], beta = 0.0;
   int itx = c->itx;  // iterations before this launch
   bool first = true;
+  // the reference's beta variable keeps its value across restarts (:281)
+  double beta_rec = (st.hist && bid == 0 && threadIdx.x == 0) ? c->beta : 0.0;
   for (;;) {
     // ---- p = z (it == 1) or p = z + beta p (:267-285); four rows per thread
     // in flight (loads of a group before its arithmetic)
@@ -204,6 +212,10 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
             if (st.host_flag) st.host_flag[2] = 1;
           } else {
             c->alpha = sm.scal[1];
+            if (st.hist) {
+              st.hist[3 * (size_t)(itx - 1)] = sm.scal[1];
+              st.hist[3 * (size_t)(itx - 1) + 1] = beta_rec;
+            }
           }
         }
       }
@@ -290,6 +302,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
         if (bid == 0) {
           c->errnum = errnum;
           c->errden = errden;
+          if (st.hist) st.hist[3 * (size_t)(itx - 1) + 2] = (errden > 0.0) ? errnum / errden : errnum;
           if (state == 1) {
             c->done = 1;
             if (st.host_flag) st.host_flag[0] = 1;
@@ -312,6 +325,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
     const int state = (int)sm.scal[3];
     if (state != 0) { drain(); return; }
     beta = sm.scal[4];
+    beta_rec = beta;
     rho = sm.scal[0];
   }
 }
@@ -348,8 +362,48 @@ int csr_build_diag_inv(psfun_csr* a) {
   return PSFUN_SUCCESS;
 }
 
+// Smallest and largest eigenvalue of the symmetric tridiagonal matrix with
+// diagonal d and off-diagonal e, by bisection on Sturm counts (the number of
+// negative pivots of the LDL^T factorisation of T - x I equals the number of
+// eigenvalues below x; Barth, Martin and Wilkinson, Numer. Math. 9 (1967)),
+// from Gershgorin bounds to adjacent doubles.
+static void tridiag_extremes(const std::vector<double>& d, const std::vector<double>& e, double* lmin,
+                             double* lmax) {
+  const int m = (int)d.size();
+  double lo = d[0], hi = d[0], emax = 0.0;
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < m ? fabs(e[i]) : 0.0);
+    lo = std::min(lo, d[i] - r);
+    hi = std::max(hi, d[i] + r);
+    if (i + 1 < m) emax = std::max(emax, fabs(e[i]));
+  }
+  const double pivmin = std::max(1e-300, 2.2e-308 * emax * emax);
+  auto below = [&](double x) {  // eigenvalues < x
+    int cnt = 0;
+    double q = 1.0;
+    for (int i = 0; i < m; ++i) {
+      q = (d[i] - x) - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+      if (fabs(q) < pivmin) q = -pivmin;
+      if (q < 0.0) ++cnt;
+    }
+    return cnt;
+  };
+  auto smallest_with = [&](int k) {  // smallest x with below(x) >= k
+    double a = lo - 1e-12 * (fabs(lo) + 1.0), b = hi + 1e-12 * (fabs(hi) + 1.0);
+    for (int it = 0; it < 200; ++it) {
+      const double mid = 0.5 * (a + b);
+      if (mid <= a || mid >= b) break;
+      if (below(mid) >= k) b = mid;
+      else a = mid;
+    }
+    return 0.5 * (a + b);
+  };
+  *lmin = smallest_with(1);
+  *lmax = smallest_with(m);
+}
+
 int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
-              int istop, int* iter, double* err) {
+              int istop, int* iter, double* err, int itrace, double* cond) {
   if (istop < 1 || istop > 2) return PSFUN_ERR_INVALID_ISTOP;
   if (!b || !x) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;
@@ -377,6 +431,13 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   st.dinv = (prec == 1) ? a->diag_inv : nullptr;
   st.part = partb.as<double>();
   st.c = ctrlb.as<CgCtrl>();
+  st.hist = nullptr;
+  static DevBuf histb;
+  if ((cond || itrace > 0) && itmax > 0) {
+    PSF_TRY(histb.ensure(sizeof(double) * 3 * (size_t)itmax));
+    PSF_CUDA(cudaMemsetAsync(histb.ptr, 0xff, sizeof(double) * 3 * (size_t)itmax, s));  // NaN
+    st.hist = histb.as<double>();
+  }
   static volatile int* hflag = nullptr;
   static int* dflag = nullptr;
   if (!hflag) {
@@ -424,7 +485,49 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   PSF_CUDA(cudaMemcpyAsync(&hc, st.c, sizeof hc, cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
   if (iter) *iter = hc.itx;
-  if (err) *err = (hc.errden > 0.0) ? hc.errnum / hc.errden : hc.errnum;
+  const double derr = (hc.errden > 0.0) ? hc.errnum / hc.errden : hc.errnum;
+  if (err) *err = derr;
+  if (st.hist) {
+    const int nit = std::min(hc.itx, itmax);
+    std::vector<double> h(3 * (size_t)std::max(nit, 1));
+    if (nit > 0)
+      PSF_CUDA(cudaMemcpy(h.data(), st.hist, sizeof(double) * 3 * (size_t)nit, cudaMemcpyDeviceToHost));
+    if (cond) {
+      // the CG tridiagonal of the reference's optional cond (:312-320):
+      // td = 1/alpha (+ beta/alpha_old), tu = sqrt(beta)/alpha_old over the
+      // iterations that formed alpha; cond = eig(max)/eig(min) (:336-347)
+      std::vector<double> td, tu;
+      double alpha_old = 0.0;
+      for (int j = 0; j < nit; ++j) {
+        const double al = h[3 * (size_t)j], be = h[3 * (size_t)j + 1];
+        if (std::isnan(al)) continue;
+        if (td.empty()) {
+          td.push_back(1.0 / al);
+        } else {
+          td.push_back(1.0 / al + be / alpha_old);
+          tu.push_back(sqrt(be) / alpha_old);
+        }
+        alpha_old = al;
+      }
+      *cond = 0.0;
+      if (!td.empty()) {
+        double lmin = td[0], lmax = td[0];
+        if (td.size() > 1) tridiag_extremes(td, tu, &lmin, &lmax);
+        *cond = lmax / lmin;
+      }
+    }
+    if (itrace > 0) {
+      // the convergence log psb_check_conv writes every itrace iterations
+      // (written after the solve, from the recorded stopping-test values)
+      std::printf("CG: %9s %16s %16s\n", "iteration", "error estimate", "tolerance");
+      for (int j = 0; j < nit; ++j)
+        if ((j + 1) % itrace == 0 && !std::isnan(h[3 * (size_t)j + 2]))
+          std::printf("CG: %9d %16.8e %16.8e\n", j + 1, h[3 * (size_t)j + 2], eps);
+      std::printf("CG: %s after %d iterations, error estimate %.8e\n", hc.done && derr <= eps ? "converged" : "stopped",
+                  hc.itx, derr);
+      std::fflush(stdout);
+    }
+  }
   return PSFUN_SUCCESS;
 }
 
@@ -441,37 +544,53 @@ static int parse_prec(const char* ptype, int* prec) {
   return 0;
 }
 
-int psfun_gpu_dcg_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
-                         double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err) {
-  psf::NvtxRange nvtx_range("psfun_gpu_dcg_device");
+int psfun_gpu_dcg_ex_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
+                            double zeta, double* x, double eps, int itmax, int itrace, int istop, int* iter,
+                            double* err, double* cond) {
+  psf::NvtxRange nvtx_range("psfun_gpu_dcg_ex_device");
   (void)method;  // only CG exists; unknown methods default to CG (psfun_krylov_mod.f90:120-125)
   if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   int prec = 0;
   if (!parse_prec(ptype, &prec)) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
-  return psf::cg_device(a, prec, b, eta, zeta, x, eps, itmax, istop, iter, err);
+  return psf::cg_device(a, prec, b, eta, zeta, x, eps, itmax, istop, iter, err, itrace, cond);
+}
+
+int psfun_gpu_dcg_device(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
+                         double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err) {
+  return psfun_gpu_dcg_ex_device(method, a, ptype, b, eta, zeta, x, eps, itmax, 0, istop, iter, err, nullptr);
+}
+
+int psfun_gpu_dcg_ex(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta,
+                     double zeta, double* x, double eps, int itmax, int itrace, int istop, int* iter, double* err,
+                     double* cond) {
+  psf::NvtxRange nvtx_range("psfun_gpu_dcg_ex");
+  if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (!b || !x) return PSFUN_ERR_INVALID_VECT_STATE;
+  const int64_t n = a->n;
+  struct Bufs {  // device copies of b and x, freed on every return
+    psf::DevBuf db, dx;
+    ~Bufs() {
+      db.release();
+      dx.release();
+    }
+  } bf;
+  PSF_TRY(bf.db.ensure(sizeof(double) * (n + 1)));
+  PSF_TRY(bf.dx.ensure(sizeof(double) * (n + 1)));
+  cudaStream_t s = psf::stream();
+  PSF_CUDA(cudaMemcpyAsync(bf.db.ptr, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  PSF_CUDA(cudaMemcpyAsync(bf.dx.ptr, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  const int rc = psfun_gpu_dcg_ex_device(method, a, ptype, bf.db.as<double>(), eta, zeta, bf.dx.as<double>(), eps,
+                                         itmax, itrace, istop, iter, err, cond);
+  if (rc == PSFUN_SUCCESS) {
+    PSF_CUDA(cudaMemcpyAsync(x, bf.dx.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    PSF_CUDA(cudaStreamSynchronize(s));
+  }
+  return rc;
 }
 
 int psfun_gpu_dcg(const char* method, psfun_csr* a, const char* ptype, const double* b, double eta, double zeta,
                   double* x, double eps, int itmax, int istop, int* iter, double* err) {
-  psf::NvtxRange nvtx_range("psfun_gpu_dcg");
-  if (!a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
-  if (!b || !x) return PSFUN_ERR_INVALID_VECT_STATE;
-  const int64_t n = a->n;
-  psf::DevBuf db, dx;
-  PSF_TRY(db.ensure(sizeof(double) * (n + 1)));
-  PSF_TRY(dx.ensure(sizeof(double) * (n + 1)));
-  cudaStream_t s = psf::stream();
-  PSF_CUDA(cudaMemcpyAsync(db.ptr, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  PSF_CUDA(cudaMemcpyAsync(dx.ptr, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  int rc = psfun_gpu_dcg_device(method, a, ptype, db.as<double>(), eta, zeta, dx.as<double>(), eps, itmax, istop,
-                                iter, err);
-  if (rc == PSFUN_SUCCESS) {
-    PSF_CUDA(cudaMemcpyAsync(x, dx.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    PSF_CUDA(cudaStreamSynchronize(s));
-  }
-  db.release();
-  dx.release();
-  return rc;
+  return psfun_gpu_dcg_ex(method, a, ptype, b, eta, zeta, x, eps, itmax, 0, istop, iter, err, nullptr);
 }
 
 }  // extern "C"

@@ -145,7 +145,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
 int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev, const double* x_dev);
 int csr_build_diag_inv(psfun_csr* a);
 int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
-              int istop, int* iter, double* err);
+              int istop, int* iter, double* err, int itrace = 0, double* cond = nullptr);
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                       const double* x, double* y, double eps, int itmax, int* iter, double* err);
 int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y);

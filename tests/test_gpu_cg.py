@@ -51,3 +51,35 @@ def test_cg_errors(lib):
     b = np.ones(64)
     assert pg.psb_krylov("CG", a, "NONE", b, 1.0, 0.0, np.zeros(64), 1e-8, istop=3)[1] == 5001
     assert pg.psb_krylov("CG", a, "ILU99", b, 1.0, 0.0, np.zeros(64), 1e-8)[1] == 111
+
+
+@pytest.mark.parametrize("prec", ["NONE", "DIAG"])
+def test_cg_cond_vs_oracle(lib, orc, prec):
+    """The optional cond: the GPU's CG tridiagonal eigenvalue ratio against the
+    oracle's (LAPACK's tridiagonal solver on the oracle's alphas and betas)."""
+    import psfun_gb300 as pg
+    A = matrices.laplacian_2d(40)
+    b = np.random.default_rng(5).standard_normal(A.shape[0])
+    x, info, it, err, cond = pg.psb_krylov("CG", pg.CsrMatrix.from_scipy(A), prec, b, 1.0, 0.25,
+                                           np.zeros_like(b), 1e-11, itmax=3000, istop=2, cond=True)
+    o = orc.dcg_cond(orc.Csr.from_scipy(A), b, 1.0, 0.25, eps=1e-11, itmax=3000, istop=2, prec=prec)
+    assert info == 0 and abs(it - o["iter"]) <= 1
+    assert cond == pytest.approx(o["cond"], rel=1e-8)
+    # without cond the solution is the same
+    x2, info2, it2, err2 = pg.psb_krylov("CG", pg.CsrMatrix.from_scipy(A), prec, b, 1.0, 0.25, np.zeros_like(b),
+                                         1e-11, itmax=3000, istop=2)
+    assert np.array_equal(x, x2) and it == it2
+
+
+def test_cg_itrace_log(lib, capfd):
+    import psfun_gb300 as pg
+    A = matrices.laplacian_2d(30)
+    b = np.ones(A.shape[0])
+    capfd.readouterr()
+    x, info, it, err = pg.psb_krylov("CG", pg.CsrMatrix.from_scipy(A), "DIAG", b, 1.0, 0.5, np.zeros_like(b), 1e-10,
+                                     itmax=500, istop=2, itrace=4)
+    lines = [l for l in capfd.readouterr().out.splitlines() if l.startswith("CG:")]
+    assert info == 0
+    its = [int(l.split()[1]) for l in lines[1:-1]]
+    assert its == list(range(4, it + 1, 4))
+    assert f"converged after {it} iterations" in lines[-1]

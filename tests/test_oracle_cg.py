@@ -33,3 +33,21 @@ def test_cg_itmax_stops(orc):
     b = np.ones(A.shape[0])
     r = orc.dcg(orc.Csr.from_scipy(A), b, 1.0, 0.0, eps=1e-30, itmax=7, istop=2)
     assert r["iter"] == 7
+
+
+@pytest.mark.parametrize("prec", ["NONE", "DIAG"])
+def test_cg_cond_matches_dense_operator(orc, prec):
+    """cond (psfun_dcg.F90:312-347): eig_max/eig_min of the CG tridiagonal.
+    Run to convergence on a small SPD system, its extreme Ritz values are the
+    extreme eigenvalues of the preconditioned operator D^{1/2}(eta A + zeta I)D^{1/2}."""
+    A = matrices.laplacian_2d(12)
+    b = np.random.default_rng(0).standard_normal(A.shape[0])
+    r = orc.dcg_cond(orc.Csr.from_scipy(A), b, 1.0, 0.5, eps=1e-12, itmax=500, istop=2, prec=prec)
+    assert r["info"] == 0 and len(r["td"]) == r["iter"]
+    Ad = A.toarray()
+    M = Ad + 0.5 * np.eye(A.shape[0])
+    d = 1.0 / np.sqrt(np.diag(Ad)) if prec == "DIAG" else np.ones(A.shape[0])
+    ev = np.linalg.eigvalsh(d[:, None] * M * d[None, :])
+    assert r["cond"] == pytest.approx(ev[-1] / ev[0], rel=1e-10)
+    # the per-iteration stopping values end at the returned err
+    assert r["errh"][-1] == r["err"] and np.all(np.diff(np.log(r["errh"])) < 2.0)
