@@ -352,6 +352,66 @@ def bench_adjoint(torch, pg, reps: int = 3):
             "cost_ratio_vs_forward": t_all / t_fwd, "krylov_dims": list(out2["iters"])}
 
 
+def bench_serial(torch, pg, m: int = 80, reps: int = 20):
+    """Dense y = f(H) x of the serial module (psfun_d_serial_apply_array) through
+    the host C-ABI call, every variant, on an m x m symmetric negative
+    definite H (seed 6, ||H||_2 ~ 10, the size of the Lanczos T of the main
+    workload): microseconds per call, copies and the one-block kernel
+    included."""
+    rng = np.random.default_rng(6)
+    B = rng.standard_normal((m, m))
+    H = -(B @ B.T / m + np.eye(m)) * 2.5
+    x = rng.standard_normal(m)
+    out = {"workload": f"dense {m}x{m} symmetric negative definite H, y = f(H)x per call (host arrays)"}
+    for fname, variant in [("EXP", "GENPADE"), ("EXP", "SASQ"), ("EXP", "TAYLOR"), ("EXP", "CHBHES"),
+                           ("EXP", "CHBGEN"), ("EXP", "CHBSYM"), ("PHI", "")]:
+        f = pg.PsfunDSerial()
+        f.set("FNAME", fname)
+        f.set("VARIANT", variant)
+        for _ in range(3):
+            y, info = f.apply(H, x)
+            assert info == 0, (fname, variant, info)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            f.apply(H, x)
+        out[f"{fname}/{variant or 'PHI1'}_us"] = 1e6 * (time.perf_counter() - t0) / reps
+    return out
+
+
+def bench_sai(torch, pg, reps: int = 2):
+    """Shift-and-invert Arnoldi (KNAME 'SAIARNOLDI', psfun_d_saiarnoldi) for
+    y = exp(-A) x on the 3-D 7-point Laplacian 48^3 (unscaled, n = 110,592),
+    tau 0 (the reference shifts only hcomp(1,1), so other shifts do not give
+    f(A)x), inner CG with DIAG to the outer eps 1e-8, istop 1 (the oracle
+    converges in 80 outer steps); the result is compared with the Lanczos
+    solve of the same problem."""
+    from psfun_gb300 import matrices
+    A = -matrices.laplacian_3d(48)
+    n = A.shape[0]
+    x = torch.tensor(matrices.unit(np.random.default_rng(8).standard_normal(n)), device="cuda")
+    a = pg.CsrMatrix.from_scipy(A)
+    fun = pg.PsfunDSerial()
+    fun.set("VARIANT", "GENPADE")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "SAIARNOLDI")
+    meth.set("TAU", 0.0)
+    meth.set("PREC", "DIAG")
+    meth.set("ITMAX", 2000)
+    y = torch.empty_like(x)
+    dt, r = _time_dev(torch, lambda: meth.apply(fun, a, x, 1e-8, itmax=120, istop=1, y=y), reps)
+    assert r.info == 0, r.info
+    lz = pg.PsfunDKrylov()
+    lz.set("KNAME", "LANCZOS")
+    funl = pg.PsfunDSerial()
+    funl.set("VARIANT", "CHBSYM")
+    yl = lz.apply(funl, a, x, 1e-13, itmax=200, istop=1).y
+    rel = float(torch.linalg.norm(y - yl) / torch.linalg.norm(yl))
+    return {"workload": "3-D 7-point Laplacian 48^3 (n=110,592), y=exp(-A)x, SAIARNOLDI tau=0, inner CG+DIAG, "
+                        "eps 1e-8, istop 1",
+            "ms_per_solve": 1e3 * dt, "outer_iterations": int(r.iter), "error_estimate": float(r.err),
+            "rel_diff_vs_lanczos": rel}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -394,7 +454,9 @@ def run_only(name: str) -> int:
           "multishift": lambda: bench_multishift(torch, pg, peak),
           "adjoint": lambda: bench_adjoint(torch, pg),
           "cg": lambda: bench_cg(torch, pg, peak),
-          "batched": lambda: bench_batched(torch, pg)}[name]
+          "batched": lambda: bench_batched(torch, pg),
+          "serial": lambda: bench_serial(torch, pg),
+          "sai": lambda: bench_sai(torch, pg)}[name]
     print(json.dumps({name: fn()}), flush=True)
     return 0
 
@@ -409,7 +471,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batched (64-instance) comparison")
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
-    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched"],
+    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "serial", "sai"],
                     help="run one secondary workload alone and print its result (for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -552,6 +614,7 @@ def main():
         "lanczos_step": {"step_ms": step_ms, "step_algorithmic_bytes": nbytes["step"],
                          "step_GBs": nbytes["step"] / (step_ms * 1e-3) / 1e9,
                          "solve_GBs": (bytes_launch + 8 * n * (M_KRYLOV + 1)) / (ms_per_step * 1e-3) / 1e9},
+        "kernels_ms_per_launch": {nm: (tot / cnt if cnt else None) for nm, (cnt, tot) in prof.items() if cnt},
         "clocks": clk,
         "gpu_launches": int(launches),
         "accuracy": {"rel_diff_m80_vs_converged": rel_conv},
@@ -562,6 +625,8 @@ def main():
         line["multishift"] = bench_multishift(torch, pg, peak)
         line["adjoint"] = bench_adjoint(torch, pg)
         line["cg"] = bench_cg(torch, pg, peak)
+        line["sai"] = bench_sai(torch, pg)
+        line["serial"] = bench_serial(torch, pg)
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_secondary:
         line["batched"] = bench_batched(torch, pg)

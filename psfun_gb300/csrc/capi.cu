@@ -571,6 +571,7 @@ int psfun_gpu_krylov_destroy(psfun_krylov* meth) {
   meth->small.release();
   meth->scratch.release();
   meth->partials.release();
+  meth->dgroup.release();
   meth->ctrl.release();
   meth->xy.release();
   if (meth->graph) cudaGraphExecDestroy(meth->graph);

@@ -42,6 +42,13 @@ struct FunParams {
   int phiorder;
 };
 
+// True when fh_apply_cta evaluates fp with matrix products (Pade, SASQ,
+// Taylor, phi); the CRAM variants solve linear systems instead.
+__host__ __device__ inline bool fh_uses_gemm(const FunParams& fp) {
+  if (fp.fname == FN_PHI) return true;
+  return fp.fname == FN_EXP && (fp.variant == VAR_GENPADE || fp.variant == VAR_SASQ || fp.variant == VAR_TAYLOR);
+}
+
 // Scratch (doubles) needed by fh_apply_cta for an m x m problem.
 __host__ __device__ inline size_t fh_scratch_doubles(int m, int phiorder) {
   size_t M = (size_t)m + (size_t)(phiorder > 0 ? phiorder : 1) + 1;
@@ -50,21 +57,43 @@ __host__ __device__ inline size_t fh_scratch_doubles(int m, int phiorder) {
   return a > b ? a : b;
 }
 
+// A group of co-resident blocks (one cooperative launch) sharing the matrix
+// products of one dense f(H) evaluation: block 0 runs the evaluation and
+// posts each product here; blocks 1..G-1 only compute their share of the
+// posted product (gemm_helper).  In global memory, zeroed by the host before
+// each launch.  All waits are bounded: a wait that gives up sets err, which
+// the kernel reports as DEVERR_TIMEOUT.
+struct GemmGroup {
+  const double* A;
+  const double* B;
+  double* C;
+  int m, lda, ldb, ldc;
+  double alpha;
+  unsigned seq;   // products posted by block 0
+  unsigned done;  // shares finished by the other blocks
+  int stop;       // block 0 has finished
+  int err;
+};
+
 struct DenseSmem {
   double red[32];
   double dv[8];
   int iv[8];
   double coef[64];
+  GemmGroup* grp;  // null: a single block does everything
+  unsigned jobs;   // products posted so far (block 0, thread 0)
 };
 
 // ---- real building blocks --------------------------------------------------
 
-// C = alpha * A * B (m x m).  alpha is folded into B(l,j) and the sum over l
-// runs in order, the operation order of the reference BLAS DGEMM.
-PSF_DEVINL void cta_gemm(int m, double alpha, const double* A, int lda, const double* B, int ldb, double* C,
-                         int ldc) {
+// Tasks [t0, t1) of C = alpha * A * B (m x m): task t is the 4-row strip
+// t mod nrb of column t / nrb.  alpha is folded into B(l,j) and the sum over
+// l runs in order, the operation order of the reference BLAS DGEMM, so every
+// entry is the same whichever block computes it.
+PSF_DEVINL void gemm_tasks(int m, double alpha, const double* A, int lda, const double* B, int ldb, double* C,
+                           int ldc, int t0, int t1) {
   const int nrb = (m + 3) >> 2;
-  for (int task = threadIdx.x; task < nrb * m; task += blockDim.x) {
+  for (int task = t0 + (int)threadIdx.x; task < t1; task += blockDim.x) {
     const int j = task / nrb;
     const int i0 = (task - j * nrb) << 2;
     double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
@@ -95,7 +124,111 @@ PSF_DEVINL void cta_gemm(int m, double alpha, const double* A, int lda, const do
       if (i0 + 2 < m) c[2] = c2;
     }
   }
+}
+
+// Share [t0, t1) of block r of a group of G blocks over T tasks.
+PSF_DEVINL void gemm_share(int T, int G, int r, int* t0, int* t1) {
+  const int per = (T + G - 1) / G;
+  *t0 = min(T, r * per);
+  *t1 = min(T, *t0 + per);
+}
+
+// C = alpha * A * B (m x m), by the calling block alone or, with a group,
+// split over the group's blocks (block 0 posts the product, computes its own
+// share and waits for the others').
+PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, int lda, const double* B, int ldb,
+                         double* C, int ldc) {
+  const int T = ((m + 3) >> 2) * m;
+  GemmGroup* g = sm.grp;
+  if (!g) {
+    gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, 0, T);
+    __syncthreads();
+    return;
+  }
+  const int G = gridDim.x;
+  __syncthreads();  // the block's writes of A and B precede the post
+  if (threadIdx.x == 0) {
+    g->A = A; g->B = B; g->C = C;
+    g->m = m; g->lda = lda; g->ldb = ldb; g->ldc = ldc;
+    g->alpha = alpha;
+    sm.jobs += 1;
+    __threadfence();
+    atomicExch(&g->seq, sm.jobs);
+  }
+  int t0, t1;
+  gemm_share(T, G, 0, &t0, &t1);
+  gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, t0, t1);
   __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned target = sm.jobs * (unsigned)(G - 1);
+    const unsigned long long w0 = globaltimer_ns();
+    while (ld_acquire_gpu(&g->done) < target) {
+      if (globaltimer_ns() - w0 > kWaitLimitNs) {
+        atomicOr(&g->err, 1);
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+// Blocks 1..G-1 of a group: compute the share of every product block 0
+// posts, until it stops.
+PSF_DEVINL void gemm_helper(GemmGroup* g) {
+  __shared__ int go;
+  unsigned k = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int state = 0;
+      const unsigned long long w0 = globaltimer_ns();
+      for (;;) {
+        if (ld_acquire_gpu(&g->seq) > k) { state = 1; break; }
+        if (ld_acquire_gpu(reinterpret_cast<const unsigned*>(&g->stop)) != 0u) break;
+        if (globaltimer_ns() - w0 > kWaitLimitNs) {
+          atomicOr(&g->err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+      __threadfence();
+      go = state;
+    }
+    __syncthreads();
+    if (!go) return;
+    ++k;
+    const volatile GemmGroup* vg = g;
+    const int m = vg->m;
+    int t0, t1;
+    gemm_share(((m + 3) >> 2) * m, gridDim.x, blockIdx.x, &t0, &t1);
+    gemm_tasks(m, vg->alpha, vg->A, vg->lda, vg->B, vg->ldb, vg->C, vg->ldc, t0, t1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(&g->done, 1u);
+    }
+    __syncthreads();
+  }
+}
+
+// Block 0 of a dense kernel: start (grp null for a single block) and end of
+// the group; the end releases the helpers and reports a wait that gave up.
+PSF_DEVINL void dense_group_begin(DenseSmem& sm, GemmGroup* grp) {
+  if (threadIdx.x == 0) {
+    sm.grp = (gridDim.x > 1) ? grp : nullptr;
+    sm.jobs = 0u;
+  }
+  __syncthreads();
+}
+
+PSF_DEVINL void dense_group_end(DenseSmem& sm, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0 && sm.grp) {
+    if (*(volatile int*)&sm.grp->err && err) atomicOr(err, DEVERR_TIMEOUT);
+    __threadfence();
+    atomicExch(&sm.grp->stop, 1);
+  }
 }
 
 PSF_DEVINL void cta_set_identity(int m, double d, double* A, int lda) {
@@ -273,7 +406,7 @@ PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, d
       sm.coef[k] = (sm.coef[k - 1] * (double)(ideg + 1 - k)) / (double)(k * (2 * ideg + 1 - k));
   }
   __syncthreads();
-  cta_gemm(m, scale2, H, ldh, H, ldh, h2, m);
+  cta_gemm(sm, m, scale2, H, ldh, H, ldh, h2, m);
   double* p = slot0;
   double* q = slot1;
   double* fr = slot2;
@@ -282,7 +415,7 @@ PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, d
   int iodd = 1;
   for (int k = ideg - 1; k > 0; --k) {
     double* used = iodd ? q : p;
-    cta_gemm(m, 1.0, used, m, h2, m, fr, m);
+    cta_gemm(sm, m, 1.0, used, m, h2, m, fr, m);
     for (int j = threadIdx.x; j < m; j += blockDim.x) fr[j + (size_t)j * m] += sm.coef[k - 1];
     __syncthreads();
     if (iodd) q = fr; else p = fr;
@@ -290,10 +423,10 @@ PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, d
     iodd = 1 - iodd;
   }
   if (iodd == 1) {
-    cta_gemm(m, scale, q, m, H, ldh, fr, m);
+    cta_gemm(sm, m, scale, q, m, H, ldh, fr, m);
     double* tmp = q; q = fr; fr = tmp;
   } else {
-    cta_gemm(m, scale, p, m, H, ldh, fr, m);
+    cta_gemm(sm, m, scale, p, m, H, ldh, fr, m);
     double* tmp = p; p = fr; fr = tmp;
   }
   for (size_t e = threadIdx.x; e < mm; e += blockDim.x) q[e] -= p[e];
@@ -311,7 +444,7 @@ PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, d
     double* get = p;
     double* put = q;
     for (int k = 0; k < ns; ++k) {
-      cta_gemm(m, 1.0, get, m, get, m, put, m);
+      cta_gemm(sm, m, 1.0, get, m, get, m, put, m);
       double* tmp = get; get = put; put = tmp;
     }
     res = get;
@@ -349,7 +482,7 @@ PSF_DEVINL int cta_expm_sasq(int n, const double* a, double* e, double* scratch,
   int p = 1;
   for (int k = 2; k <= q; ++k) {
     c = c * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
-    cta_gemm(n, 1.0, a2, n, x, n, tmp, n);
+    cta_gemm(sm, n, 1.0, a2, n, x, n, tmp, n);
     cta_copy(n, tmp, n, x, n);
     for (size_t l = threadIdx.x; l < nn; l += blockDim.x) {
       e[l] = e[l] + c * x[l];
@@ -360,7 +493,7 @@ PSF_DEVINL int cta_expm_sasq(int n, const double* a, double* e, double* scratch,
   }
   if (!cta_fss(n, d, n, e, sm)) return DEVERR_SINGULAR;
   for (int k = 0; k < s; ++k) {
-    cta_gemm(n, 1.0, e, n, e, n, tmp, n);
+    cta_gemm(sm, n, 1.0, e, n, e, n, tmp, n);
     cta_copy(n, tmp, n, e, n);
   }
   return 0;
@@ -384,7 +517,7 @@ PSF_DEVINL int cta_expm_taylor(int n, const double* a, double* e, double* scratc
     if (!__syncthreads_or(sig)) break;
     for (size_t l = threadIdx.x; l < nn; l += blockDim.x) e[l] += f[l];
     __syncthreads();
-    cta_gemm(n, 1.0, a, n, f, n, tmp, n);
+    cta_gemm(sm, n, 1.0, a, n, f, n, tmp, n);
     for (size_t l = threadIdx.x; l < nn; l += blockDim.x) f[l] = tmp[l] / (double)k;
     __syncthreads();
     k = k + 1;

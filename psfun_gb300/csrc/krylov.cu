@@ -565,8 +565,19 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
   }
 }
 
-__global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams fp, int i, double eps, int tridiag) {
-  __shared__ DenseSmem sm;
+// The dense kernels below (k_estimate, k_sai_estimate, k_final,
+// k_serial_apply) run as a group of gridDim.x co-resident blocks: block 0
+// runs the f(H) evaluation, the other blocks compute their shares of its
+// matrix products (gemm_helper).  Launched with one block they run alone.
+#define PSF_DENSE_KERNEL_ENTRY(grp, err)    \
+  if (blockIdx.x > 0) {                      \
+    gemm_helper(grp);                        \
+    return;                                  \
+  }                                          \
+  __shared__ DenseSmem sm;                   \
+  dense_group_begin(sm, grp)
+
+__device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps, int tridiag, DenseSmem& sm) {
   KCtrl* c = st.ctrl;
   if (c->done) return;
   const int m = i - 1;
@@ -581,6 +592,13 @@ __global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams
     return;
   }
   estimate_tail(st, i, eps, sm.red);
+}
+
+__global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams fp, int i, double eps, int tridiag,
+                                                            GemmGroup* grp) {
+  PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
+  estimate_body(st, fp, i, eps, tridiag, sm);
+  dense_group_end(sm, &st.ctrl->err);
 }
 
 // USERF estimate tail: yk was produced by the host-assisted path.
@@ -611,9 +629,7 @@ __global__ void __launch_bounds__(kVecThreads) k_sai_rhs(KState st, int i) {
 // hcomp = inv(H(1:i-1,1:i-1)) and, as in the reference's loop
 // `do j=1,i-1,i`, only hcomp(1,1) shifted by -tau; then the residual estimate
 // of the Arnoldi method.
-__global__ void __launch_bounds__(kDenseThreads) k_sai_estimate(KState st, FunParams fp, int i, double eps,
-                                                                double tau) {
-  __shared__ DenseSmem sm;
+__device__ void sai_estimate_body(KState& st, const FunParams& fp, int i, double eps, double tau, DenseSmem& sm) {
   KCtrl* c = st.ctrl;
   if (c->done) return;
   const int m = i - 1;
@@ -643,6 +659,13 @@ __global__ void __launch_bounds__(kDenseThreads) k_sai_estimate(KState st, FunPa
   estimate_tail(st, i, eps, sm.red);
 }
 
+__global__ void __launch_bounds__(kDenseThreads) k_sai_estimate(KState st, FunParams fp, int i, double eps,
+                                                                double tau, GemmGroup* grp) {
+  PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
+  sai_estimate_body(st, fp, i, eps, tau, sm);
+  dense_group_end(sm, &st.ctrl->err);
+}
+
 // Final f(H) e1 when no estimate converged, and the assembly coefficients
 // (psfun_d_arnoldi.f90:282-329, psfun_d_lanczos.f90:330-377).
 // mode: 0 = compute f on the device, 1 = yk already computed (USERF).
@@ -650,9 +673,8 @@ __device__ int final_dim(const KCtrl* c, int arnoldi) {
   return (arnoldi && c->breakdown) ? c->itx : c->itx - 1;
 }
 
-__global__ void __launch_bounds__(kDenseThreads) k_final(KState st, FunParams fp, int tridiag, int keeplast,
-                                                         int arnoldi, int mode) {
-  __shared__ DenseSmem sm;
+__device__ void final_body(KState& st, const FunParams& fp, int tridiag, int keeplast, int arnoldi, int mode,
+                           DenseSmem& sm) {
   KCtrl* c = st.ctrl;
   if (c->info != 0) return;
   if (c->beta0 == 0.0) {
@@ -690,6 +712,13 @@ __global__ void __launch_bounds__(kDenseThreads) k_final(KState st, FunParams fp
   }
 }
 
+__global__ void __launch_bounds__(kDenseThreads) k_final(KState st, FunParams fp, int tridiag, int keeplast,
+                                                         int arnoldi, int mode, GemmGroup* grp) {
+  PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
+  final_body(st, fp, tridiag, keeplast, arnoldi, mode, sm);
+  dense_group_end(sm, &st.ctrl->err);
+}
+
 // y = sum_j coef_j W_j  (the assembly y = rs(1) * sum yk(j) v(j))
 __global__ void __launch_bounds__(kVecThreads) k_recombine(KState st, double* __restrict__ y) {
   const KCtrl* c = st.ctrl;
@@ -717,6 +746,7 @@ __global__ void __launch_bounds__(kVecThreads) k_recombine(KState st, double* __
 __global__ void __launch_bounds__(kDenseThreads) k_symeig(int m, const double* H, int ldh, double* w, double* V,
                                                           double* work) {
   __shared__ DenseSmem sm;
+  dense_group_begin(sm, nullptr);
   cta_sym_eig(m, H, ldh, w, V, work, sm);
 }
 
@@ -796,6 +826,31 @@ static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder)
   PSF_TRY(meth->scratch.ensure(sizeof(double) * fs));
   PSF_TRY(meth->partials.ensure(sizeof(double) * 2 * 4096));
   PSF_TRY(meth->ctrl.ensure(sizeof(KCtrl) + 64));
+  PSF_TRY(meth->dgroup.ensure(sizeof(GemmGroup) + 64));
+  return PSFUN_SUCCESS;
+}
+
+// Blocks of the group that shares the matrix products of a dense f(H) whose
+// products have order m: one block while its 256 threads need at most three
+// rounds of 4-row strips, else about 192 strips per block, at most 16.
+static int dense_group_blocks(int m) {
+  const long T = (long)((m + 3) / 4) * m;
+  if (T <= 3L * kDenseThreads) return 1;
+  return (int)std::min<long>(16, (T + 191) / 192);
+}
+
+// A dense kernel (its last parameter the GemmGroup*, set in args) as a group
+// of G co-resident blocks, or as one block with no group.
+static int launch_dense(const void* kern, int G, GemmGroup* grp, GemmGroup** grp_arg, void** args, cudaStream_t s) {
+  if (G > 1) {
+    *grp_arg = grp;
+    PSF_CUDA(cudaMemsetAsync(grp, 0, sizeof(GemmGroup), s));
+    PSF_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(kDenseThreads), args, 0, s));
+  } else {
+    *grp_arg = nullptr;
+    PSF_CUDA(cudaLaunchKernel(kern, dim3(1), dim3(kDenseThreads), args, 0, s));
+  }
+  count_launch();
   return PSFUN_SUCCESS;
 }
 
@@ -1015,7 +1070,14 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   };
   auto enqueue_epilogue = [&](int mode) -> int {
     prof_begin(PROF_FINAL, s);
-    k_final<<<1, kDenseThreads, 0, s>>>(st, fpk, tridiag, meth->keeplast, arnoldi, mode);
+    {
+      int keeplast = meth->keeplast;
+      GemmGroup* g = nullptr;
+      void* args[] = {(void*)&st, (void*)&fpk, (void*)&tridiag, (void*)&keeplast, (void*)&arnoldi, (void*)&mode,
+                      (void*)&g};
+      const int G = (tridiag || mode != 0 || !fh_uses_gemm(fpk)) ? 1 : dense_group_blocks(nl + 1 + fpk.phiorder);
+      PSF_TRY(launch_dense((const void*)k_final, G, meth->dgroup.as<GemmGroup>(), &g, args, s));
+    }
     prof_end(PROF_FINAL, s);
     prof_begin(PROF_RECOMBINE, s);
     k_recombine<<<gv, kVecThreads, 0, s>>>(st, y);
@@ -1083,8 +1145,15 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       PSF_TRY(enqueue_step(i));
       if (istop == 1) {
         if (sai) {
-          k_sai_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, meth->tau);
-          count_launch();
+          {
+            double tau = meth->tau;
+            int ii = i;
+            double e = eps;
+            GemmGroup* g = nullptr;
+            void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&tau, (void*)&g};
+            PSF_TRY(launch_dense((const void*)k_sai_estimate, fh_uses_gemm(fpk) ? dense_group_blocks(i + fpk.phiorder) : 1,
+                                 meth->dgroup.as<GemmGroup>(), &g, args, s));
+          }
           PSF_CUDA(cudaStreamSynchronize(s));  // the next inner solve waits for the verdict
         } else if (userf) {
           // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
@@ -1096,8 +1165,14 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
           k_estimate_tail<<<1, kDenseThreads, 0, s>>>(st, i, eps);
           count_launch();
         } else {
-          k_estimate<<<1, kDenseThreads, 0, s>>>(st, fpk, i, eps, tridiag);
-          count_launch();
+          {
+            int ii = i, td = tridiag;
+            double e = eps;
+            GemmGroup* g = nullptr;
+            void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&td, (void*)&g};
+            const int G = (tridiag || !fh_uses_gemm(fpk)) ? 1 : dense_group_blocks(i + fpk.phiorder);
+            PSF_TRY(launch_dense((const void*)k_estimate, G, meth->dgroup.as<GemmGroup>(), &g, args, s));
+          }
         }
       }
       PSF_CUDA(cudaGetLastError());
@@ -1171,10 +1246,11 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kDenseThreads) k_serial_apply(FunParams fp, int n, const double* a, int lda,
                                                                 const double* x, double* y, double* scratch,
-                                                                int* status) {
-  __shared__ DenseSmem sm;
+                                                                int* status, GemmGroup* grp) {
+  PSF_DENSE_KERNEL_ENTRY(grp, status);
   const int rc = fh_apply_cta(fp, n, a, lda, x, y, scratch, false, sm);
   if (threadIdx.x == 0) *status = rc;
+  dense_group_end(sm, status);
 }
 
 int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev, const double* x_dev) {
@@ -1191,8 +1267,19 @@ int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, 
     rc = userf_apply(fun->f_ptr, fun->scaling, n, a_dev, lda, x_dev, y_dev, scr.as<double>());
   } else {
     int* dstat = reinterpret_cast<int*>(scr.as<char>() + sizeof(double) * fs);
-    k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr.as<double>(), dstat);
-    count_launch();
+    static DevBuf dgroup;
+    PSF_TRY(dgroup.ensure(sizeof(GemmGroup) + 64));
+    {
+      int nn = n, ld = lda;
+      const double *aa = a_dev, *xx = x_dev;
+      double* yy = y_dev;
+      double* sp = scr.as<double>();
+      GemmGroup* g = nullptr;
+      void* args[] = {(void*)&fp, (void*)&nn, (void*)&aa, (void*)&ld, (void*)&xx, (void*)&yy, (void*)&sp,
+                      (void*)&dstat, (void*)&g};
+      const int G = fh_uses_gemm(fp) ? dense_group_blocks(n + fp.phiorder + 1) : 1;
+      PSF_TRY(launch_dense((const void*)k_serial_apply, G, dgroup.as<GemmGroup>(), &g, args, s));
+    }
     int hs = 0;
     cudaError_t e = cudaMemcpyAsync(&hs, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -1914,7 +2001,7 @@ static int serial_apply_static(psfun_serial* fun, int n, const double* a_dev, in
   int* dstat = reinterpret_cast<int*>(scr + fs);
   cudaStream_t s = stream();
   PSF_CUDA(cudaMemsetAsync(dstat, 0xff, sizeof(int), s));
-  k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr, dstat);
+  k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr, dstat, nullptr);
   count_launch();
   PSF_CUDA(cudaGetLastError());
   int hs = -1;
