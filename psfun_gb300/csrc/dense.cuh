@@ -1,4 +1,5 @@
-// dense.cuh -- the projected f(H) on the device, FP64, inside one CTA.
+// dense.cuh -- the projected f(H) on the device, FP64, run by one block
+// (block 0), whose matrix products a cooperative group of blocks can share.
 //
 // Restates the dense routines behind psfun_d_serial%apply
 // (serial/psfun_d_serial_mod.F90:172-523):
@@ -13,7 +14,8 @@
 // All matrices are column-major with a leading dimension, exactly as the
 // Fortran arrays.  Every routine is called by all threads of the block with
 // block-uniform arguments and ends with __syncthreads().  Work arrays live in
-// a global scratch buffer (L1/L2 resident at these sizes).
+// a global scratch buffer (L1/L2 resident at these sizes), which is also how
+// the blocks of a group see each other's product shares.
 #pragma once
 
 #include <cuComplex.h>
