@@ -55,26 +55,30 @@ __host__ __device__ inline bool fh_uses_gemm(const FunParams& fp) {
 __host__ __device__ inline size_t fh_scratch_doubles(int m, int phiorder) {
   size_t M = (size_t)m + (size_t)(phiorder > 0 ? phiorder : 1) + 1;
   size_t a = 6 * M * M + 64 * M + 512;
-  size_t b = 16 * M * M + 64 * M + 512;  // 7 complex m x m systems
+  size_t b = 16 * M * M + 64 * M + 512;  // 7 complex m x m systems, solutions and multipliers
   return a > b ? a : b;
 }
 
-// A group of co-resident blocks (one cooperative launch) sharing the matrix
-// products of one dense f(H) evaluation: block 0 runs the evaluation and
-// posts each product here; blocks 1..G-1 only compute their share of the
-// posted product (gemm_helper).  In global memory, zeroed by the host before
-// each launch.  All waits are bounded: a wait that gives up sets err, which
-// the kernel reports as DEVERR_TIMEOUT.
-struct GemmGroup {
-  const double* A;
+// A group of co-resident blocks (one cooperative launch) sharing one dense
+// f(H) evaluation: block 0 runs the evaluation and posts its heavy parts
+// here, a matrix product (kind 0: each block computes a share of the 4-row
+// strips) or the seven pole solves of CRAM on a full H (kind 1: block r
+// solves the poles r, r + G, ...); blocks 1..G-1 only serve those jobs
+// (dense_helper).  In global memory, zeroed by the host before each launch.
+// All waits are bounded: a wait that gives up sets err, which the kernel
+// reports as DEVERR_TIMEOUT.
+struct DenseGroup {
+  int kind;
+  const double* A;  // kind 0: C = alpha A B; kind 1: A = H (ldh = lda), B = x, alpha = t, C = scratch
   const double* B;
   double* C;
   int m, lda, ldb, ldc;
   double alpha;
-  unsigned seq;   // products posted by block 0
-  unsigned done;  // shares finished by the other blocks
+  unsigned seq;   // jobs posted by block 0
+  unsigned done;  // jobs finished by the other blocks
   int stop;       // block 0 has finished
   int err;
+  int bad;        // kind 1: a pole system was singular
 };
 
 struct DenseSmem {
@@ -82,7 +86,7 @@ struct DenseSmem {
   double dv[8];
   int iv[8];
   double coef[64];
-  GemmGroup* grp;  // null: a single block does everything
+  DenseGroup* grp;  // null: a single block does everything
   unsigned jobs;   // products posted so far (block 0, thread 0)
 };
 
@@ -135,21 +139,13 @@ PSF_DEVINL void gemm_share(int T, int G, int r, int* t0, int* t1) {
   *t1 = min(T, *t0 + per);
 }
 
-// C = alpha * A * B (m x m), by the calling block alone or, with a group,
-// split over the group's blocks (block 0 posts the product, computes its own
-// share and waits for the others').
-PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, int lda, const double* B, int ldb,
-                         double* C, int ldc) {
-  const int T = ((m + 3) >> 2) * m;
-  GemmGroup* g = sm.grp;
-  if (!g) {
-    gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, 0, T);
-    __syncthreads();
-    return;
-  }
-  const int G = gridDim.x;
-  __syncthreads();  // the block's writes of A and B precede the post
+// Block 0 posts a job to its group (all threads call it).
+PSF_DEVINL void group_post(DenseSmem& sm, int kind, int m, double alpha, const double* A, int lda, const double* B,
+                           int ldb, double* C, int ldc) {
+  DenseGroup* g = sm.grp;
+  __syncthreads();  // the block's writes of the operands precede the post
   if (threadIdx.x == 0) {
+    g->kind = kind;
     g->A = A; g->B = B; g->C = C;
     g->m = m; g->lda = lda; g->ldb = ldb; g->ldc = ldc;
     g->alpha = alpha;
@@ -157,12 +153,14 @@ PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, in
     __threadfence();
     atomicExch(&g->seq, sm.jobs);
   }
-  int t0, t1;
-  gemm_share(T, G, 0, &t0, &t1);
-  gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, t0, t1);
+}
+
+// Block 0 waits until the other blocks have finished the posted job.
+PSF_DEVINL void group_wait(DenseSmem& sm) {
+  DenseGroup* g = sm.grp;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned target = sm.jobs * (unsigned)(G - 1);
+    const unsigned target = sm.jobs * (unsigned)(gridDim.x - 1);
     const unsigned long long w0 = globaltimer_ns();
     while (ld_acquire_gpu(&g->done) < target) {
       if (globaltimer_ns() - w0 > kWaitLimitNs) {
@@ -176,9 +174,28 @@ PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, in
   __syncthreads();
 }
 
-// Blocks 1..G-1 of a group: compute the share of every product block 0
-// posts, until it stops.
-PSF_DEVINL void gemm_helper(GemmGroup* g) {
+// C = alpha * A * B (m x m), by the calling block alone or, with a group,
+// split over the group's blocks (block 0 posts the product, computes its own
+// share and waits for the others').
+PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, int lda, const double* B, int ldb,
+                         double* C, int ldc) {
+  const int T = ((m + 3) >> 2) * m;
+  if (!sm.grp) {
+    gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, 0, T);
+    __syncthreads();
+    return;
+  }
+  group_post(sm, 0, m, alpha, A, lda, B, ldb, C, ldc);
+  int t0, t1;
+  gemm_share(T, gridDim.x, 0, &t0, &t1);
+  gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, t0, t1);
+  group_wait(sm);
+}
+
+static __device__ bool cram_pole_block(int m, double t, const double* H, int ldh, const double* x, int p, double* scratch);
+
+// Blocks 1..G-1 of a group: serve every job block 0 posts, until it stops.
+PSF_DEVINL void dense_helper(DenseGroup* g) {
   __shared__ int go;
   unsigned k = 0;
   for (;;) {
@@ -200,11 +217,21 @@ PSF_DEVINL void gemm_helper(GemmGroup* g) {
     __syncthreads();
     if (!go) return;
     ++k;
-    const volatile GemmGroup* vg = g;
+    const volatile DenseGroup* vg = g;
     const int m = vg->m;
-    int t0, t1;
-    gemm_share(((m + 3) >> 2) * m, gridDim.x, blockIdx.x, &t0, &t1);
-    gemm_tasks(m, vg->alpha, vg->A, vg->lda, vg->B, vg->ldb, vg->C, vg->ldc, t0, t1);
+    if (vg->kind == 0) {
+      int t0, t1;
+      gemm_share(((m + 3) >> 2) * m, gridDim.x, blockIdx.x, &t0, &t1);
+      gemm_tasks(m, vg->alpha, vg->A, vg->lda, vg->B, vg->ldb, vg->C, vg->ldc, t0, t1);
+    } else {
+      const double t = vg->alpha;
+      const double* H = vg->A;
+      const int ldh = vg->lda;
+      const double* x = vg->B;
+      double* scr = vg->C;
+      for (int p = blockIdx.x; p < 7; p += gridDim.x)
+        if (!cram_pole_block(m, t, H, ldh, x, p, scr) && threadIdx.x == 0) atomicExch(&g->bad, 1);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -216,7 +243,7 @@ PSF_DEVINL void gemm_helper(GemmGroup* g) {
 
 // Block 0 of a dense kernel: start (grp null for a single block) and end of
 // the group; the end releases the helpers and reports a wait that gave up.
-PSF_DEVINL void dense_group_begin(DenseSmem& sm, GemmGroup* grp) {
+PSF_DEVINL void dense_group_begin(DenseSmem& sm, DenseGroup* grp) {
   if (threadIdx.x == 0) {
     sm.grp = (gridDim.x > 1) ? grp : nullptr;
     sm.jobs = 0u;
@@ -620,8 +647,100 @@ PSF_DEVINL void cta_cram_hessenberg(int m, double t, const double* H, int ldh, c
 }
 
 // CHBSYM / CHBGEN on a general matrix: one warp per pole, complex GEPP.
-PSF_DEVINL bool cta_cram_full(int m, double t, const double* H, int ldh, const double* x, double* y,
+// Pole p of CRAM on a full H by the whole block: (-tH - theta_p I) b = x by
+// Gaussian elimination with partial pivoting, the operations of the
+// warp-per-pole solver below entry by entry (same pivot rule, same row
+// updates, the same back substitution by one warp), with each elimination
+// step's row updates spread over all threads.  Layout of cta_cram_full's
+// scratch, plus the multipliers of pole p after the seven systems.  Returns
+// false on a zero pivot.
+static __device__ bool cram_pole_block(int m, double t, const double* H, int ldh, const double* x, int p, double* scratch) {
+  __shared__ int s_bi, s_bad;
+  zc* b = (zc*)scratch + (size_t)p * m;
+  zc* a = (zc*)(scratch + 2 * 7 * (size_t)m) + (size_t)p * m * m;
+  zc* lc = (zc*)(scratch + 2 * 7 * (size_t)m + 2 * 7 * (size_t)m * m) + (size_t)p * m;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = blockDim.x;
+  const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
+  for (int e = threadIdx.x; e < m * m; e += nt) {
+    const int j = e / m, i = e - j * m;
+    zc v = zmk(-t * H[i + (size_t)j * ldh], 0.0);
+    if (i == j) v = zsub(v, theta);
+    a[i + (size_t)j * m] = v;
+  }
+  for (int j = threadIdx.x; j < m; j += nt) b[j] = zmk(x[j], 0.0);
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + lane; i < m; i += 32) {
+        const double v = zabs(a[i + (size_t)k * m]);
+        if (v > best) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) {
+        s_bi = bi;
+        if (best == 0.0) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    if (s_bad) break;
+    const int bi = s_bi;
+    if (bi != k) {
+      for (int j = threadIdx.x; j < m; j += nt) {
+        const zc tt = a[k + (size_t)j * m]; a[k + (size_t)j * m] = a[bi + (size_t)j * m]; a[bi + (size_t)j * m] = tt;
+      }
+      if (threadIdx.x == 0) { const zc tt = b[k]; b[k] = b[bi]; b[bi] = tt; }
+      __syncthreads();
+    }
+    const zc piv = a[k + (size_t)k * m];
+    for (int i = k + 1 + threadIdx.x; i < m; i += nt) lc[i] = zdiv(a[i + (size_t)k * m], piv);
+    __syncthreads();
+    const int rows = m - k - 1;
+    for (int e = threadIdx.x; e < rows * rows; e += nt) {
+      const int jj = e / rows, ii = e - jj * rows;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      a[i + (size_t)j * m] = zsub(a[i + (size_t)j * m], zmul(lc[i], a[k + (size_t)j * m]));
+    }
+    for (int i = k + 1 + threadIdx.x; i < m; i += nt) b[i] = zsub(b[i], zmul(lc[i], b[k]));
+    __syncthreads();
+  }
+  const bool bad = s_bad != 0;
+  __syncthreads();
+  if (!bad && warp == 0) {
+    for (int i = m - 1; i >= 0; --i) {
+      zc part = zmk(0.0, 0.0);
+      for (int j = i + 1 + lane; j < m; j += 32) part = zadd(part, zmul(a[i + (size_t)j * m], b[j]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        part.x += __shfl_xor_sync(0xffffffffu, part.x, o);
+        part.y += __shfl_xor_sync(0xffffffffu, part.y, o);
+      }
+      if (lane == 0) b[i] = zdiv(zsub(b[i], part), a[i + (size_t)i * m]);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  return !bad;
+}
+
+PSF_DEVINL bool cta_cram_full(DenseSmem& sm, int m, double t, const double* H, int ldh, const double* x, double* y,
                               double* scratch) {
+  if (sm.grp) {  // one block per pole (block 0 takes poles 0, G, ...)
+    group_post(sm, 1, m, t, H, ldh, x, 0, scratch, 0);
+    bool ok = true;
+    for (int p = 0; p < 7; p += gridDim.x) ok = cram_pole_block(m, t, H, ldh, x, p, scratch) && ok;
+    group_wait(sm);
+    if (!ok || *(volatile int*)&sm.grp->bad) return false;
+    cram_accumulate(m, x, (const zc*)scratch, y);
+    return true;
+  }
   zc* sols = (zc*)scratch;
   zc* work = (zc*)(scratch + 2 * 7 * (size_t)m);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -892,7 +1011,7 @@ PSF_DEVINL int fh_apply_cta(const FunParams& fp, int m, const double* H, int ldh
       case VAR_CHBGEN:
       case VAR_CHBSYM: {
         const bool ok = tridiag ? cta_cram_tridiag(m, fp.scaling, H, ldh, x, y, scratch)
-                                : cta_cram_full(m, fp.scaling, H, ldh, x, y, scratch);
+                                : cta_cram_full(sm, m, fp.scaling, H, ldh, x, y, scratch);
         return ok ? 0 : DEVERR_SINGULAR;
       }
       default:

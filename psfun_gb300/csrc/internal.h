@@ -123,7 +123,7 @@ struct psfun_krylov {
   int prec = 0;  // inner-solve preconditioner of SAIARNOLDI: 0 NONE, 1 DIAG
   // cached workspace (never per call)
   psf::DevBuf V, u, small, scratch, partials, ctrl, xy;
-  psf::DevBuf dgroup;  // GemmGroup of the dense f(H) kernels
+  psf::DevBuf dgroup;  // DenseGroup of the dense f(H) kernels
   int64_t ldv = 0;
   int nl_cap = 0;
   // CUDA graph of a whole fixed-length (istop = 2) solve, replayed while the

@@ -568,10 +568,10 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
 // The dense kernels below (k_estimate, k_sai_estimate, k_final,
 // k_serial_apply) run as a group of gridDim.x co-resident blocks: block 0
 // runs the f(H) evaluation, the other blocks compute their shares of its
-// matrix products (gemm_helper).  Launched with one block they run alone.
+// matrix products (dense_helper).  Launched with one block they run alone.
 #define PSF_DENSE_KERNEL_ENTRY(grp, err)    \
   if (blockIdx.x > 0) {                      \
-    gemm_helper(grp);                        \
+    dense_helper(grp);                        \
     return;                                  \
   }                                          \
   __shared__ DenseSmem sm;                   \
@@ -595,7 +595,7 @@ __device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps
 }
 
 __global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams fp, int i, double eps, int tridiag,
-                                                            GemmGroup* grp) {
+                                                            DenseGroup* grp) {
   PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
   estimate_body(st, fp, i, eps, tridiag, sm);
   dense_group_end(sm, &st.ctrl->err);
@@ -660,7 +660,7 @@ __device__ void sai_estimate_body(KState& st, const FunParams& fp, int i, double
 }
 
 __global__ void __launch_bounds__(kDenseThreads) k_sai_estimate(KState st, FunParams fp, int i, double eps,
-                                                                double tau, GemmGroup* grp) {
+                                                                double tau, DenseGroup* grp) {
   PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
   sai_estimate_body(st, fp, i, eps, tau, sm);
   dense_group_end(sm, &st.ctrl->err);
@@ -713,7 +713,7 @@ __device__ void final_body(KState& st, const FunParams& fp, int tridiag, int kee
 }
 
 __global__ void __launch_bounds__(kDenseThreads) k_final(KState st, FunParams fp, int tridiag, int keeplast,
-                                                         int arnoldi, int mode, GemmGroup* grp) {
+                                                         int arnoldi, int mode, DenseGroup* grp) {
   PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
   final_body(st, fp, tridiag, keeplast, arnoldi, mode, sm);
   dense_group_end(sm, &st.ctrl->err);
@@ -826,7 +826,7 @@ static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder)
   PSF_TRY(meth->scratch.ensure(sizeof(double) * fs));
   PSF_TRY(meth->partials.ensure(sizeof(double) * 2 * 4096));
   PSF_TRY(meth->ctrl.ensure(sizeof(KCtrl) + 64));
-  PSF_TRY(meth->dgroup.ensure(sizeof(GemmGroup) + 64));
+  PSF_TRY(meth->dgroup.ensure(sizeof(DenseGroup) + 64));
   return PSFUN_SUCCESS;
 }
 
@@ -839,12 +839,21 @@ static int dense_group_blocks(int m) {
   return (int)std::min<long>(16, (T + 191) / 192);
 }
 
-// A dense kernel (its last parameter the GemmGroup*, set in args) as a group
+// Blocks of the group for a dense f(H) of order m: the product-based
+// variants by dense_group_blocks (phi's products have order m + k + 1), the
+// CRAM variants on a full H one block per pole from order 24, else one.
+static int dense_blocks(const FunParams& fp, int m, bool tridiag) {
+  if (fh_uses_gemm(fp)) return dense_group_blocks(m + (fp.fname == FN_PHI ? fp.phiorder + 1 : 0));
+  if (fp.fname == FN_EXP && (fp.variant == VAR_CHBGEN || fp.variant == VAR_CHBSYM) && !tridiag && m >= 24) return 7;
+  return 1;
+}
+
+// A dense kernel (its last parameter the DenseGroup*, set in args) as a group
 // of G co-resident blocks, or as one block with no group.
-static int launch_dense(const void* kern, int G, GemmGroup* grp, GemmGroup** grp_arg, void** args, cudaStream_t s) {
+static int launch_dense(const void* kern, int G, DenseGroup* grp, DenseGroup** grp_arg, void** args, cudaStream_t s) {
   if (G > 1) {
     *grp_arg = grp;
-    PSF_CUDA(cudaMemsetAsync(grp, 0, sizeof(GemmGroup), s));
+    PSF_CUDA(cudaMemsetAsync(grp, 0, sizeof(DenseGroup), s));
     PSF_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(kDenseThreads), args, 0, s));
   } else {
     *grp_arg = nullptr;
@@ -1072,11 +1081,11 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     prof_begin(PROF_FINAL, s);
     {
       int keeplast = meth->keeplast;
-      GemmGroup* g = nullptr;
+      DenseGroup* g = nullptr;
       void* args[] = {(void*)&st, (void*)&fpk, (void*)&tridiag, (void*)&keeplast, (void*)&arnoldi, (void*)&mode,
                       (void*)&g};
-      const int G = (tridiag || mode != 0 || !fh_uses_gemm(fpk)) ? 1 : dense_group_blocks(nl + 1 + fpk.phiorder);
-      PSF_TRY(launch_dense((const void*)k_final, G, meth->dgroup.as<GemmGroup>(), &g, args, s));
+      const int G = (mode != 0) ? 1 : dense_blocks(fpk, nl + 1, tridiag != 0);
+      PSF_TRY(launch_dense((const void*)k_final, G, meth->dgroup.as<DenseGroup>(), &g, args, s));
     }
     prof_end(PROF_FINAL, s);
     prof_begin(PROF_RECOMBINE, s);
@@ -1149,10 +1158,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
             double tau = meth->tau;
             int ii = i;
             double e = eps;
-            GemmGroup* g = nullptr;
+            DenseGroup* g = nullptr;
             void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&tau, (void*)&g};
-            PSF_TRY(launch_dense((const void*)k_sai_estimate, fh_uses_gemm(fpk) ? dense_group_blocks(i + fpk.phiorder) : 1,
-                                 meth->dgroup.as<GemmGroup>(), &g, args, s));
+            PSF_TRY(launch_dense((const void*)k_sai_estimate, dense_blocks(fpk, i, false),
+                                 meth->dgroup.as<DenseGroup>(), &g, args, s));
           }
           PSF_CUDA(cudaStreamSynchronize(s));  // the next inner solve waits for the verdict
         } else if (userf) {
@@ -1168,10 +1177,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
           {
             int ii = i, td = tridiag;
             double e = eps;
-            GemmGroup* g = nullptr;
+            DenseGroup* g = nullptr;
             void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&td, (void*)&g};
-            const int G = (tridiag || !fh_uses_gemm(fpk)) ? 1 : dense_group_blocks(i + fpk.phiorder);
-            PSF_TRY(launch_dense((const void*)k_estimate, G, meth->dgroup.as<GemmGroup>(), &g, args, s));
+            const int G = dense_blocks(fpk, i, tridiag != 0);
+            PSF_TRY(launch_dense((const void*)k_estimate, G, meth->dgroup.as<DenseGroup>(), &g, args, s));
           }
         }
       }
@@ -1246,7 +1255,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kDenseThreads) k_serial_apply(FunParams fp, int n, const double* a, int lda,
                                                                 const double* x, double* y, double* scratch,
-                                                                int* status, GemmGroup* grp) {
+                                                                int* status, DenseGroup* grp) {
   PSF_DENSE_KERNEL_ENTRY(grp, status);
   const int rc = fh_apply_cta(fp, n, a, lda, x, y, scratch, false, sm);
   if (threadIdx.x == 0) *status = rc;
@@ -1268,17 +1277,17 @@ int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, 
   } else {
     int* dstat = reinterpret_cast<int*>(scr.as<char>() + sizeof(double) * fs);
     static DevBuf dgroup;
-    PSF_TRY(dgroup.ensure(sizeof(GemmGroup) + 64));
+    PSF_TRY(dgroup.ensure(sizeof(DenseGroup) + 64));
     {
       int nn = n, ld = lda;
       const double *aa = a_dev, *xx = x_dev;
       double* yy = y_dev;
       double* sp = scr.as<double>();
-      GemmGroup* g = nullptr;
+      DenseGroup* g = nullptr;
       void* args[] = {(void*)&fp, (void*)&nn, (void*)&aa, (void*)&ld, (void*)&xx, (void*)&yy, (void*)&sp,
                       (void*)&dstat, (void*)&g};
-      const int G = fh_uses_gemm(fp) ? dense_group_blocks(n + fp.phiorder + 1) : 1;
-      PSF_TRY(launch_dense((const void*)k_serial_apply, G, dgroup.as<GemmGroup>(), &g, args, s));
+      const int G = dense_blocks(fp, n, false);
+      PSF_TRY(launch_dense((const void*)k_serial_apply, G, dgroup.as<DenseGroup>(), &g, args, s));
     }
     int hs = 0;
     cudaError_t e = cudaMemcpyAsync(&hs, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
