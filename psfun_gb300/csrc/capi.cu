@@ -635,6 +635,19 @@ int psfun_gpu_d_krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun
   return krylov_apply_device(meth, fun, a, y, x, eps, itmax, itrace, istop, iter, err, res, res_cap, res_len);
 }
 
+// The device address of host memory that is pinned and mapped into the
+// device's address space (cudaHostAlloc, cudaHostRegister), else null:
+// pageable memory is staged through device buffers instead.
+static void* mapped_device_ptr(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return at.devicePointer;
+}
+
 int psfun_gpu_d_krylov_apply(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, double* y, const double* x,
                              double eps, int itmax, int itrace, int istop, int* iter, double* err, double* res,
                              int res_cap, int* res_len) {
@@ -647,10 +660,23 @@ int psfun_gpu_d_krylov_apply(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a
   double* dx = meth->xy.as<double>();
   double* dy = reinterpret_cast<double*>(meth->xy.as<char>() + vb);
   cudaStream_t s = stream();
-  PSF_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  // Pinned, mapped host vectors are read and written by the kernels in place
+  // (x once by the first kernel, y once by the assembly), over the
+  // CPU-GPU link, instead of through staging copies; x is staged when it
+  // shares memory with y.
+  const double* mx = static_cast<const double*>(mapped_device_ptr(x));
+  double* my = static_cast<double*>(mapped_device_ptr(y));
+  if (mx && my) {
+    const char *xb = reinterpret_cast<const char*>(x), *yb = reinterpret_cast<const char*>(y);
+    const size_t len = sizeof(double) * (size_t)n;
+    if (xb < yb + len && yb < xb + len) mx = nullptr;
+  }
+  if (mx) dx = const_cast<double*>(mx);
+  else PSF_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (my) dy = my;
   const int rc = krylov_apply_device(meth, fun, a, dy, dx, eps, itmax, itrace, istop, iter, err, res, res_cap, res_len);
   if (rc != PSFUN_SUCCESS) return rc;
-  PSF_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (!my) PSF_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
   return PSFUN_SUCCESS;
 }

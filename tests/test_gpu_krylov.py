@@ -257,3 +257,29 @@ def test_itrace_log(lib, capfd):
     # itrace 0: silent
     meth.apply(fun, pg.CsrMatrix.from_scipy(A), x, 1e-10, itmax=80, istop=1)
     assert "ARNOLDI+" not in capfd.readouterr().out
+
+
+@pytest.mark.parametrize("kname,variant,istop", [("LANCZOS", "CHBSYM", 2), ("ARNOLDI", "GENPADE", 1)])
+def test_pinned_host_vectors_in_place(lib, kname, variant, istop):
+    """Pinned, mapped host vectors are read and written by the kernels in place
+    (no staging copies): the same result, bit for bit, as pageable arrays;
+    x sharing memory with y is staged first."""
+    import torch
+    import psfun_gb300 as pg
+    A = -matrices.laplacian_2d(60)
+    n = A.shape[0]
+    x = matrices.unit(np.random.default_rng(9).standard_normal(n))
+    a = pg.CsrMatrix.from_scipy(A)
+    fun = pg.PsfunDSerial()
+    assert fun.set("VARIANT", variant) == 0
+    meth = pg.PsfunDKrylov()
+    assert meth.set("KNAME", kname) == 0
+    ref = meth.apply(fun, a, x.copy(), 1e-10, itmax=60, istop=istop)
+    xp = torch.tensor(x).pin_memory()
+    yp = torch.zeros(n, dtype=torch.float64).pin_memory()
+    r = meth.apply(fun, a, xp.numpy(), 1e-10, itmax=60, istop=istop, y=yp.numpy())
+    assert r.info == 0 and r.iter == ref.iter
+    assert np.array_equal(yp.numpy(), ref.y)
+    # in place: y is x
+    r2 = meth.apply(fun, a, xp.numpy(), 1e-10, itmax=60, istop=istop, y=xp.numpy())
+    assert r2.info == 0 and np.array_equal(xp.numpy(), ref.y)
