@@ -8,8 +8,9 @@ reference's Lanczos variant EXP/CHBSYM.  Lanczos ignores fun%scaling in the
 reference (psfun_d_lanczos.f90:172-173), so the matrix passed is -0.05 A.
 
   value      solves/s with x, y and A resident in HBM (device-pointer C-ABI)
-  e2e        solves/s through the host-pointer C-ABI (x pinned on the host,
-             H2D of x and D2H of y inside every step)
+  e2e        solves/s through the host-pointer C-ABI with x and y pinned on
+             the host: every step moves x to the device and y back (the
+             kernels read x and write y in place over the CPU-GPU link)
   roofline   k_lz_persist, the cooperative kernel that runs all 80 Lanczos
              steps: algorithmic bytes per launch (80 (B_spmv + 32 n) - 8 n,
              B_spmv = 12 nnz + 4 (n+1) + 16 n) / its CUDA-event launch time;
