@@ -1337,52 +1337,67 @@ struct MsParams {
 // step at which every shift has converged, or at a breakdown: c->itx is that
 // step and the Lanczos steps computed after it are ignored.
 __global__ void k_ms_monitor(KState st, MsParams mp, int i0, int i1) {
+  // one thread per shift (blockDim.x >= N); the recurrence of each shift
+  // stays in registers over the chunk and a complex division is one
+  // reciprocal of a squared modulus and products
   __shared__ double red[32];
   KCtrl* c = st.ctrl;
   if (c->done) return;
   const int ibd = c->breakdown ? c->itx : i1;  // a breakdown found at step itx ends the basis there
+  const int j = threadIdx.x;
+  const bool act = j < mp.N;
+  const zc xi = act ? zmk(mp.xi[2 * j], mp.xi[2 * j + 1]) : zmk(0.0, 0.0);
+  zc d = zmk(1.0, 0.0), phi = zmk(0.0, 0.0);
+  if (act && i0 > 1) {
+    d = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
+    phi = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
+  }
   for (int i = i0; i < i1; ++i) {
     const bool last_valid = i >= ibd;
     const double alpha = HAT(st, i, i);
     const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
     const double bnext = HAT(st, i + 1, i);
-    double worst = 0.0;
-    for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
-      const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
+    double r = 0.0;
+    if (act) {
       const zc a = zadd(xi, zmk(mp.sign * alpha, 0.0));
-      zc d, phi;
       if (i == 1) {
         d = a;
-        phi = zdiv(zmk(1.0, 0.0), d);
+        const double id = 1.0 / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
+        phi = zmk(cuCreal(d) * id, -cuCimag(d) * id);  // 1 / d
       } else {
-        const zc dprev = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
-        const zc phiprev = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
         const double b = mp.sign * bi;
-        d = zsub(a, zdiv(zmk(b * b, 0.0), dprev));
-        phi = zdiv(zmul(phiprev, zmk(-b, 0.0)), d);
+        // d = a - b^2 / d_prev ; phi = -b phi_prev / d
+        const double ip = (b * b) / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
+        d = zmk(cuCreal(a) - cuCreal(d) * ip, cuCimag(a) + cuCimag(d) * ip);
+        const double id = 1.0 / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
+        const zc num = zmk(-b * cuCreal(phi), -b * cuCimag(phi));
+        phi = zmk((cuCreal(num) * cuCreal(d) + cuCimag(num) * cuCimag(d)) * id,
+                  (cuCimag(num) * cuCreal(d) - cuCreal(num) * cuCimag(d)) * id);
       }
-      mp.d[2 * j] = cuCreal(d);
-      mp.d[2 * j + 1] = cuCimag(d);
-      mp.phi[2 * j] = cuCreal(phi);
-      mp.phi[2 * j + 1] = cuCimag(phi);
-      const double r = bnext * zabs(phi);
+      r = bnext * sqrt(cuCreal(phi) * cuCreal(phi) + cuCimag(phi) * cuCimag(phi));
       mp.resid[j] = r;
-      worst = fmax(worst, r);
     }
-    worst = block_max(worst, red);  // ends with a block barrier: d, phi visible
-    bool stop = false;
+    const double worst = (blockDim.x == 32) ? warp_max(r) : block_max(r, red);
+    const bool stop = worst < mp.eps || last_valid;
     if (threadIdx.x == 0) {
       c->itx = i;
       c->errnum = worst;
       c->errden = 1.0;
-      if (worst < mp.eps || last_valid) {
+      if (stop) {
         c->done = 1;
         c->conv = 1;
         if (st.host_flag) st.host_flag[0] = 1;
       }
     }
-    stop = worst < mp.eps || last_valid;
-    if (stop) return;
+    if (stop || i + 1 == i1) {
+      if (act) {
+        mp.d[2 * j] = cuCreal(d);
+        mp.d[2 * j + 1] = cuCimag(d);
+        mp.phi[2 * j] = cuCreal(phi);
+        mp.phi[2 * j + 1] = cuCimag(phi);
+      }
+      return;
+    }
   }
 }
 
@@ -1401,43 +1416,65 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
   zc* band = Z + (size_t)mp.N * m;          // per shift: d, du, du2, dl (4 m)
   double* g = st.fscratch + 2 * (size_t)mp.N * m + 8 * (size_t)mp.N * m;
   int bad = 0;
+  // One thread per shift: (xi_j I + sign T) z = beta e1 by elimination with
+  // adjacent-row pivoting (the row with the larger squared modulus leads),
+  // the LAPACK ZGTSV scheme.  The active rows live in registers, the next
+  // row of T is read one step ahead, and the finished rows of U (diagonal,
+  // two superdiagonals, right-hand side) go to the band scratch for the back
+  // substitution; a division is one reciprocal of |p|^2 and products.
   for (int j = threadIdx.x; j < mp.N; j += blockDim.x) {
     const zc xi = zmk(mp.xi[2 * j], mp.xi[2 * j + 1]);
-    zc* d = band + (size_t)j * 4 * m;
-    zc* du = d + m;
-    zc* du2 = du + m;
-    zc* dl = du2 + m;
+    zc* U = band + (size_t)j * 4 * m;  // rows of U: u0, u1, u2, rhs
     zc* b = Z + (size_t)j * m;
-    for (int k = 0; k < m; ++k) {
-      d[k] = zadd(xi, zmk(mp.sign * HAT(st, k + 1, k + 1), 0.0));
-      const double off = (k + 1 < m) ? mp.sign * HAT(st, k + 2, k + 1) : 0.0;
-      du[k] = zmk(off, 0.0);
-      dl[k] = zmk(off, 0.0);
-      du2[k] = zmk(0.0, 0.0);
-      b[k] = zmk(k == 0 ? beta : 0.0, 0.0);
-    }
-    for (int k = 0; k < m - 1 && !bad; ++k) {
-      if (zabs(d[k]) < zabs(dl[k])) {
+    auto diag = [&](int k) { return zadd(xi, zmk(mp.sign * HAT(st, k + 1, k + 1), 0.0)); };
+    auto off = [&](int k) { return zmk(k + 1 < m ? mp.sign * HAT(st, k + 2, k + 1) : 0.0, 0.0); };
+    zc a0 = diag(0), a1 = off(0), a2 = zmk(0.0, 0.0), bk = zmk(beta, 0.0);
+    zc q0 = zmk(0.0, 0.0), q1 = q0, q2 = q0, qb = q0;
+    if (m > 1) { q0 = off(0); q1 = diag(1); q2 = off(1); }
+    for (int k = 0; k < m - 1; ++k) {
+      zc n0 = zmk(0.0, 0.0), n1 = n0, n2 = n0;
+      if (k + 2 < m) { n0 = off(k + 1); n1 = diag(k + 2); n2 = off(k + 2); }
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      const double nq = cuCreal(q0) * cuCreal(q0) + cuCimag(q0) * cuCimag(q0);
+      if (na < nq) {
         zc t;
-        t = d[k]; d[k] = dl[k]; dl[k] = t;
-        t = du[k]; du[k] = d[k + 1]; d[k + 1] = t;
-        if (k + 1 < m - 1) { t = du2[k]; du2[k] = du[k + 1]; du[k + 1] = t; }
-        t = b[k]; b[k] = b[k + 1]; b[k + 1] = t;
+        t = a0; a0 = q0; q0 = t;
+        t = a1; a1 = q1; q1 = t;
+        t = a2; a2 = q2; q2 = t;
+        t = bk; bk = qb; qb = t;
       }
-      if (zabs(d[k]) == 0.0) { bad = 1; break; }
-      const zc l = zdiv(dl[k], d[k]);
-      d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
-      if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
-      b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+      const double np = (na < nq) ? nq : na;
+      if (np == 0.0) { bad = 1; break; }
+      const double inv = 1.0 / np;
+      const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
+                       (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
+      U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      a0 = zsub(q1, zmul(l, a1));
+      a1 = zsub(q2, zmul(l, a2));
+      a2 = zmk(0.0, 0.0);
+      bk = zsub(qb, zmul(l, bk));
+      q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
     }
-    if (!bad && zabs(d[m - 1]) == 0.0) bad = 1;
-    if (!bad)
+    if (!bad) {
+      if (cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) bad = 1;
+      U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
+    }
+    if (!bad) {
+      zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);  // solution at k+1, k+2
+      zc u0 = U[4 * (m - 1)], u1 = U[4 * (m - 1) + 1], u2 = U[4 * (m - 1) + 2], ub = U[4 * (m - 1) + 3];
       for (int k = m - 1; k >= 0; --k) {
-        zc s = b[k];
-        if (k + 1 < m) s = zsub(s, zmul(du[k], b[k + 1]));
-        if (k + 2 < m) s = zsub(s, zmul(du2[k], b[k + 2]));
-        b[k] = zdiv(s, d[k]);
+        const zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
+        if (k > 0) { u0 = U[4 * (k - 1)]; u1 = U[4 * (k - 1) + 1]; u2 = U[4 * (k - 1) + 2]; ub = U[4 * (k - 1) + 3]; }
+        const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+        zc sv = zsub(vb, zmul(v1, x1));
+        sv = zsub(sv, zmul(v2, x2));
+        const zc xk = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
+                          (cuCimag(sv) * cuCreal(v0) - cuCreal(sv) * cuCimag(v0)) * inv);
+        b[k] = xk;
+        x2 = x1;
+        x1 = xk;
       }
+    }
   }
   if (__syncthreads_or(bad)) {
     if (threadIdx.x == 0) { c->info = PSFUN_ERR_FROM_SUBROUTINE_NON; atomicOr(&c->err, DEVERR_SINGULAR); }
@@ -1546,7 +1583,7 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
     if (hflag[0]) break;
     const int i1 = std::min(i + kMsChunk, nl + 1);
     PSF_TRY(launch_lz_persist(st, A, i, i1, s));
-    k_ms_monitor<<<1, 256, 0, s>>>(st, mp, i, i1);
+    k_ms_monitor<<<1, std::min(1024, 32 * ((N + 31) / 32)), 0, s>>>(st, mp, i, i1);
     count_launch();
     PSF_CUDA(cudaGetLastError());
     for (long spin = 0; i - hflag[1] > 32 && !hflag[0]; ++spin) {
@@ -1568,7 +1605,7 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
                       const double* x, double* y, double eps, int itmax, int* iter, double* err) {
   if (!a || !xi || !cw) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
-  if (N < 1 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  if (N < 1 || N > 1024 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;  // one monitor thread per shift
   static psfun_krylov* meth = nullptr;
   if (!meth) meth = new psfun_krylov();
   static DevBuf msbuf;
