@@ -77,21 +77,15 @@ struct BatchArgs {
   unsigned* bar;    // [0] count, [1] gen
   int* err;
   unsigned* active; // instances still running
+  const int* tile_inst;  // instance of every global tile
 };
 
 PSF_DEVINL double* pa(const BInst& I, int q, int which, int nl) {
   return I.scal + ((size_t)q * PA_N + which) * (size_t)(nl + 2);
 }
 
-// Instance of a global tile (binary search on tile_begin).
-PSF_DEVINL int find_inst(const BatchArgs& B, int g) {
-  int lo = 0, hi = B.count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (B.inst[mid].tile_begin <= g) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
+// Instance of a global tile (a map built on the host: one load).
+PSF_DEVINL int find_inst(const BatchArgs& B, int g) { return B.tile_inst[g]; }
 
 // ---- CRAM on the tridiagonal t*T(1:m): y = exp(t T) e1 (dnchbv.f:54-69 rule,
 // banded GEPP per pole, one thread per pole).
@@ -169,7 +163,8 @@ enum { PH_INIT = 0, PH_SPMM = 1, PH_UPDATE = 2, PH_RECOMB = 3 };
 
 // Row-level work of one tile for phase `ph`; returns the R partial sums.
 template <int R>
-PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs& B, SpmvSmem& sm, double* accR) {
+PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs& B, SpmvSmem& sm, double* accR,
+                          int bufi) {
   const TileInfo ti = tile_info(I.A, lt);
   const int nr = ti.r1 - ti.r0;
   if (ph == PH_INIT) {
@@ -209,14 +204,14 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
       }
       return;
     }
-    if (threadIdx.x == 0) spmv_issue(I.A, ti, sm, 0);
-    const bool ok = mbar_wait(&sm.bar[0], sm.phase[0]);
+    // the caller staged the tile into buf[bufi] (stage_tile)
+    const bool ok = mbar_wait(&sm.bar[bufi], sm.phase[bufi]);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicOr(B.err, DEVERR_TIMEOUT);
-      mbar_wait(&sm.bar[0], sm.phase[0]);
+      mbar_wait(&sm.bar[bufi], sm.phase[bufi]);
       return;
     }
-    const SpmvTile& tb = sm.buf[0];
+    const SpmvTile& tb = sm.buf[bufi];
     const int dj = ti.kv0 - ti.kj0, di = ti.r0 - ti.ki0;
     if (I.mapping == 0) {  // one thread per row, R accumulators
       for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
@@ -224,20 +219,37 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
         double s[R];
 #pragma unroll
         for (int q = 0; q < R; ++q) s[q] = 0.0;
-        for (int k = kb; k < ke; ++k) {
+        // four entries' gathers in flight before their FMAs (entry order kept)
+        int k = kb;
+        for (; k + 4 <= ke; k += 4) {
+          double a[4], xv[4][R];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            a[e] = tb.val[k + e];
+            const double* xr = wi + (size_t)tb.ja[k + e + dj] * R;
+            if (R == 4) {
+              const double2 x01 = __ldg(reinterpret_cast<const double2*>(xr));
+              const double2 x23 = __ldg(reinterpret_cast<const double2*>(xr) + 1);
+              xv[e][0] = x01.x;
+              xv[e][1 % R] = x01.y;
+              xv[e][2 % R] = x23.x;
+              xv[e][3 % R] = x23.y;
+            } else {
+#pragma unroll
+              for (int q = 0; q < R; ++q) xv[e][q] = __ldg(xr + q);
+            }
+          }
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+#pragma unroll
+            for (int q = 0; q < R; ++q) s[q] = fma(a[e], xv[e][q], s[q]);
+          }
+        }
+        for (; k < ke; ++k) {
           const double a = tb.val[k];
           const double* xr = wi + (size_t)tb.ja[k + dj] * R;
-          if (R == 4) {
-            const double2 x01 = __ldg(reinterpret_cast<const double2*>(xr));
-            const double2 x23 = __ldg(reinterpret_cast<const double2*>(xr) + 1);
-            s[0] = fma(a, x01.x, s[0]);
-            s[1] = fma(a, x01.y, s[1]);
-            s[2 % R] = fma(a, x23.x, s[2 % R]);
-            s[3 % R] = fma(a, x23.y, s[3 % R]);
-          } else {
 #pragma unroll
-            for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
-          }
+          for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
         }
         const int r = ti.r0 + lr;
 #pragma unroll
@@ -251,7 +263,18 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
         const int lr = task / R, q = task - lr * R;
         const int kb = tb.irp[lr + di] - ti.kv0, ke = tb.irp[lr + di + 1] - ti.kv0;
         double s = 0.0;
-        for (int k = kb; k < ke; ++k) s = fma(tb.val[k], __ldg(wi + (size_t)tb.ja[k + dj] * R + q), s);
+        int k = kb;
+        for (; k + 4 <= ke; k += 4) {
+          double a[4], xv[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            a[e] = tb.val[k + e];
+            xv[e] = __ldg(wi + (size_t)tb.ja[k + e + dj] * R + q);
+          }
+#pragma unroll
+          for (int e = 0; e < 4; ++e) s = fma(a[e], xv[e], s);
+        }
+        for (; k < ke; ++k) s = fma(tb.val[k], __ldg(wi + (size_t)tb.ja[k + dj] * R + q), s);
         const int r = ti.r0 + lr;
         I.u[(size_t)r * R + q] = s;
         const double pv = s * wi[(size_t)r * R + q];
@@ -261,7 +284,7 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
           if (qq == q) accR[qq] += pv;
       }
     }
-    if (threadIdx.x == 0) sm.phase[0] ^= 1u;
+    if (threadIdx.x == 0) sm.phase[bufi] ^= 1u;
     return;
   }
   if (ph == PH_UPDATE) {
@@ -459,53 +482,218 @@ PSF_DEVINL void final_pairs(const BInst& I, const BatchArgs& B, double* red) {
   __syncthreads();
 }
 
+// Thread 0: stage tile lt of instance I into buf[bufi] for the SpMM phase
+// (a tile that is one long row is read from global memory instead).
+PSF_DEVINL bool tile_staged(const BInst& I, int lt) {
+  const TileInfo ti = tile_info(I.A, lt);
+  return ti.k1 - ti.k0 <= kTileNnz;
+}
+
+// Sums of the R per-thread values over the block, for thread 0: each warp's
+// butterfly, then the warps in order.  red holds 16 * R doubles; it is
+// rewritten only after the caller's next block barrier.
 template <int R>
-PSF_DEVINL bool run_phase(const BatchArgs& B, int ph, int i, unsigned* qctr, SpmvSmem& sm) {
-  __shared__ int g_sh, last_sh, skip_sh;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      // -1 drains the queue after a device error; decided once per block
-      g_sh = (*(volatile int*)B.err != 0) ? -1 : (int)atomicAdd(qctr, 1u);
-      skip_sh = 0;
-      if (g_sh >= 0 && g_sh < B.total_tiles && ph != PH_INIT && ph != PH_RECOMB)
-        skip_sh = (*(volatile unsigned*)&B.inst[find_inst(B, g_sh)].cnt[1] == 0u);
-    }
-    __syncthreads();
-    const int g = g_sh;
-    const bool skip = skip_sh != 0;
-    __syncthreads();
-    if (g < 0 || g >= B.total_tiles) break;
-    const int k = find_inst(B, g);
-    const BInst& I = B.inst[k];
-    const int lt = g - I.tile_begin;
-    double accR[R];
+PSF_DEVINL void block_sum_R(const double* acc, double* red, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) accR[q] = 0.0;
-    if (!skip) tile_work<R>(I, ph, i, lt, B, sm, accR);
-    if (ph == PH_RECOMB) { __syncthreads(); continue; }
+  for (int q = 0; q < R; ++q) v[q] = acc[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) red[wid * R + q] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-      const double v = block_sum(accR[q], sm.red);
-      if (threadIdx.x == 0) I.part[((size_t)((ph == PH_UPDATE) ? 1 : 0) * I.ntiles + lt) * R + q] = v;
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += red[w * R + q];
+      out[q] = t;
     }
-    if (threadIdx.x == 0) {
-      __threadfence();
-      last_sh = (atomicAdd(&I.cnt[0], 1u) == (unsigned)I.ntiles - 1);
+  }
+}
+
+// The update phase over rows [rb, re) of instance I (whole runs of tiles):
+// W_{i+1} = 2^k (u - alpha W_i - c W_{i-1}) for the live pairs, the norms'
+// partial sums in accR; several rows per thread in flight.
+template <int R>
+PSF_DEVINL void update_rows(const BInst& I, int i, int rb, int re, const BatchArgs& B, double* accR) {
+  const double* __restrict__ wi = I.V + (size_t)(i - 1) * I.ldv;
+  const double* __restrict__ wm = (i >= 2) ? I.V + (size_t)(i - 2) * I.ldv : wi;
+  double* __restrict__ wo = I.V + (size_t)i * I.ldv;
+  double c1[R], c2[R];
+  int k2[R];
+  bool live[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const double sc = pa(I, q, PA_S, B.nl)[i];
+    c1[q] = pa(I, q, PA_ALPHA, B.nl)[i];
+    c2[q] = (i >= 2) ? pa(I, q, PA_BETA, B.nl)[i] * pa(I, q, PA_S, B.nl)[i - 1] / sc : 0.0;
+    k2[q] = ilog2_normal(sc);
+    live[q] = !I.ps[q].done;
+  }
+  const int bd = blockDim.x;
+  constexpr int NR = (R >= 3) ? 2 : 4;  // rows per thread in flight (registers)
+  int lr = rb + (int)threadIdx.x;
+  for (; lr + (NR - 1) * bd < re; lr += NR * bd) {
+    double uu[NR][R], a[NR][R], b[NR][R];
+#pragma unroll
+    for (int e = 0; e < NR; ++e) {
+      const size_t r = (size_t)(lr + e * bd) * R;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        uu[e][q] = I.u[r + q];
+        a[e][q] = wi[r + q];
+        b[e][q] = wm[r + q];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < NR; ++e) {
+      const size_t r = (size_t)(lr + e * bd) * R;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        if (!live[q]) continue;
+        const double w = fma(-c2[q], b[e][q], fma(-c1[q], a[e][q], uu[e][q]));
+        accR[q] = fma(w, w, accR[q]);
+        wo[r + q] = scale_pow2(w, k2[q]);
+      }
+    }
+  }
+  for (; lr < re; lr += bd) {
+    const size_t r = (size_t)lr * R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      if (!live[q]) continue;
+      const double w = fma(-c2[q], wm[r + q], fma(-c1[q], wi[r + q], I.u[r + q]));
+      accR[q] = fma(w, w, accR[q]);
+      wo[r + q] = scale_pow2(w, k2[q]);
+    }
+  }
+}
+
+constexpr int kBatchChunk = 4;  // queue tiles taken per grab
+
+// One phase over the global tile queue.  A block takes kBatchChunk
+// consecutive tiles per grab; in the SpMM phase the next tile of the chunk is
+// staged by TMA into the other buffer while the current one is computed.
+// The tiles of each instance in the chunk are counted with one atomic; the
+// block that completes an instance finalises it.
+template <int R>
+PSF_DEVINL bool run_phase(const BatchArgs& B, int ph, int i, unsigned* qctr, SpmvSmem& sm) {
+  __shared__ int g0_sh, last_sh;
+  __shared__ int inst_sh[kBatchChunk];
+  __shared__ unsigned char skip_sh[kBatchChunk], staged_sh[kBatchChunk];
+  __shared__ double redR[16 * kBatchMaxRhs];
+  for (;;) {
+    if (threadIdx.x < 32) {
+      // -1 drains the queue after a device error; decided once per block.
+      // Lanes 0..kBatchChunk-1 look up one tile each, in parallel.
+      int g0 = 0;
+      if (threadIdx.x == 0) g0 = (*(volatile int*)B.err != 0) ? -1 : (int)atomicAdd(qctr, (unsigned)kBatchChunk);
+      g0 = __shfl_sync(0xffffffffu, g0, 0);
+      const int c = threadIdx.x;
+      if (c == 0) g0_sh = g0;
+      if (g0 >= 0 && c < kBatchChunk && g0 + c < B.total_tiles) {
+        const int g = g0 + c;
+        const int k = find_inst(B, g);
+        inst_sh[c] = k;
+        const BInst& I = B.inst[k];
+        const bool skip = (ph != PH_INIT && ph != PH_RECOMB) && (*(volatile unsigned*)&I.cnt[1] == 0u);
+        skip_sh[c] = skip;
+        const bool st = (ph == PH_SPMM && !skip && tile_staged(I, g - I.tile_begin));
+        staged_sh[c] = st;
+        if (c == 0 && st) spmv_issue(I.A, tile_info(I.A, g - I.tile_begin), sm, 0);
+      }
     }
     __syncthreads();
-    if (last_sh) {
-      __threadfence();
-      if (threadIdx.x == 0) I.cnt[0] = 0u;
-      if (!skip) finalize<R>(I, ph, i, B, sm.red);
-      __threadfence();
+    const int g0 = g0_sh;
+    if (g0 < 0 || g0 >= B.total_tiles) break;
+    const int nc = min(B.total_tiles, g0 + kBatchChunk) - g0;
+    // runs of consecutive tiles of one instance (chunk boundaries are fixed
+    // multiples of kBatchChunk, so the runs and their partial slots are the
+    // same whichever block takes the chunk)
+    for (int c = 0; c < nc;) {
+      const int k = inst_sh[c];
+      int ce = c + 1;
+      while (ce < nc && inst_sh[ce] == k) ++ce;
+      const BInst& I = B.inst[k];
+      const bool skip = skip_sh[c] != 0;
+      const size_t pslot = (size_t)((ph == PH_UPDATE) ? 1 : 0) * I.ntiles;
+      if (ph == PH_UPDATE) {
+        // the whole run at once; its partial in the slot of its first tile
+        const int lt0 = g0 + c - I.tile_begin, lt1 = g0 + ce - I.tile_begin;
+        double accR[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) accR[q] = 0.0;
+        if (!skip) update_rows<R>(I, i, I.A.tile_desc[lt0].x, I.A.tile_desc[lt1].x, B, accR);
+        double tot[R];
+        block_sum_R<R>(accR, redR, tot);
+        if (threadIdx.x == 0) {
+          for (int lt = lt0; lt < lt1; ++lt) {
+            double* part = I.part + (pslot + lt) * R;
+#pragma unroll
+            for (int q = 0; q < R; ++q) part[q] = (lt == lt0) ? tot[q] : 0.0;
+          }
+        }
+      } else {
+        // tile by tile (the SpMM stages each tile, double-buffered), the
+        // run's partial summed once, in the slot of its first tile
+        double accR[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) accR[q] = 0.0;
+        for (int cc = c; cc < ce; ++cc) {
+          const int g = g0 + cc, b = cc & 1;
+          const int lt = g - I.tile_begin;
+          if (threadIdx.x == 0 && cc + 1 < nc && staged_sh[cc + 1]) {
+            const BInst& In = B.inst[inst_sh[cc + 1]];
+            spmv_issue(In.A, tile_info(In.A, g + 1 - In.tile_begin), sm, b ^ 1);
+          }
+          if (!skip) tile_work<R>(I, ph, i, lt, B, sm, accR, b);
+          __syncthreads();  // the tile's buffer is free for the next prefetch
+        }
+        if (ph != PH_RECOMB) {
+          const int lt0 = g0 + c - I.tile_begin, lt1 = g0 + ce - I.tile_begin;
+          double tot[R];
+          block_sum_R<R>(accR, redR, tot);
+          if (threadIdx.x == 0) {
+            for (int lt = lt0; lt < lt1; ++lt) {
+              double* part = I.part + (pslot + lt) * R;
+#pragma unroll
+              for (int q = 0; q < R; ++q) part[q] = (lt == lt0) ? tot[q] : 0.0;
+            }
+          }
+        }
+      }
+      if (ph != PH_RECOMB) {
+        // the run's tiles are counted at once; the block completing the
+        // instance finalises it
+        if (threadIdx.x == 0) {
+          __threadfence();
+          last_sh = (atomicAdd(&I.cnt[0], (unsigned)(ce - c)) + (unsigned)(ce - c) == (unsigned)I.ntiles);
+        }
+        __syncthreads();
+        if (last_sh) {
+          __threadfence();
+          if (threadIdx.x == 0) I.cnt[0] = 0u;
+          if (!skip) finalize<R>(I, ph, i, B, sm.red);
+          __threadfence();
+        }
+      }
+      __syncthreads();
+      c = ce;
     }
-    __syncthreads();
   }
   return true;
 }
 
 template <int R>
-__global__ void __launch_bounds__(kBatchThreads) k_batch(BatchArgs B) {
+__global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs B) {
   PSF_SPMV_SMEM();
   spmv_smem_init(sm);
   int ph_idx = 0;
@@ -539,7 +727,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_spmm_probe(BatchArgs B,
   double accR[R];
   for (int lt = blockIdx.x; lt < I.ntiles; lt += gridDim.x) {
     for (int q = 0; q < R; ++q) accR[q] = 0.0;
-    tile_work<R>(I, PH_SPMM, 1, lt, B, sm, accR);
+    if (threadIdx.x == 0 && tile_staged(I, lt)) spmv_issue(I.A, tile_info(I.A, lt), sm, 0);
+    tile_work<R>(I, PH_SPMM, 1, lt, B, sm, accR, 0);
     __syncthreads();
   }
 }
@@ -700,6 +889,7 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
   const size_t oInst = carve((sizeof(BInst) * count + 7) / 8);
   const size_t oQ = carve(2 * (size_t)nl + 8);
   const size_t oMisc = carve(8);
+  const size_t oTI = carve(((size_t)tiles + 1) / 2);
   DevBuf& ws = meth->scratch;  // reuse the handle's scratch for the batch
   PSF_TRY(ws.ensure(sizeof(double) * off));
   double* base = ws.as<double>();
@@ -722,6 +912,11 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
   BInst* dinst = reinterpret_cast<BInst*>(base + oInst);
   PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * count, cudaMemcpyHostToDevice, s));
   unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
+  std::vector<int> tile_inst((size_t)std::max(tiles, 1));
+  for (int k = 0; k < count; ++k)
+    for (int t = 0; t < hinst[k].ntiles; ++t) tile_inst[(size_t)hinst[k].tile_begin + t] = k;
+  int* dti = reinterpret_cast<int*>(base + oTI);
+  PSF_CUDA(cudaMemcpyAsync(dti, tile_inst.data(), sizeof(int) * (size_t)tiles, cudaMemcpyHostToDevice, s));
   BatchArgs B;
   B.inst = dinst;
   B.count = count;
@@ -734,6 +929,7 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
   B.bar = misc;
   B.err = reinterpret_cast<int*>(misc + 2);
   B.active = misc + 3;
+  B.tile_inst = dti;
   const unsigned active = (unsigned)count;
   PSF_CUDA(cudaMemcpyAsync(B.active, &active, sizeof active, cudaMemcpyHostToDevice, s));
   int rc;
