@@ -78,6 +78,7 @@ struct BatchArgs {
   int* err;
   unsigned* active; // instances still running
   const int* tile_inst;  // instance of every global tile
+  int chunk;             // tiles per queue grab (1..kBatchChunkMax)
 };
 
 PSF_DEVINL double* pa(const BInst& I, int q, int which, int nl) {
@@ -577,9 +578,9 @@ PSF_DEVINL void update_rows(const BInst& I, int i, int rb, int re, const BatchAr
   }
 }
 
-constexpr int kBatchChunk = 4;  // queue tiles taken per grab
+constexpr int kBatchChunkMax = 16;  // queue tiles taken per grab, at most (B.chunk)
 
-// One phase over the global tile queue.  A block takes kBatchChunk
+// One phase over the global tile queue.  A block takes B.chunk
 // consecutive tiles per grab; in the SpMM phase the next tile of the chunk is
 // staged by TMA into the other buffer while the current one is computed.
 // The tiles of each instance in the chunk are counted with one atomic; the
@@ -587,19 +588,19 @@ constexpr int kBatchChunk = 4;  // queue tiles taken per grab
 template <int R>
 PSF_DEVINL bool run_phase(const BatchArgs& B, int ph, int i, unsigned* qctr, SpmvSmem& sm) {
   __shared__ int g0_sh, last_sh;
-  __shared__ int inst_sh[kBatchChunk];
-  __shared__ unsigned char skip_sh[kBatchChunk], staged_sh[kBatchChunk];
+  __shared__ int inst_sh[kBatchChunkMax];
+  __shared__ unsigned char skip_sh[kBatchChunkMax], staged_sh[kBatchChunkMax];
   __shared__ double redR[16 * kBatchMaxRhs];
   for (;;) {
     if (threadIdx.x < 32) {
       // -1 drains the queue after a device error; decided once per block.
-      // Lanes 0..kBatchChunk-1 look up one tile each, in parallel.
+      // Lanes 0..B.chunk-1 look up one tile each, in parallel.
       int g0 = 0;
-      if (threadIdx.x == 0) g0 = (*(volatile int*)B.err != 0) ? -1 : (int)atomicAdd(qctr, (unsigned)kBatchChunk);
+      if (threadIdx.x == 0) g0 = (*(volatile int*)B.err != 0) ? -1 : (int)atomicAdd(qctr, (unsigned)B.chunk);
       g0 = __shfl_sync(0xffffffffu, g0, 0);
       const int c = threadIdx.x;
       if (c == 0) g0_sh = g0;
-      if (g0 >= 0 && c < kBatchChunk && g0 + c < B.total_tiles) {
+      if (g0 >= 0 && c < B.chunk && g0 + c < B.total_tiles) {
         const int g = g0 + c;
         const int k = find_inst(B, g);
         inst_sh[c] = k;
@@ -614,9 +615,9 @@ PSF_DEVINL bool run_phase(const BatchArgs& B, int ph, int i, unsigned* qctr, Spm
     __syncthreads();
     const int g0 = g0_sh;
     if (g0 < 0 || g0 >= B.total_tiles) break;
-    const int nc = min(B.total_tiles, g0 + kBatchChunk) - g0;
+    const int nc = min(B.total_tiles, g0 + B.chunk) - g0;
     // runs of consecutive tiles of one instance (chunk boundaries are fixed
-    // multiples of kBatchChunk, so the runs and their partial slots are the
+    // multiples of B.chunk, so the runs and their partial slots are the
     // same whichever block takes the chunk)
     for (int c = 0; c < nc;) {
       const int k = inst_sh[c];
@@ -813,6 +814,9 @@ static int batch_launch(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, c
   if (per < 1) per = 1;
   int G = sm_count() * per;
   if (G > B.total_tiles) G = std::max(1, B.total_tiles);
+  // about four grabs per block and phase, at most kBatchChunkMax tiles each:
+  // larger grabs amortise the queue and per-run costs, smaller ones balance
+  B.chunk = std::max(1, std::min(kBatchChunkMax, B.total_tiles / (4 * G)));
   void* args[] = {(void*)&B};
   PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_batch<R>, dim3(G), dim3(kBatchThreads), args, kSpmvSmemBytes, s));
   count_launch();
