@@ -89,42 +89,60 @@ PSF_DEVINL double* pa(const BInst& I, int q, int which, int nl) {
 PSF_DEVINL int find_inst(const BatchArgs& B, int g) { return B.tile_inst[g]; }
 
 // ---- CRAM on the tridiagonal t*T(1:m): y = exp(t T) e1 (dnchbv.f:54-69 rule,
-// banded GEPP per pole, one thread per pole).
+// banded GEPP per pole with adjacent-row pivoting, one thread per pole).  The
+// active rows live in registers and the next row of T is read one step
+// ahead; the finished rows of U (u0, u1, u2, rhs) go to `band` (4 m complex)
+// for the back substitution, the solution to b.  Magnitudes are compared
+// squared and a division is one reciprocal of |p|^2 and products.
 PSF_DEVINL void cram_pole_tridiag(int m, double t, const double* alpha, const double* beta, int p, zc* band,
                                   zc* b, int* bad) {
   const zc theta = zmk(kCramTheta[p][0], kCramTheta[p][1]);
-  zc* d = band;
-  zc* du = d + m;
-  zc* du2 = du + m;
-  zc* dl = du2 + m;
-  for (int i = 0; i < m; ++i) {
-    d[i] = zsub(zmk(-t * alpha[i + 1], 0.0), theta);  // alpha is 1-based
-    const double off = (i + 1 < m) ? -t * beta[i + 2] : 0.0;  // beta[i+2] = T(i+2,i+1)
-    du[i] = zmk(off, 0.0);
-    dl[i] = zmk(off, 0.0);
-    du2[i] = zmk(0.0, 0.0);
-    b[i] = zmk(i == 0 ? 1.0 : 0.0, 0.0);
-  }
+  zc* U = band;
+  // alpha is 1-based; beta[i+2] = T(i+2,i+1)
+  auto diag = [&](int i) { return zsub(zmk(-t * alpha[i + 1], 0.0), theta); };
+  auto off = [&](int i) { return zmk(i + 1 < m ? -t * beta[i + 2] : 0.0, 0.0); };
+  zc a0 = diag(0), a1 = off(0), a2 = zmk(0.0, 0.0), bk = zmk(1.0, 0.0);
+  zc q0 = zmk(0.0, 0.0), q1 = q0, q2 = q0, qb = q0;
+  if (m > 1) { q0 = off(0); q1 = diag(1); q2 = off(1); }
   for (int k = 0; k < m - 1; ++k) {
-    if (zabs(d[k]) < zabs(dl[k])) {
+    zc n0 = zmk(0.0, 0.0), n1 = n0, n2 = n0;
+    if (k + 2 < m) { n0 = off(k + 1); n1 = diag(k + 2); n2 = off(k + 2); }
+    const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+    const double nq = cuCreal(q0) * cuCreal(q0) + cuCimag(q0) * cuCimag(q0);
+    if (na < nq) {
       zc tt;
-      tt = d[k]; d[k] = dl[k]; dl[k] = tt;
-      tt = du[k]; du[k] = d[k + 1]; d[k + 1] = tt;
-      if (k + 1 < m - 1) { tt = du2[k]; du2[k] = du[k + 1]; du[k + 1] = tt; }
-      tt = b[k]; b[k] = b[k + 1]; b[k + 1] = tt;
+      tt = a0; a0 = q0; q0 = tt;
+      tt = a1; a1 = q1; q1 = tt;
+      tt = a2; a2 = q2; q2 = tt;
+      tt = bk; bk = qb; qb = tt;
     }
-    if (zabs(d[k]) == 0.0) { *bad = 1; return; }
-    const zc l = zdiv(dl[k], d[k]);
-    d[k + 1] = zsub(d[k + 1], zmul(l, du[k]));
-    if (k + 1 < m - 1) du[k + 1] = zsub(du[k + 1], zmul(l, du2[k]));
-    b[k + 1] = zsub(b[k + 1], zmul(l, b[k]));
+    const double np = (na < nq) ? nq : na;
+    if (np == 0.0) { *bad = 1; return; }
+    const double inv = 1.0 / np;
+    const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
+                     (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
+    U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+    a0 = zsub(q1, zmul(l, a1));
+    a1 = zsub(q2, zmul(l, a2));
+    a2 = zmk(0.0, 0.0);
+    bk = zsub(qb, zmul(l, bk));
+    q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
   }
-  if (zabs(d[m - 1]) == 0.0) { *bad = 1; return; }
+  if (cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) { *bad = 1; return; }
+  U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
+  zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);  // solution at i+1, i+2
+  zc u0 = U[4 * (m - 1)], u1 = U[4 * (m - 1) + 1], u2 = U[4 * (m - 1) + 2], ub = U[4 * (m - 1) + 3];
   for (int i = m - 1; i >= 0; --i) {
-    zc s = b[i];
-    if (i + 1 < m) s = zsub(s, zmul(du[i], b[i + 1]));
-    if (i + 2 < m) s = zsub(s, zmul(du2[i], b[i + 2]));
-    b[i] = zdiv(s, d[i]);
+    const zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
+    if (i > 0) { u0 = U[4 * (i - 1)]; u1 = U[4 * (i - 1) + 1]; u2 = U[4 * (i - 1) + 2]; ub = U[4 * (i - 1) + 3]; }
+    const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+    zc sv = zsub(vb, zmul(v1, x1));
+    sv = zsub(sv, zmul(v2, x2));
+    const zc xi = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
+                      (cuCimag(sv) * cuCreal(v0) - cuCreal(sv) * cuCimag(v0)) * inv);
+    b[i] = xi;
+    x2 = x1;
+    x1 = xi;
   }
 }
 
