@@ -1330,6 +1330,8 @@ struct MsParams {
   double* d;      // 2N: LDL pivots of the last step
   double* phi;    // 2N
   double* resid;  // N
+  int* mon;       // [0]: the monitor's last step (its own word: the monitor
+                  // of one chunk runs while the next chunk's Lanczos steps do)
 };
 
 // Shifted residuals of Lanczos steps i0..i1-1 (in order; each step's LDL^T
@@ -1380,7 +1382,7 @@ __global__ void k_ms_monitor(KState st, MsParams mp, int i0, int i1) {
     const double worst = (blockDim.x == 32) ? warp_max(r) : block_max(r, red);
     const bool stop = worst < mp.eps || last_valid;
     if (threadIdx.x == 0) {
-      c->itx = i;
+      mp.mon[0] = i;
       c->errnum = worst;
       c->errden = 1.0;
       if (stop) {
@@ -1410,7 +1412,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
     if (threadIdx.x == 0) c->nterms = 0;
     return;
   }
-  const int m = c->itx;
+  const int m = mp.mon[0];
   const double beta = c->beta0;
   zc* Z = (zc*)st.fscratch;                 // N * m solutions
   zc* band = Z + (size_t)mp.N * m;          // per shift: d, du, du2, dl (4 m)
@@ -1520,7 +1522,7 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   const int64_t n = a->n;
   const int nl = itmax;
   PSF_TRY(ensure_workspace(ws, n, nl, 1));
-  PSF_TRY(msbuf.ensure(sizeof(double) * (4 * (size_t)N + 4 * (size_t)N + N) + 256));
+  PSF_TRY(msbuf.ensure(sizeof(double) * (4 * (size_t)N + 4 * (size_t)N + N) + 256 + 64));
   cudaStream_t s = stream();
   double* mb = msbuf.as<double>();
   MsParams& mp = out->mp;
@@ -1530,6 +1532,7 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   mp.d = mb + 4 * N;
   mp.phi = mb + 6 * N;
   mp.resid = mb + 8 * N;
+  mp.mon = reinterpret_cast<int*>(mb + 9 * N + 32);
   mp.sign = sign;
   mp.eta = 0.0;
   mp.eps = eps;
@@ -1579,11 +1582,32 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   // launch, followed by the shifted-residual monitor of the chunk; at most
   // kMsChunk - 1 steps run past convergence.
   constexpr int kMsChunk = 8;
+  constexpr int kMsOverlapFrom = 32;
+  // Past the first kMsOverlapFrom steps, the monitor of a chunk runs on a
+  // second stream, concurrently with the next chunk's Lanczos steps (it reads
+  // only the chunk's T entries and writes its own words); one more chunk may
+  // then run past convergence, which only long solves can afford.
+  static cudaStream_t s2 = nullptr;
+  static cudaEvent_t ev_lz = nullptr, ev_mon = nullptr;
+  if (!s2) {
+    PSF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    PSF_CUDA(cudaEventCreateWithFlags(&ev_lz, cudaEventDisableTiming));
+    PSF_CUDA(cudaEventCreateWithFlags(&ev_mon, cudaEventDisableTiming));
+  }
+  PSF_CUDA(cudaMemsetAsync(mp.mon, 0, sizeof(int), s));
+  PSF_CUDA(cudaEventRecord(ev_lz, s));
+  PSF_CUDA(cudaStreamWaitEvent(s2, ev_lz, 0));  // the monitor stream starts after the setup
   for (int i = 1; i <= nl; i += kMsChunk) {
     if (hflag[0]) break;
     const int i1 = std::min(i + kMsChunk, nl + 1);
     PSF_TRY(launch_lz_persist(st, A, i, i1, s));
-    k_ms_monitor<<<1, std::min(1024, 32 * ((N + 31) / 32)), 0, s>>>(st, mp, i, i1);
+    cudaStream_t smon = s;
+    if (i > kMsOverlapFrom) {
+      PSF_CUDA(cudaEventRecord(ev_lz, s));
+      PSF_CUDA(cudaStreamWaitEvent(s2, ev_lz, 0));
+      smon = s2;
+    }
+    k_ms_monitor<<<1, std::min(1024, 32 * ((N + 31) / 32)), 0, smon>>>(st, mp, i, i1);
     count_launch();
     PSF_CUDA(cudaGetLastError());
     for (long spin = 0; i - hflag[1] > 32 && !hflag[0]; ++spin) {
@@ -1591,12 +1615,16 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
       if (spin > 200000000L) break;
     }
   }
+  PSF_CUDA(cudaEventRecord(ev_mon, s2));
+  PSF_CUDA(cudaStreamWaitEvent(s, ev_mon, 0));  // everything after waits for the last monitor
   KCtrl hc;
+  int hmon = 0;
   PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaMemcpyAsync(&hmon, mp.mon, sizeof(int), cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
   if (hc.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
   if (hc.info != 0) return hc.info;
-  out->m = hc.itx;
+  out->m = hmon;
   out->err = hc.errnum;
   return PSFUN_SUCCESS;
 }
@@ -1629,7 +1657,7 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   PSF_CUDA(cudaStreamSynchronize(s));
   if (hc.err & DEVERR_TIMEOUT) return PSFUN_ERR_DEVICE_TIMEOUT;
   if (hc.info != 0) return hc.info;
-  if (iter) *iter = hc.itx;
+  if (iter) *iter = run.m;
   if (err) *err = hc.errnum;
   return PSFUN_SUCCESS;
 }
