@@ -580,6 +580,10 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
 __device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps, int tridiag, DenseSmem& sm) {
   KCtrl* c = st.ctrl;
   if (c->done) return;
+  // Lanczos: a breakdown found at the end of step i-1 ends the iteration
+  // before this estimate (psfun_d_lanczos.f90:225-230), whether or not step
+  // i's kernel has already stopped the solve
+  if (tridiag && c->breakdown) return;
   const int m = i - 1;
   const int rc = fh_apply_cta(fp, m, st.H, st.ldh, st.e1, st.yk, st.fscratch, tridiag != 0, sm);
   if (rc) {
@@ -682,7 +686,9 @@ __device__ void final_body(KState& st, const FunParams& fp, int tridiag, int kee
     return;
   }
   const int conv = c->conv;
-  const int itx = c->itx;
+  // on convergence the estimate's yk_len (= its itx); a Lanczos step running
+  // beside the estimate may write itx as well
+  const int itx = conv ? c->yk_len : c->itx;
   int yk_len;
   if (!conv) {
     const int m = final_dim(c, arnoldi);
@@ -1149,10 +1155,35 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       PSF_CUDA(cudaStreamSynchronize(s));
     }
     const int max_ahead = 24;
+    // Lanczos with a one-block estimate: the estimate of iteration i needs
+    // only T(1:i-1) and beta_i, so it runs on a second stream while step i's
+    // Lanczos kernel runs (on the SM that kernel leaves free), and step i+1
+    // waits for it.  Step i was computed before the estimate in any case.
+    static cudaStream_t s2 = nullptr;
+    static cudaEvent_t ev_step = nullptr, ev_est = nullptr;
+    const bool overlap = istop == 1 && !arnoldi && !sai && !userf && dense_blocks(fpk, nl + 1, tridiag != 0) == 1;
+    if (overlap && !s2) {
+      PSF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      PSF_CUDA(cudaEventCreateWithFlags(&ev_step, cudaEventDisableTiming));
+      PSF_CUDA(cudaEventCreateWithFlags(&ev_est, cudaEventDisableTiming));
+    }
     for (int i = 2; i <= nl; ++i) {
       if ((istop == 1 || sai) && hflag[0]) break;
-      PSF_TRY(enqueue_step(i));
-      if (istop == 1) {
+      if (overlap) {
+        PSF_CUDA(cudaEventRecord(ev_step, s));  // steps 1..i-1 are done
+        PSF_CUDA(cudaStreamWaitEvent(s2, ev_step, 0));
+        int ii = i, td = tridiag;
+        double e = eps;
+        DenseGroup* g = nullptr;
+        void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&td, (void*)&g};
+        PSF_TRY(launch_dense((const void*)k_estimate, 1, meth->dgroup.as<DenseGroup>(), &g, args, s2));
+        PSF_CUDA(cudaEventRecord(ev_est, s2));
+        PSF_TRY(enqueue_step(i));
+        PSF_CUDA(cudaStreamWaitEvent(s, ev_est, 0));  // step i+1 sees the verdict
+      } else {
+        PSF_TRY(enqueue_step(i));
+      }
+      if (istop == 1 && !overlap) {
         if (sai) {
           {
             double tau = meth->tau;
@@ -1218,6 +1249,9 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     return PSFUN_ERR_DEVICE_TIMEOUT;
   }
   if (hc.info != 0) return hc.info;
+  // on convergence the estimate's own word (a Lanczos step running beside the
+  // estimate may have written itx too)
+  hc.itx = hc.conv ? hc.yk_len : hc.itx;
   if (iter) *iter = hc.itx;
   if (err) *err = hc.derr;
   if (res) {
