@@ -33,9 +33,11 @@ extern "C" {
 /* ---- status codes: PSBLAS psb_const_mod values used by the reference ---- */
 /* Concurrency: the library keeps per-process state (the current stream set by
  * psfun_gpu_set_stream, workspaces cached per handle and per entry point,
- * mapped progress flags).  Calls must not overlap: call it from one host
- * thread at a time, as the reference's procedures are called by one thread
- * per MPI rank. */
+ * mapped progress flags, a second stream and events for overlapped
+ * monitors).  Calls must not overlap: call it from one host thread at a
+ * time, as the reference's procedures are called by one thread per MPI
+ * rank, and use one device per process (the device current at the first
+ * call). */
 
 #define PSFUN_SUCCESS 0
 #define PSFUN_ERR_INVALID_ARGS_COMBINATION 111 /* psb_err_invalid_args_combination_ */
