@@ -837,12 +837,12 @@ static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder)
 }
 
 // Blocks of the group that shares the matrix products of a dense f(H) whose
-// products have order m: one block while its 256 threads need at most three
-// rounds of 4-row strips, else about 192 strips per block, at most 16.
+// products have order m: one block while its 256 threads need one round of
+// 4-row strips, else about 128 strips per block, at most 16.
 static int dense_group_blocks(int m) {
   const long T = (long)((m + 3) / 4) * m;
-  if (T <= 3L * kDenseThreads) return 1;
-  return (int)std::min<long>(16, (T + 191) / 192);
+  if (T <= (long)kDenseThreads) return 1;
+  return (int)std::min<long>(16, (T + 127) / 128);
 }
 
 // Blocks of the group for a dense f(H) of order m: the product-based
