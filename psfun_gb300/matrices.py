@@ -112,21 +112,33 @@ def rgg_knn_laplacian(n: int, k: int, rng: np.random.Generator, shift: float = 1
 
 
 def read_matrix_market(path) -> sp.csr_matrix:
-    """Coordinate real/integer MatrixMarket, general or symmetric, 1-based."""
+    """Coordinate real/integer/pattern MatrixMarket, general, symmetric or
+    skew-symmetric, 1-based (the format of the reference's fixture
+    examples/polynomial/laplacian.mtx, which stores the lower triangle of a
+    symmetric matrix)."""
     with open(path) as f:
         header = f.readline().lower().split()
         if len(header) < 5 or header[0] != "%%matrixmarket" or header[2] != "coordinate":
             raise ValueError("only coordinate MatrixMarket files are supported")
-        symm = header[4] in ("symmetric", "skew-symmetric")
+        if header[3] not in ("real", "integer", "pattern"):
+            raise ValueError(f"unsupported MatrixMarket field {header[3]!r} (real, integer or pattern)")
+        if header[4] not in ("general", "symmetric", "skew-symmetric"):
+            raise ValueError(f"unsupported MatrixMarket symmetry {header[4]!r}")
+        symm = header[4] != "general"
         skew = header[4] == "skew-symmetric"
         line = f.readline()
-        while line.startswith("%"):
+        while line.startswith("%") or not line.strip():
             line = f.readline()
         nr, nc, nz = (int(t) for t in line.split())
-        data = np.loadtxt(f, ndmin=2, max_rows=nz)
+        ncol = 2 if header[3] == "pattern" else 3
+        data = np.loadtxt(f, ndmin=2, max_rows=nz) if nz > 0 else np.zeros((0, ncol))
+    if data.shape[0] != nz or data.shape[1] < ncol:
+        raise ValueError(f"expected {nz} entries of {ncol} columns, read {data.shape[0]}")
     i = data[:, 0].astype(np.int64) - 1
     j = data[:, 1].astype(np.int64) - 1
-    v = data[:, 2] if data.shape[1] > 2 else np.ones(len(i))
+    if nz and (i.min() < 0 or j.min() < 0 or i.max() >= nr or j.max() >= nc):
+        raise ValueError("MatrixMarket entry index out of range")
+    v = data[:, 2].astype(np.float64) if ncol == 3 else np.ones(len(i))
     if symm:
         off = i != j
         i, j, v = (np.concatenate([i, j[off]]), np.concatenate([j, i[off]]),
