@@ -297,57 +297,105 @@ PSF_DEVINL void cta_gemv(int m, const double* A, int lda, const double* x, doubl
   __syncthreads();
 }
 
-// First index of the largest |A(i,k)|, i in [k, m) (LAPACK IDAMAX rule).
-PSF_DEVINL void cta_pivot(int m, int k, const double* A, int lda, DenseSmem& sm) {
-  if (threadIdx.x < 32) {
-    double best = -1.0;
-    int bi = k;
-    for (int i = k + (int)threadIdx.x; i < m; i += 32) {
-      const double v = fabs(A[i + (size_t)k * lda]);
-      if (v > best) { best = v; bi = i; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    if (threadIdx.x == 0) { sm.iv[0] = bi; sm.dv[0] = best; }
+// One warp: the first index p of the largest |A(i,k)|, i in [k, m) (LAPACK
+// IDAMAX rule), into sm.iv[0], |A(p,k)| into sm.dv[0] and sm.iv[1] = (it is
+// zero), the signed pivot A(p,k) into sm.dv[1] and A(k,k) into sm.dv[2].
+// The magnitudes are compared as the integers of their bit patterns, which
+// order non-negative doubles as their values do, so that the search keeps
+// the scarce FP64 pipe out of its critical path; a NaN is never chosen, as
+// with a floating-point '>' test.
+PSF_DEVINL void warp_pivot(int m, int k, const double* A, int lda, DenseSmem& sm) {
+  const int lane = threadIdx.x & 31;
+  long long best = -1;
+  int bi = k;
+  for (int i = k + lane; i < m; i += 32) {
+    long long v = __double_as_longlong(A[i + (size_t)k * lda]) & 0x7fffffffffffffffLL;
+    if (v > 0x7ff0000000000000LL) v = -1;  // NaN
+    if (v > best) { best = v; bi = i; }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+  }
+  if (lane == 0) {
+    sm.iv[0] = bi;
+    sm.iv[1] = (best == 0);
+    sm.dv[0] = (best < 0) ? -1.0 : __longlong_as_double(best);
+    sm.dv[1] = A[bi + (size_t)k * lda];
+    sm.dv[2] = A[k + (size_t)k * lda];
+  }
+}
+
+PSF_DEVINL void cta_pivot(int m, int k, const double* A, int lda, DenseSmem& sm) {
+  if (threadIdx.x < 32) warp_pivot(m, k, A, lda, sm);
   __syncthreads();
 }
 
 // Solve A X = B (A m x m, B m x nrhs) by Gaussian elimination with partial
-// pivoting, B eliminated alongside (DGESV semantics).  Returns false on an
-// exactly zero pivot.
+// pivoting, B eliminated alongside (DGESV semantics); A is left holding L
+// and U.  At step k the pivot row and row k are exchanged across A and B,
+// the multipliers of column k are formed, and the trailing part of A (one
+// warp per column) and of B (one entry per thread) is updated; warp 0
+// updates column k + 1 first and finds its pivot, so that a step takes two
+// block barriers.  Then a thread per column of B back-substitutes.  Returns
+// false on an exactly zero pivot.
 PSF_DEVINL bool cta_gesv(int m, int nrhs, double* A, int lda, double* B, int ldb, DenseSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  cta_pivot(m, 0, A, lda, sm);
   for (int k = 0; k < m; ++k) {
-    cta_pivot(m, k, A, lda, sm);
     const int p = sm.iv[0];
-    if (sm.dv[0] == 0.0) { __syncthreads(); return false; }
+    const double piv = sm.dv[1], akk = sm.dv[2];
+    if (sm.iv[1]) { __syncthreads(); return false; }
     if (p != k) {
       for (int j = threadIdx.x; j < m + nrhs; j += blockDim.x) {
+        if (j == k) continue;
         double* a = (j < m) ? A + (size_t)j * lda : B + (size_t)(j - m) * ldb;
         const double t = a[k]; a[k] = a[p]; a[p] = t;
       }
-      __syncthreads();
+      if (threadIdx.x == 0) A[k + (size_t)k * lda] = piv;
     }
-    const double piv = A[k + (size_t)k * lda];
-    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)k * lda] /= piv;
+    double* lk = A + (size_t)k * lda;
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) lk[i] = ((i == p) ? akk : lk[i]) / piv;
     __syncthreads();
     const int rows = m - k - 1;
     if (rows > 0) {
-      const int cols = rows + nrhs;
-      for (int t = threadIdx.x; t < rows * cols; t += blockDim.x) {
-        const int jj = t / rows, i = k + 1 + (t - jj * rows);
-        const double l = A[i + (size_t)k * lda];
-        if (jj < rows) {
-          const int j = k + 1 + jj;
-          A[i + (size_t)j * lda] = fma(-l, A[k + (size_t)j * lda], A[i + (size_t)j * lda]);
-        } else {
-          const int j = jj - rows;
-          B[i + (size_t)j * ldb] = fma(-l, B[k + (size_t)j * ldb], B[i + (size_t)j * ldb]);
+      if (rows <= 128) {
+        double l[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = k + 1 + lane + 32 * q;
+          l[q] = (i < m) ? lk[i] : 0.0;
         }
+        const int nq = (rows + 31) >> 5;  // row groups with an active lane
+        for (int j = k + 1 + warp; j < m; j += nw) {
+          double* col = A + (size_t)j * lda;
+          const double akj = col[k];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int i = k + 1 + lane + 32 * q;
+            if (q < nq && i < m) col[i] = fma(-l[q], akj, col[i]);
+          }
+          if (j == k + 1) {  // warp 0: the pivot of the next step
+            __syncwarp();
+            warp_pivot(m, k + 1, A, lda, sm);
+          }
+        }
+      } else {
+        for (int j = k + 1 + warp; j < m; j += nw) {
+          double* col = A + (size_t)j * lda;
+          const double akj = col[k];
+          for (int i = k + 1 + lane; i < m; i += 32) col[i] = fma(-lk[i], akj, col[i]);
+          if (j == k + 1) {
+            __syncwarp();
+            warp_pivot(m, k + 1, A, lda, sm);
+          }
+        }
+      }
+      for (int t = threadIdx.x; t < rows * nrhs; t += blockDim.x) {
+        const int j = t / rows, i = k + 1 + (t - j * rows);
+        B[i + (size_t)j * ldb] = fma(-lk[i], B[k + (size_t)j * ldb], B[i + (size_t)j * ldb]);
       }
     }
     __syncthreads();
