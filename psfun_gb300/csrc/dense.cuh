@@ -343,6 +343,7 @@ PSF_DEVINL void cta_pivot(int m, int k, const double* A, int lda, DenseSmem& sm)
 // false on an exactly zero pivot.
 PSF_DEVINL bool cta_gesv(int m, int nrhs, double* A, int lda, double* B, int ldb, DenseSmem& sm) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (m < 1) { __syncthreads(); return true; }
   cta_pivot(m, 0, A, lda, sm);
   for (int k = 0; k < m; ++k) {
     const int p = sm.iv[0];
