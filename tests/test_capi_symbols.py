@@ -75,3 +75,17 @@ def test_plot_residual_history(lib, tmp_path):
     assert k.plot(f, 10, res, directory=str(tmp_path)) == 0
     assert (tmp_path / "Lanczos-EXP-GENPADE-Residual.svg").read_text().count("<circle") == 5
     assert k.plot(f, 1, res, directory=str(tmp_path / "missing")) == pg.api.ERR_FROM_SUBROUTINE
+
+
+def test_missing_library_raises(tmp_path):
+    """No fallback: a missing library is an error (fresh interpreter, since the
+    loader caches the library it opened)."""
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, sys.argv[1])\n"
+            "from psfun_gb300 import _capi\n"
+            "try:\n    _capi.load(sys.argv[2])\nexcept RuntimeError as e:\n    print('raised:', e)\n")
+    r = subprocess.run([sys.executable, "-c", code, str(ROOT), str(tmp_path / "absent.so")], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "raised:" in r.stdout and "no CPU fallback" in r.stdout
