@@ -1179,7 +1179,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
         PSF_TRY(launch_dense((const void*)k_estimate, 1, meth->dgroup.as<DenseGroup>(), &g, args, s2));
         PSF_CUDA(cudaEventRecord(ev_est, s2));
         PSF_TRY(enqueue_step(i));
-        PSF_CUDA(cudaStreamWaitEvent(s, ev_est, 0));  // step i+1 sees the verdict
+        PSF_CUDA(cudaStreamWaitEvent(s, ev_est, 0));  // step i+1 sees the convergence decision
       } else {
         PSF_TRY(enqueue_step(i));
       }
@@ -1194,7 +1194,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
             PSF_TRY(launch_dense((const void*)k_sai_estimate, dense_blocks(fpk, i, false),
                                  meth->dgroup.as<DenseGroup>(), &g, args, s));
           }
-          PSF_CUDA(cudaStreamSynchronize(s));  // the next inner solve waits for the verdict
+          PSF_CUDA(cudaStreamSynchronize(s));  // the next inner solve waits for the convergence decision
         } else if (userf) {
           // yk = f(H(1:i-1,1:i-1)) e1 with the host callback; needs the step done
           PSF_CUDA(cudaStreamSynchronize(s));
