@@ -62,3 +62,28 @@ def test_fixture_matrix_fingerprint():
     T = -matrices.laplacian_1d(50)
     assert fp["n"] == 50 and fp["equals"] == "tridiag(1,-2,1)"
     assert T.nnz == 2 * fp["nnz_stored"] - 50
+
+
+@pytest.mark.parametrize("L", [0.02, 0.05, 0.3, 1.0, 3.0, 9.9, 10.5])
+def test_product_elliptic_equals_scipy(lib, L):
+    """An independent pin: K and K' (ellipkkp, m = exp(-2 pi L)) against SciPy's
+    ellipk / ellipkm1, real sn/cn/dn against scipy.special.ellipj, and, for
+    moderate L, purely imaginary arguments through Jacobi's imaginary
+    transformation sn(iy|m) = i sc(y|1-m), cn(iy|m) = nc(y|1-m),
+    dn(iy|m) = dc(y|1-m)."""
+    ss = pytest.importorskip("scipy.special")
+    import psfun_gb300 as pg
+    m = np.exp(-2.0 * np.pi * L)
+    K, Kp = pg.ellipkkp(L)
+    assert abs(K / ss.ellipk(m) - 1.0) <= 4e-16
+    assert abs(Kp / ss.ellipkm1(m) - 1.0) <= 4e-16
+    for u in (0.1, 0.7, 1.3, 2.9):
+        got = np.array(pg.ellipj(u, L))
+        want = np.array(ss.ellipj(u, m)[:3])
+        assert np.abs(got - want).max() <= 2e-15
+    if L <= 1.0:
+        for y in (0.2, 0.6):
+            sn, cn, dn = pg.ellipj(complex(0.0, y), L)
+            s1, c1, d1, _ = ss.ellipj(y, 1.0 - m)
+            for got, want in ((sn, 1j * s1 / c1), (cn, 1.0 / c1), (dn, d1 / c1)):
+                assert abs(got - want) <= 1e-14 * max(1.0, abs(want))
