@@ -333,6 +333,50 @@ def bench_cg(torch, pg, peak_gbs: float, reps: int = 3):
             "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs}
 
 
+def bench_laplace2d(torch, pg, reps: int = 20):
+    """The reference's CPU-sized case: y = exp(-A)x on the 2-D 5-point
+    Laplacian 100 x 100 (n = 10,000, unit x), Arnoldi (EXP/GENPADE on
+    scaling -1) and Lanczos (EXP/CHBSYM on -A), eps 1e-10, itmax 50, istop 1:
+    milliseconds per solve with the vectors in device memory and with host
+    arrays (copies included), beside the C restatement (the oracle) on all
+    host cores, and the relative difference of the two results."""
+    from oracle import oracle as orc
+    from psfun_gb300 import matrices
+    p = matrices.laplace2d_expm()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    xd = torch.tensor(p.x, device="cuda")
+    yd = torch.empty_like(xd)
+    out = {"workload": "2-D 5-point Laplacian 100^2 (n=10,000), y=exp(-A)x, eps 1e-10, itmax 50, istop 1"}
+    for kname, variant, scaling, A in (("ARNOLDI", "GENPADE", -1.0, p.A), ("LANCZOS", "CHBSYM", 1.0, -p.A)):
+        fun = pg.PsfunDSerial()
+        fun.set("FNAME", "EXP")
+        fun.set("VARIANT", variant)
+        fun.set("SCALING", scaling)
+        meth = pg.PsfunDKrylov()
+        meth.set("KNAME", kname)
+        a = pg.CsrMatrix.from_scipy(A)
+        dt_dev, r = _time_dev(torch, lambda: meth.apply(fun, a, xd, 1e-10, itmax=50, istop=1, y=yd), reps)
+        assert r.info == 0, (kname, r.info)
+        rh = meth.apply(fun, a, p.x, 1e-10, itmax=50, istop=1)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            rh = meth.apply(fun, a, p.x, 1e-10, itmax=50, istop=1)
+        dt_host = (time.perf_counter() - t0) / reps
+        of, oa = orc.serial("EXP", variant, scaling), orc.Csr.from_scipy(A)
+        o = orc.krylov(kname, of, oa, p.x, 1e-10, itmax=50, istop=1)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            o = orc.krylov(kname, of, oa, p.x, 1e-10, itmax=50, istop=1)
+        dt_cpu = (time.perf_counter() - t0) / reps
+        y = rh.y.cpu().numpy() if hasattr(rh.y, "cpu") else np.asarray(rh.y)
+        out[kname.lower()] = {
+            "iterations": int(r.iter), "gpu_ms_device": 1e3 * dt_dev, "gpu_ms_host_arrays": 1e3 * dt_host,
+            "cpu_restatement_ms": 1e3 * dt_cpu, "cpu_threads": threads,
+            "rel_diff_vs_restatement": float(np.linalg.norm(y - o["y"]) / np.linalg.norm(o["y"]))}
+    return out
+
+
 def bench_adjoint(torch, pg, reps: int = 3):
     """Gradient of L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2 on the 512 x 512
     grid-graph Laplacian (n = 262,144, 523,264 edge weights theta): the cost of
@@ -460,7 +504,8 @@ def run_only(name: str) -> int:
           "cg": lambda: bench_cg(torch, pg, peak),
           "batched": lambda: bench_batched(torch, pg),
           "serial": lambda: bench_serial(torch, pg),
-          "sai": lambda: bench_sai(torch, pg)}[name]
+          "sai": lambda: bench_sai(torch, pg),
+          "laplace2d": lambda: bench_laplace2d(torch, pg)}[name]
     print(json.dumps({name: fn()}), flush=True)
     return 0
 
@@ -475,7 +520,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batched (64-instance) comparison")
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
-    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "serial", "sai"],
+    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "serial", "sai", "laplace2d"],
                     help="run one secondary workload alone and print its result (for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
