@@ -5,9 +5,9 @@
  * This is the drop-in boundary.  Every entry point is `extern "C"`, takes plain
  * pointers and sizes, and returns an int status whose values are the PSBLAS
  * error codes the reference reports through `info` (0 = psb_success_).  A
- * Fortran ISO_C_BINDING shim binds these from the
- * reference's own module interfaces; the Python package psfun_gb300 binds them
- * with ctypes.
+ * Fortran ISO_C_BINDING shim (fortran/psfun_gb300_bind.f90) binds these from
+ * the reference's own module interfaces; the Python package psfun_gb300 binds
+ * them with ctypes.
  *
  * Conventions
  *  - Sparse matrices are CSR with int32 row pointers / column indices and FP64
@@ -102,6 +102,13 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
                          int index_base, psfun_csr** out);
 int psfun_gpu_csr_destroy(psfun_csr* a);
 int psfun_gpu_csr_info(const psfun_csr* a, int64_t* n, int64_t* nnz, int64_t* ntiles, double* norm_inf);
+/* No counterpart in the reference.  *sym = 1 when A equals A^T entry by entry
+ * (the same stored pattern and equal values), else 0.  Checked once per
+ * handle on the host (the matrix is copied back) and cached.  The entry
+ * points that rely on a symmetric A (psfun_gpu_d_krylov_batch and the
+ * quadrature sum, which run Lanczos) return PSFUN_ERR_INVALID_ARGS_COMBINATION
+ * for a matrix that fails it. */
+int psfun_gpu_csr_is_symmetric(psfun_csr* a, int* sym);
 /* y = alpha*A*x + beta*y on device vectors: psb_spmm as called at
  * krylov/polynomial/psfun_d_arnoldi.f90:202 and krylov/shifted/psfun_dcg.F90:261. */
 int psfun_gpu_csr_spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y);
@@ -131,10 +138,13 @@ int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, co
  * with device pointers a (lda), x, y, for callers that must not allocate device
  * memory: its scratch is one static 1 MiB __device__ array per device, held
  * until the process exits, instead of a cudaMalloc/cudaFree pair per call
- * (cudaFree waits for the whole device).  Accepts n <= 64 and phiorder <= 8;
- * larger sizes and USERF return 111 with a message in psfun_gpu_last_error.
- * The first call on a device looks up the array's address; make it before
- * any stream capture.  Calls that overlap on the GPU race on the array. */
+ * (cudaFree waits for the whole device).  Accepts n <= 64 and, for PHI,
+ * phiorder <= 8 (the other functions ignore PHIORDER); larger sizes and USERF
+ * return 111 with a message in psfun_gpu_last_error.  The first call on a
+ * device looks up the array's address; make that first call before any stream
+ * capture begins.  Every call waits for its stream to finish (it reads a
+ * status word back to the host).  Calls that overlap on the GPU race on the
+ * array. */
 int psfun_gpu_serial_apply_device_static(psfun_serial* fun, int n, const double* a, int lda, double* y,
                                          const double* x);
 

@@ -35,6 +35,7 @@ PROTOS = {
     "psfun_gpu_csr_create": (C.c_int, [C.c_int64, C.c_int64, ip, ip, dp, C.c_int, C.POINTER(vp)]),
     "psfun_gpu_csr_destroy": (C.c_int, [vp]),
     "psfun_gpu_csr_info": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp]),
+    "psfun_gpu_csr_is_symmetric": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "psfun_gpu_csr_spmv_device": (C.c_int, [vp, C.c_double, vp, C.c_double, vp]),
     "psfun_gpu_csr_spmv": (C.c_int, [vp, C.c_double, dp, C.c_double, dp]),
     "psfun_gpu_serial_create": (C.c_int, [C.POINTER(vp)]),

@@ -94,6 +94,14 @@ class CsrMatrix:
         m.sort_indices()
         return cls(m.indptr, m.indices, m.data)
 
+    def is_symmetric(self) -> bool:
+        """A == A^T entry by entry (checked once per handle on the host)."""
+        v = C.c_int(0)
+        info = _lib().psfun_gpu_csr_is_symmetric(self.handle, C.byref(v))
+        if info != SUCCESS:
+            raise PsfunError(info, "psfun_gpu_csr_is_symmetric")
+        return bool(v.value)
+
     def spmv(self, x, alpha: float = 1.0, beta: float = 0.0, y=None):
         """y = alpha*A*x + beta*y (psb_spmm)."""
         if _is_device(x):

@@ -874,6 +874,14 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
     if (!items[k].a || items[k].nrhs != R) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
     if (!items[k].x || !items[k].y) return PSFUN_ERR_INVALID_VECT_STATE;
   }
+  for (int k = 0; k < count; ++k) {  // Lanczos needs A = A^T
+    int sym = 0;
+    PSF_TRY(csr_symmetric(items[k].a, &sym));
+    if (!sym) {
+      set_last_error("batch item " + std::to_string(k) + ": the batched Lanczos needs a symmetric matrix");
+      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    }
+  }
   const int nl = itmax;
   cudaStream_t s = stream();
   // workspace: one allocation, carved per instance

@@ -354,6 +354,7 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
 
 int psfun_gpu_csr_destroy(psfun_csr* a) {
   if (!a) return PSFUN_SUCCESS;
+  if (a->T) psfun_gpu_csr_destroy(a->T);
   if (a->irp) cudaFree(a->irp);
   if (a->ja) cudaFree(a->ja);
   if (a->val) cudaFree(a->val);
@@ -374,9 +375,102 @@ int psfun_gpu_csr_info(const psfun_csr* a, int64_t* n, int64_t* nnz, int64_t* nt
   return PSFUN_SUCCESS;
 }
 
+int psfun_gpu_csr_is_symmetric(psfun_csr* a, int* sym) {
+  psf::NvtxRange nvtx_range("psfun_gpu_csr_is_symmetric");
+  if (!a || !sym) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  return psf::csr_symmetric(a, sym);
+}
+
 }  // extern "C"
 
 namespace psf {
+
+// The matrix back on the host (0-based CSR).
+static int csr_download(psfun_csr* a, std::vector<int32_t>& irp, std::vector<int32_t>& ja, std::vector<double>& val) {
+  irp.resize(a->n + 1);
+  ja.resize(a->nnz);
+  val.resize(a->nnz);
+  cudaStream_t s = stream();
+  PSF_CUDA(cudaMemcpyAsync(irp.data(), a->irp, sizeof(int32_t) * (a->n + 1), cudaMemcpyDeviceToHost, s));
+  if (a->nnz > 0) {
+    PSF_CUDA(cudaMemcpyAsync(ja.data(), a->ja, sizeof(int32_t) * a->nnz, cudaMemcpyDeviceToHost, s));
+    PSF_CUDA(cudaMemcpyAsync(val.data(), a->val, sizeof(double) * a->nnz, cudaMemcpyDeviceToHost, s));
+  }
+  PSF_CUDA(cudaStreamSynchronize(s));
+  return PSFUN_SUCCESS;
+}
+
+// Transpose by a counting sort over the columns: traversing the rows in
+// order leaves every row of the transpose in increasing column order.
+static void host_transpose(int64_t n, const std::vector<int32_t>& irp, const std::vector<int32_t>& ja,
+                           const std::vector<double>& val, std::vector<int32_t>& irpT, std::vector<int32_t>& jaT,
+                           std::vector<double>& valT) {
+  const int64_t nnz = (int64_t)ja.size();
+  irpT.assign(n + 1, 0);
+  for (int64_t k = 0; k < nnz; ++k) ++irpT[ja[k] + 1];
+  for (int64_t i = 0; i < n; ++i) irpT[i + 1] += irpT[i];
+  std::vector<int32_t> cur(irpT.begin(), irpT.end() - 1);
+  jaT.resize(nnz);
+  valT.resize(nnz);
+  for (int64_t i = 0; i < n; ++i)
+    for (int32_t k = irp[i]; k < irp[i + 1]; ++k) {
+      const int32_t pos = cur[ja[k]]++;
+      jaT[pos] = (int32_t)i;
+      valT[pos] = val[k];
+    }
+}
+
+int csr_symmetric(psfun_csr* a, int* sym) {
+  if (a->sym >= 0) {
+    *sym = a->sym;
+    return PSFUN_SUCCESS;
+  }
+  std::vector<int32_t> irp, ja, irpT, jaT;
+  std::vector<double> val, valT;
+  PSF_TRY(csr_download(a, irp, ja, val));
+  host_transpose(a->n, irp, ja, val, irpT, jaT, valT);
+  int ok = (irp == irpT) ? 1 : 0;
+  std::vector<std::pair<int32_t, double>> ra, rt;
+  for (int64_t i = 0; ok && i < a->n; ++i) {
+    const int32_t b = irp[i], e = irp[i + 1];
+    bool sorted = true;
+    for (int32_t k = b + 1; k < e; ++k)
+      if (ja[k] <= ja[k - 1]) { sorted = false; break; }
+    if (sorted) {
+      for (int32_t k = b; k < e && ok; ++k)
+        if (ja[k] != jaT[k] || !(val[k] == valT[k])) ok = 0;
+    } else {  // unsorted row or repeated entries: compare as sorted (column, value) lists
+      ra.clear();
+      rt.clear();
+      for (int32_t k = b; k < e; ++k) {
+        ra.emplace_back(ja[k], val[k]);
+        rt.emplace_back(jaT[k], valT[k]);
+      }
+      std::sort(ra.begin(), ra.end());
+      std::sort(rt.begin(), rt.end());
+      for (size_t q = 0; q < ra.size() && ok; ++q)
+        if (ra[q].first != rt[q].first || !(ra[q].second == rt[q].second)) ok = 0;
+    }
+  }
+  a->sym = ok;
+  *sym = ok;
+  return PSFUN_SUCCESS;
+}
+
+int csr_transpose(psfun_csr* a, psfun_csr** out) {
+  if (!a->T) {
+    std::vector<int32_t> irp, ja, irpT, jaT;
+    std::vector<double> val, valT;
+    PSF_TRY(csr_download(a, irp, ja, val));
+    host_transpose(a->n, irp, ja, val, irpT, jaT, valT);
+    psfun_csr* t = nullptr;
+    PSF_TRY(psfun_gpu_csr_create(a->n, a->nnz, irpT.data(), jaT.data(), valT.data(), 0, &t));
+    a->T = t;
+  }
+  *out = a->T;
+  return PSFUN_SUCCESS;
+}
+
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_axpby(CsrDev A, const double* x, double alpha, double beta,
                                                              double* y, int* err) {
   PSF_SPMV_SMEM();

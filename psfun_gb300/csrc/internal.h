@@ -73,6 +73,12 @@ struct KCtrl {
   unsigned bar_gen;
   unsigned red_counter;
   unsigned red_counter2;
+  // monitor CTA of a persistent Lanczos launch (shifted residuals or the
+  // a posteriori estimate running beside the steps)
+  int pub;        // last Lanczos step whose T entries are published (CTA 0)
+  int stop_req;   // the monitor asks the steps to stop
+  int stop_dec;   // CTA 0's reading of stop_req, taken before a grid barrier
+  int bd_step;    // step at which a Lanczos breakdown was found
   double beta0;   // rs(1) = ||x||
   double errnum;
   double errden;
@@ -95,6 +101,8 @@ struct psfun_csr {
   int2* tile_desc = nullptr;   // per tile {first row, first stored entry}, ntiles + 1 entries
   int32_t max_tile_rows = 0;
   std::vector<double> h_diag;  // diagonal of A (host copy, for DIAG)
+  int sym = -1;                // A == A^T (pattern and values): 1 yes, 0 no, -1 not yet checked
+  psfun_csr* T = nullptr;      // A^T as its own handle, built on first use (nonsymmetric A)
   psf::CsrDev dev() const {
     psf::CsrDev d;
     d.n = n; d.nnz = nnz; d.irp = irp; d.ja = ja; d.val = val; d.tile_row = tile_row; d.ntiles = ntiles;
@@ -150,6 +158,12 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                       const double* x, double* y, double eps, int itmax, int* iter, double* err);
 int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y);
+// Whether A equals A^T entry by entry (same stored pattern, equal values),
+// checked once per handle on the host and cached: *sym = 1 or 0.
+int csr_symmetric(psfun_csr* a, int* sym);
+// A^T as a CSR handle owned by `a` (built once, on the host, rows in
+// increasing column order); destroyed with `a`.
+int csr_transpose(psfun_csr* a, psfun_csr** out);
 
 // Optional per-kernel timing: CUDA events recorded around selected launches
 // on the launching stream, accumulated when the solve synchronises.

@@ -68,6 +68,7 @@ __global__ void k_reset(KState st, size_t small_doubles) {
     KCtrl* c = st.ctrl;
     c->done = c->conv = c->breakdown = c->itx = c->yk_len = c->nterms = c->err = c->info = 0;
     c->bar_count = c->bar_gen = c->red_counter = c->red_counter2 = 0u;
+    c->pub = c->stop_req = c->stop_dec = c->bd_step = 0;
     c->beta0 = c->errnum = c->c1 = c->c2 = c->derr = 0.0;
     c->errden = 1.0;
   }
@@ -1668,6 +1669,14 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   if (!a || !xi || !cw) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (!x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   if (N < 1 || N > 1024 || itmax < 1) return PSFUN_ERR_INVALID_ARGS_COMBINATION;  // one monitor thread per shift
+  {  // the shared Lanczos basis needs A = A^T
+    int sym = 0;
+    PSF_TRY(csr_symmetric(a, &sym));
+    if (!sym) {
+      set_last_error("quadrature sum: the multi-shift Lanczos solve needs a symmetric matrix");
+      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    }
+  }
   static psfun_krylov* meth = nullptr;
   if (!meth) meth = new psfun_krylov();
   static DevBuf msbuf;
@@ -1873,6 +1882,14 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
                         int recompute, double* y, double* grad_x, double* grad_t, double* grad_vals, int* iters) {
   if (!a || !x || !g) return PSFUN_ERR_INVALID_VECT_STATE;
   if (nquad < 4 || (nquad & 1) || itmax < 2 || t == 0.0) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  {
+    int sym = 0;
+    PSF_TRY(csr_symmetric(a, &sym));
+    if (!sym) {
+      set_last_error("expm adjoint: the Lanczos bases need a symmetric matrix");
+      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    }
+  }
   const int Nq = nquad / 2;
   std::vector<double> zc_h(2 * Nq), cw_h(2 * Nq), xi_h(2 * Nq);
   if (psfun_gpu_talbot_rule(nquad, zc_h.data(), cw_h.data()) != PSFUN_SUCCESS) return PSFUN_ERR_INTERNAL;
@@ -2039,8 +2056,11 @@ int psfun_gpu_z_quadrature_apply(psfun_csr* a, int N, const double* xi, const do
 //
 // The array holds kSerialStaticDoubles doubles (1 MiB) and is resident on every
 // device that loads the library until the process exits.  Accepted sizes:
-// n <= kSerialStaticMaxN (64) and, for PHI, phiorder <= kSerialStaticMaxPhi (8);
-// larger requests are rejected with PSFUN_ERR_INVALID_ARGS_COMBINATION.
+// n <= kSerialStaticMaxN (64) and, for PHI, phiorder <= kSerialStaticMaxPhi (8)
+// (the other functions ignore PHIORDER); larger requests are rejected with
+// PSFUN_ERR_INVALID_ARGS_COMBINATION.  The evaluation runs on the same group of
+// blocks as serial_apply_device.  Each call waits for its stream to finish
+// (it reads the status word back to the host).
 // Every call on a device shares the array and finds the previous call's
 // contents in it: the dense kernels write every scratch entry before reading
 // it (the Krylov workspace is reused the same way), and the status word is
@@ -2088,34 +2108,68 @@ static int serial_static_scratch(double** out) {
 
 static int serial_apply_static(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev,
                                const double* x_dev) {
-  if (!fun) return PSFUN_ERR_INVALID_VECT_STATE;
-  if (!a_dev || !x_dev || !y_dev) return PSFUN_ERR_INVALID_VECT_STATE;
-  if (n < 1 || lda < n) return PSFUN_ERR_FROM_SUBROUTINE;
+  if (!fun || !a_dev || !x_dev || !y_dev) {
+    set_last_error("serial_apply_static: null handle or pointer");
+    return PSFUN_ERR_INVALID_VECT_STATE;
+  }
+  if (n < 1 || lda < n) {
+    set_last_error("serial_apply_static: n < 1 or lda < n");
+    return PSFUN_ERR_FROM_SUBROUTINE;
+  }
   FunParams fp;
-  if (!parse_fun(fun, &fp)) return PSFUN_ERR_FROM_SUBROUTINE;
+  if (!parse_fun(fun, &fp)) {
+    set_last_error("serial_apply_static: invalid function name / variant");
+    return PSFUN_ERR_FROM_SUBROUTINE;
+  }
   if (fp.fname == FN_USERF) {
     set_last_error("serial_apply_static: USERF evaluates f on the host and is not supported here");
     return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   }
-  // status word (one double slot) + dense scratch, as serial_apply_device
-  const size_t fs = fh_scratch_doubles(n, fp.phiorder) + 4 * (size_t)n * n + 8 * (size_t)n;
-  if (n > kSerialStaticMaxN || (fp.fname == FN_PHI && fp.phiorder > kSerialStaticMaxPhi) ||
-      fs + 32 > kSerialStaticDoubles) {
-    set_last_error("serial_apply_static: size beyond the static scratch (n <= 64, phiorder <= 8)");
+  // PHIORDER sizes the augmented matrix of PHI only; the other functions
+  // ignore what the handle holds there.
+  const int po = (fp.fname == FN_PHI) ? fp.phiorder : 1;
+  if (n > kSerialStaticMaxN || po > kSerialStaticMaxPhi) {
+    set_last_error("serial_apply_static: size beyond the static scratch (n <= 64, and phiorder <= 8 for PHI)");
+    return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  }
+  // dense scratch as serial_apply_device sizes it, then the status word
+  // (one double slot), then the DenseGroup of a cooperative launch
+  const size_t fs = fh_scratch_doubles(n, po) + 4 * (size_t)n * n + 8 * (size_t)n;
+  const size_t grp_off = fs + 8;
+  static_assert(sizeof(DenseGroup) <= 24 * sizeof(double), "DenseGroup outgrew its static slot");
+  if (grp_off + 24 > kSerialStaticDoubles) {
+    set_last_error("serial_apply_static: size beyond the static scratch (n <= 64, and phiorder <= 8 for PHI)");
     return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   }
   double* scr = nullptr;
   PSF_TRY(serial_static_scratch(&scr));
   int* dstat = reinterpret_cast<int*>(scr + fs);
+  DenseGroup* grp = reinterpret_cast<DenseGroup*>(scr + grp_off);
   cudaStream_t s = stream();
   PSF_CUDA(cudaMemsetAsync(dstat, 0xff, sizeof(int), s));
-  k_serial_apply<<<1, kDenseThreads, 0, s>>>(fp, n, a_dev, lda, x_dev, y_dev, scr, dstat, nullptr);
-  count_launch();
+  {
+    FunParams fpl = fp;
+    fpl.phiorder = po;
+    int nn = n, ld = lda;
+    const double *aa = a_dev, *xx = x_dev;
+    double* yy = y_dev;
+    double* sp = scr;
+    DenseGroup* g = nullptr;
+    void* args[] = {(void*)&fpl, (void*)&nn, (void*)&aa, (void*)&ld, (void*)&xx, (void*)&yy, (void*)&sp,
+                    (void*)&dstat, (void*)&g};
+    // the same group of blocks as serial_apply_device (launch_dense zeroes
+    // the group's slot before a cooperative launch)
+    PSF_TRY(launch_dense((const void*)k_serial_apply, dense_blocks(fpl, n, false), grp, &g, args, s));
+  }
   PSF_CUDA(cudaGetLastError());
   int hs = -1;
   PSF_CUDA(cudaMemcpyAsync(&hs, dstat, sizeof(int), cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
-  return hs == 0 ? PSFUN_SUCCESS : PSFUN_ERR_FROM_SUBROUTINE;
+  if (hs != 0) {
+    set_last_error("serial_apply_static: the dense evaluation failed (status " + std::to_string(hs) + ")");
+    return PSFUN_ERR_FROM_SUBROUTINE;
+  }
+  return PSFUN_SUCCESS;
 }
 
 }  // namespace psf

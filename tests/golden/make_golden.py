@@ -1,6 +1,8 @@
-"""Generates the committed golden fixtures (run in the development container,
-where the reference sources are readable; the fixtures travel, this script
-does not need to).
+"""Generates the committed golden fixtures from a checkout of the reference's
+sources (the fixtures travel with the tests; this script and the reference
+checkout are needed only to regenerate them).
+
+Usage: python tests/golden/make_golden.py <path to the psfun source tree>
 
 1. utiltest_control.json -- the control values printed by the reference's own
    known-answer test, parsed as text from examples/utils/utiltest.f90:63-87.
@@ -24,7 +26,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
-REF = Path("/root/reference")
+REF = Path(".")  # set from the command line in main()
 
 
 def utiltest_controls() -> dict:
@@ -45,6 +47,10 @@ def utiltest_controls() -> dict:
 
 
 def main():
+    global REF
+    if len(sys.argv) != 2 or not (Path(sys.argv[1]) / "examples/utils/utiltest.f90").is_file():
+        raise SystemExit("usage: make_golden.py <psfun source tree (holding examples/utils/utiltest.f90)>")
+    REF = Path(sys.argv[1])
     from oracle import oracle as orc
     from psfun_gb300 import matrices
 

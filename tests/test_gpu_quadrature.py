@@ -4,24 +4,14 @@ structure of the grid Laplacians, at test size and at the full 96^3 size."""
 import numpy as np
 import pytest
 
+from oracle import exact
 from psfun_gb300 import matrices
 
 pytestmark = pytest.mark.gpu
 
 
-def spectral_1d(n1):
-    k = np.arange(1, n1 + 1)
-    lam = 4.0 * np.sin(np.pi * k / (2.0 * (n1 + 1))) ** 2
-    Q = np.sqrt(2.0 / (n1 + 1)) * np.sin(np.outer(k, k) * np.pi / (n1 + 1))
-    return lam, Q
-
-
 def apply_fun_3d(n1, x, fun):
-    lam, Q = spectral_1d(n1)
-    X = x.reshape(n1, n1, n1)
-    Xh = np.einsum("ia,jb,kc,ijk->abc", Q, Q, Q, X, optimize=True)
-    L = lam[:, None, None] + lam[None, :, None] + lam[None, None, :]
-    return np.einsum("ia,jb,kc,abc->ijk", Q, Q, Q, fun(L) * Xh, optimize=True).ravel()
+    return exact.laplacian_3d_apply(n1, x, fun)
 
 
 def run(n1, N, x, eps=1e-10):

@@ -69,3 +69,24 @@ def test_static_scratch_rejects_oversize(lib):
                                                   C.c_void_p(p + 8 * (m * m + m)))
     assert rc == 111
     assert b"static scratch" in lib.psfun_gpu_last_error()
+
+
+def test_static_scratch_limits_follow_the_function(lib):
+    """PHIORDER limits PHI only: an EXP call at n = 64 whose handle still holds
+    a large PHIORDER runs; PHI with phiorder 9 and USERF are refused."""
+    import torch
+    H, x = case(64, 4)
+    fun = mk("EXP", "GENPADE", 0.6, 20)
+    ref, info = fun.apply(H, x)
+    assert info == 0
+    rc, y = static_apply(lib, fun, H, x)
+    assert rc == 0, lib.psfun_gpu_last_error()
+    assert np.linalg.norm(y - ref) <= RTOL * np.linalg.norm(ref)
+    H, x = case(16, 5)
+    rc, _ = static_apply(lib, mk("PHI", "", 0.6, 9), H, x)
+    assert rc == 111 and b"phiorder" in lib.psfun_gpu_last_error()
+    fu = mk("USERF", "SYM", 0.6)
+    assert fu.set("FPOINTER", lambda v, k: np.exp(v)) == 0
+    rc, _ = static_apply(lib, fu, H, x)
+    assert rc == 111 and b"USERF" in lib.psfun_gpu_last_error()
+    torch.cuda.synchronize()
