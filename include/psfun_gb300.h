@@ -5,9 +5,10 @@
  * This is the drop-in boundary.  Every entry point is `extern "C"`, takes plain
  * pointers and sizes, and returns an int status whose values are the PSBLAS
  * error codes the reference reports through `info` (0 = psb_success_).  A
- * Fortran ISO_C_BINDING shim (fortran/psfun_gb300_bind.f90) binds these from
- * the reference's own module interfaces; the Python package psfun_gb300 binds
- * them with ctypes.
+ * Fortran ISO_C_BINDING module (psfun_gb300/fortran/psfun_gb300_cabi.f90)
+ * declares every entry point for Fortran callers, and the shim
+ * psfun_gb300/fortran/psfun_gb300_shim.F90 calls them from the reference's own
+ * module interfaces; the Python package psfun_gb300 binds them with ctypes.
  *
  * Conventions
  *  - Sparse matrices are CSR with int32 row pointers / column indices and FP64
