@@ -74,12 +74,15 @@ struct KCtrl {
   unsigned red_counter;
   unsigned red_counter2;
   // monitor CTA of a persistent Lanczos launch (shifted residuals or the
-  // a posteriori estimate running beside the steps)
-  int pub;        // last Lanczos step whose T entries are published (CTA 0)
+  // a posteriori estimate running beside the steps); on a cache line of
+  // their own, away from the grid barrier's counter that the monitor's
+  // polling would otherwise slow down
+  alignas(128) int pub;  // last Lanczos step whose T entries are published (CTA 0)
   int stop_req;   // the monitor asks the steps to stop
   int stop_dec;   // CTA 0's reading of stop_req, taken before a grid barrier
-  int bd_step;    // step at which a Lanczos breakdown was found
-  double beta0;   // rs(1) = ||x||
+  int bd_step;    // step at which a Lanczos breakdown was found (0: none)
+  int conv_first; // concurrent Arnoldi estimates: the first converged iteration (INT_MAX: none)
+  alignas(128) double beta0;  // rs(1) = ||x||
   double errnum;
   double errden;
   double c1, c2;  // Lanczos update coefficients
@@ -132,6 +135,7 @@ struct psfun_krylov {
   // cached workspace (never per call)
   psf::DevBuf V, u, small, scratch, partials, ctrl, xy;
   psf::DevBuf dgroup;  // DenseGroup of the dense f(H) kernels
+  psf::DevBuf par;     // concurrent Arnoldi estimates: per-iteration yk / error words, scratch and groups
   int64_t ldv = 0;
   int nl_cap = 0;
   // CUDA graph of a whole fixed-length (istop = 2) solve, replayed while the

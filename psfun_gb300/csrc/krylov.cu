@@ -47,6 +47,11 @@ struct KState {
   double* fscratch;
   double* ework;  // USERF: eigenvalues / f values / eigenvectors
   volatile int* host_flag;  // mapped: [0] done, [1] last finished step
+  // Concurrent Arnoldi estimates (null otherwise): each estimate i writes its
+  // own error words errn_all[i], errd_all[i] (yk into its own slot, st.yk of
+  // its launch) and records convergence by an atomicMin on conv_first.
+  double* errn_all = nullptr;
+  double* errd_all = nullptr;
 };
 
 #define HAT(st, i, j) (st).H[((i)-1) + (size_t)((j)-1) * (st).ldh]
@@ -69,6 +74,7 @@ __global__ void k_reset(KState st, size_t small_doubles) {
     c->done = c->conv = c->breakdown = c->itx = c->yk_len = c->nterms = c->err = c->info = 0;
     c->bar_count = c->bar_gen = c->red_counter = c->red_counter2 = 0u;
     c->pub = c->stop_req = c->stop_dec = c->bd_step = 0;
+    c->conv_first = 0x7fffffff;
     c->beta0 = c->errnum = c->c1 = c->c2 = c->derr = 0.0;
     c->errden = 1.0;
   }
@@ -196,6 +202,20 @@ __global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) 
 // Every CTA derives the scalars itself, so none is re-read from memory, and
 // CTA 0 records H, s and itx for the estimate / final kernels.
 // ---------------------------------------------------------------------------
+// Shifts of a multi-shift solve on one Lanczos basis (quadrature sums and
+// the adjoint): (xi_j I + sign T) is monitored by the LDL^T recurrences.
+struct MsParams {
+  int N;
+  const double* xi;  // 2N
+  const double* c;   // 2N
+  double sign, eta, eps;
+  double* d;      // 2N: LDL pivots of the last step
+  double* phi;    // 2N
+  double* resid;  // N
+  int* mon;       // [0]: the monitor's last step (its own word: the monitor
+                  // of one chunk runs while the next chunk's Lanczos steps do)
+};
+
 // Lanczos epilogue of the SpMV phase: u = A W_i and the partial alpha dot.
 struct EpiLzDot {
   double* __restrict__ u;
@@ -207,10 +227,33 @@ struct EpiLzDot {
   }
 };
 
+// Monitor CTA of a persistent launch (the last block of the grid, outside
+// the grid barriers): it follows the steps as CTA 0 publishes their T entries
+// and asks them to stop (ms_monitor_cta: the shifted residuals of a
+// multi-shift solve; est_monitor_cta: the a posteriori estimate of istop = 1).
+enum : int { LZ_PLAIN = 0, LZ_MON_SHIFTS = 1, LZ_MON_ESTIMATE = 2 };
+struct LzMonitor {
+  MsParams mp;   // LZ_MON_SHIFTS
+  FunParams fp;  // LZ_MON_ESTIMATE: f and its variant (scaling 1)
+  double eps;
+  int tridiag;
+};
+__device__ __noinline__ void ms_monitor_cta(KState& st, const MsParams& mp, int i_begin, int i_end);
+__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end);
+
+// MODE LZ_PLAIN: the grid is the compute CTAs.  Otherwise the grid has one
+// more block, the monitor.  The steps read the monitor's stop request through
+// CTA 0: its thread 0 copies stop_req into stop_dec before arriving at the
+// first grid barrier of a step, and every CTA reads stop_dec after that
+// barrier, so all of them leave at the same step.  Steps run past the one at
+// which the monitor decides change nothing it uses (they write later basis
+// slots and T entries).
+template <int MODE>
 __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A, int i_begin, int i_end,
-                                                             int tiles_per_cta) {
+                                                             int tiles_per_cta, LzMonitor mon) {
   extern __shared__ __align__(128) unsigned char lz_smem_raw[];
   LzSmem& sm = *reinterpret_cast<LzSmem*>(lz_smem_raw);
+  constexpr bool kMon = MODE != LZ_PLAIN;
   KCtrl* c = st.ctrl;
   if (c->done) return;
   if (c->breakdown) {  // found by the previous launch: exit at the top of iteration i_begin
@@ -220,8 +263,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     }
     return;
   }
+  const int G = gridDim.x - (kMon ? 1 : 0), bid = blockIdx.x;
+  if (kMon && bid == G) {
+    if (MODE == LZ_MON_SHIFTS) ms_monitor_cta(st, mon.mp, i_begin, i_end);
+    else est_monitor_cta(st, mon, i_begin, i_end);
+    return;
+  }
   lz_smem_init(sm);
-  const int G = gridDim.x, bid = blockIdx.x;
   const int t0 = min(A.ntiles, bid * tiles_per_cta);
   const int t1 = min(A.ntiles, t0 + tiles_per_cta);
   const int rb = A.tile_desc[t0].x, re = A.tile_desc[t1].x;
@@ -239,6 +287,8 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
   double sprev = (i_begin >= 2) ? st.s[i_begin - 1] : 0.0;
   double beta_i = (i_begin >= 2) ? HAT(st, i_begin - 1, i_begin) : 0.0;
   double* __restrict__ u = st.u;
+  // tiles staged beyond the passes that ran: waited for before any early exit
+  auto drain = [&](int passes) { pipe_drain(sm, pc, (unsigned)passes * (unsigned)(t1 - t0)); };
   for (int i = i_begin; i < i_end; ++i) {
     const double* __restrict__ wi = WAT(st, i);
     // ---- phase 1
@@ -262,20 +312,30 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       pipe_spmv(A, wi, t0, t1, sm, epi, &c->err, pc, i + 1 < i_end, stream);
       acc = epi.acc;
     }
+    if (kMon && bid == 0 && threadIdx.x == 0) c->stop_dec = *(volatile int*)&c->stop_req;
     block_sum_store_512(acc, sm.vals, sm.red, &st.partials[bid]);
-    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i - 1) * (unsigned)G, &c->err)) return;
+    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i - 1) * (unsigned)G, &c->err)) {
+      drain(i - i_begin + 1);
+      return;
+    }
     {
       const double S = partials_sum_to0(st.partials, G, sm.red);
       if (threadIdx.x == 0) {
         const double a = sc * sc * S;
         sm.scal[2] = a;
-        if (bid == 0) {
+        const int stop = kMon ? *(volatile int*)&c->stop_dec : 0;
+        sm.scal[4] = stop ? 1.0 : 0.0;
+        if (bid == 0 && !stop) {
           HAT(st, i, i) = a;
           if (i >= 2) c->itx = i - 1;
         }
       }
     }
     __syncthreads();
+    if (kMon && sm.scal[4] != 0.0) {  // the monitor has decided: leave before the update
+      drain(i - i_begin + 1);
+      return;
+    }
     sc = sm.scal[0];
     const double alpha = sm.scal[2];
     const double c2 = sm.scal[1];
@@ -309,7 +369,10 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
       wo[r] = scale_pow2(w, k2);
     }
     block_sum_store_512(acc2, sm.vals, sm.red, &st.partials[G + bid]);
-    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i) * (unsigned)G, &c->err)) return;
+    if (!grid_sync_to(&c->bar_count, (unsigned)(2 * i) * (unsigned)G, &c->err)) {
+      drain(i - i_begin + 1);
+      return;
+    }
     {
       const double S = partials_sum_to0(st.partials + G, G, sm.red);
       if (threadIdx.x == 0) {
@@ -322,6 +385,15 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
           HAT(st, i, i + 1) = bt;
           HAT(st, i + 1, i) = bt;
           if (st.host_flag) st.host_flag[1] = i;
+          if (kMon) {  // publish step i to the monitor, a breakdown first
+            if (i + 1 <= st.nl && fabs(bt) < 1e-16) {  // the monitors read bd_step alone
+              c->bd_step = i;
+              c->breakdown = 1;
+              c->itx = i;
+            }
+            __threadfence();
+            *(volatile int*)&c->pub = i;
+          }
         }
       }
     }
@@ -330,9 +402,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     if (i + 1 <= st.nl && fabs(beta) < 1e-16) {  // checked at the top of iteration i+1
       if (bid == 0 && threadIdx.x == 0) {
         st.s[i + 1] = 1.0 / ldexp(wn_prev, k2_prev);
+        c->bd_step = i;
         c->breakdown = 1;
         c->itx = i;
       }
+      drain(i - i_begin + 1);
       return;
     }
     sprev = sc;
@@ -554,6 +628,15 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
     const double errden = sqrt(ss);
     const double r = errnum / errden;
     st.rs[i - 1] = r;
+    if (st.errn_all) {  // concurrent estimates: own words, the first converged one wins
+      st.errn_all[i] = errnum;
+      st.errd_all[i] = errden;
+      if (r < eps) {
+        atomicMin(&c->conv_first, i);
+        if (st.host_flag) st.host_flag[0] = 1;
+      }
+      return;
+    }
     c->errnum = errnum;
     c->errden = errden;
     if (r < eps) {
@@ -578,13 +661,21 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
   __shared__ DenseSmem sm;                   \
   dense_group_begin(sm, grp)
 
-__device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps, int tridiag, DenseSmem& sm) {
+__device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps, int tridiag, DenseSmem& sm,
+                              bool breakdown_ends = true) {
   KCtrl* c = st.ctrl;
-  if (c->done) return;
+  if (st.errn_all) {
+    // concurrent estimates: skip only when an estimate of an earlier
+    // iteration has converged (c->done can be set by a later step meanwhile)
+    if (*(volatile int*)&c->conv_first < i || c->beta0 == 0.0) return;
+  } else if (c->done) {
+    return;
+  }
   // Lanczos: a breakdown found at the end of step i-1 ends the iteration
   // before this estimate (psfun_d_lanczos.f90:225-230), whether or not step
-  // i's kernel has already stopped the solve
-  if (tridiag && c->breakdown) return;
+  // i's kernel has already stopped the solve.  (The monitor CTA, whose steps
+  // run ahead, tests the breakdown step itself and passes false.)
+  if (breakdown_ends && tridiag && c->breakdown) return;
   const int m = i - 1;
   const int rc = fh_apply_cta(fp, m, st.H, st.ldh, st.e1, st.yk, st.fscratch, tridiag != 0, sm);
   if (rc) {
@@ -604,6 +695,155 @@ __global__ void __launch_bounds__(kDenseThreads) k_estimate(KState st, FunParams
   PSF_DENSE_KERNEL_ENTRY(grp, &st.ctrl->err);
   estimate_body(st, fp, i, eps, tridiag, sm);
   dense_group_end(sm, &st.ctrl->err);
+}
+
+// ---------------------------------------------------------------------------
+// Monitor CTAs of the persistent Lanczos kernel.
+// ---------------------------------------------------------------------------
+// Thread 0 waits (bounded) until CTA 0 has published step `want`; returns the
+// last published step, or -1 when the steps failed or the wait timed out.
+__device__ int monitor_wait_pub(KCtrl* c, int want) {
+  const unsigned long long t0 = globaltimer_ns();
+  int p;
+  while ((p = *(volatile int*)&c->pub) < want) {
+    if (*(volatile int*)&c->err != 0) return -1;
+    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+      atomicOr(&c->err, DEVERR_TIMEOUT);
+      return -1;
+    }
+    __nanosleep(64);
+  }
+  __threadfence();
+  return p;
+}
+
+// Shifted residuals of the steps as they are published (each step's LDL^T
+// update of every shift depends on the previous one): per shift the LDL^T
+// pivot d and phi = last entry of (xi I + sign T_i)^{-1} e1, relative
+// residual beta_{i+1} |phi|.  Stops at the first step at which every shift
+// has converged, or at a breakdown step.  mp.mon[0] = the last step handled.
+__device__ __noinline__ void ms_monitor_cta(KState& st, const MsParams& mp, int i_begin, int i_end) {
+  __shared__ double red[32];
+  __shared__ int s_pub;
+  KCtrl* c = st.ctrl;
+  const bool one_warp = mp.N <= 32;
+  if (one_warp && threadIdx.x >= 32) return;
+  constexpr int kPer = 2;  // shifts per thread (N <= 2 * blockDim.x)
+  zc xi[kPer], d[kPer], phi[kPer];
+  bool act[kPer];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int j = threadIdx.x + q * blockDim.x;
+    act[q] = j < mp.N;
+    xi[q] = act[q] ? zmk(mp.xi[2 * j], mp.xi[2 * j + 1]) : zmk(0.0, 0.0);
+    d[q] = zmk(1.0, 0.0);
+    phi[q] = zmk(0.0, 0.0);
+    if (act[q] && i_begin > 1) {
+      d[q] = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
+      phi[q] = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
+    }
+  }
+  auto sync = [&]() {
+    if (one_warp) __syncwarp();
+    else __syncthreads();
+  };
+  int pub = i_begin - 1;
+  for (int i = i_begin; i < i_end; ++i) {
+    if (pub < i) {
+      if (threadIdx.x == 0) s_pub = monitor_wait_pub(c, i);
+      sync();
+      pub = s_pub;
+      sync();
+      if (pub < 0) return;
+    }
+    const int bd = *(volatile int*)&c->bd_step;  // 0: no breakdown (steps count from 1)
+    const bool last_valid = bd != 0 && i >= bd;
+    const double alpha = HAT(st, i, i);
+    const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
+    const double bnext = HAT(st, i + 1, i);
+    double r = 0.0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      if (!act[q]) continue;
+      const zc a = zadd(xi[q], zmk(mp.sign * alpha, 0.0));
+      if (i == 1) {
+        d[q] = a;
+        const double id = 1.0 / (cuCreal(a) * cuCreal(a) + cuCimag(a) * cuCimag(a));
+        phi[q] = zmk(cuCreal(a) * id, -cuCimag(a) * id);  // 1 / d
+      } else {
+        const double b = mp.sign * bi;
+        // d = a - b^2 / d_prev ; phi = -b phi_prev / d
+        const double ip = (b * b) / (cuCreal(d[q]) * cuCreal(d[q]) + cuCimag(d[q]) * cuCimag(d[q]));
+        d[q] = zmk(cuCreal(a) - cuCreal(d[q]) * ip, cuCimag(a) + cuCimag(d[q]) * ip);
+        const double id = 1.0 / (cuCreal(d[q]) * cuCreal(d[q]) + cuCimag(d[q]) * cuCimag(d[q]));
+        const zc num = zmk(-b * cuCreal(phi[q]), -b * cuCimag(phi[q]));
+        phi[q] = zmk((cuCreal(num) * cuCreal(d[q]) + cuCimag(num) * cuCimag(d[q])) * id,
+                     (cuCimag(num) * cuCreal(d[q]) - cuCreal(num) * cuCimag(d[q])) * id);
+      }
+      const double rq = bnext * sqrt(cuCreal(phi[q]) * cuCreal(phi[q]) + cuCimag(phi[q]) * cuCimag(phi[q]));
+      mp.resid[threadIdx.x + q * blockDim.x] = rq;
+      r = fmax(r, rq);
+    }
+    const double worst = one_warp ? warp_max(r) : block_max(r, red);
+    const bool stop = worst < mp.eps || last_valid;
+    if (threadIdx.x == 0) {
+      mp.mon[0] = i;
+      c->errnum = worst;
+      c->errden = 1.0;
+      if (stop) {
+        c->done = 1;
+        c->conv = 1;
+        if (st.host_flag) st.host_flag[0] = 1;
+        __threadfence();
+        *(volatile int*)&c->stop_req = 1;
+      }
+    }
+    if (stop || i + 1 == i_end) {
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        if (!act[q]) continue;
+        const int j = threadIdx.x + q * blockDim.x;
+        mp.d[2 * j] = cuCreal(d[q]);
+        mp.d[2 * j + 1] = cuCimag(d[q]);
+        mp.phi[2 * j] = cuCreal(phi[q]);
+        mp.phi[2 * j + 1] = cuCimag(phi[q]);
+      }
+      return;
+    }
+  }
+}
+
+// The a posteriori estimate of istop = 1 (estimate_body) for the
+// iterations i = 2 .. i_end-1 of a solve, beside the steps: estimate i waits
+// for step i-1 to be published.  A breakdown found at the end of step i-1
+// ends the estimates there (psfun_d_lanczos.f90:225-230); on convergence the
+// estimate records itx and yk (estimate_tail) and asks the steps to stop.
+// One block: the dense evaluation runs without a helper group.
+__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end) {
+  __shared__ DenseSmem dsm;
+  __shared__ int s_pub;
+  KCtrl* c = st.ctrl;
+  dense_group_begin(dsm, nullptr);
+  int pub = i_begin - 1;
+  for (int i = max(2, i_begin + 1); i < i_end; ++i) {
+    if (pub < i - 1) {
+      if (threadIdx.x == 0) s_pub = monitor_wait_pub(c, i - 1);
+      __syncthreads();
+      pub = s_pub;
+      __syncthreads();
+      if (pub < 0) return;
+    }
+    if (*(volatile int*)&c->bd_step == i - 1) return;  // 0: no breakdown (i - 1 >= 1)
+    estimate_body(st, mon.fp, i, mon.eps, mon.tridiag, dsm, false);
+    __syncthreads();
+    if (*(volatile int*)&c->done) {  // converged (or failed): stop the steps
+      if (threadIdx.x == 0) {
+        __threadfence();
+        *(volatile int*)&c->stop_req = 1;
+      }
+      return;
+    }
+  }
 }
 
 // USERF estimate tail: yk was produced by the host-assisted path.
@@ -716,6 +956,30 @@ __device__ void final_body(KState& st, const FunParams& fp, int tridiag, int kee
     c->yk_len = yk_len;
     c->nterms = nterms;
     c->derr = (c->errden > 0.0) ? c->errnum / c->errden : c->errnum;
+  }
+}
+
+// Concurrent Arnoldi estimates, after all of them: the first converged
+// iteration j becomes the solve's convergence (itx, yk of its slot, its error
+// words), as the serial loop would have stopped there; without one, the error
+// words of the last estimate (iteration i_last).
+__global__ void k_par_select(KState st, const double* yk_all, int ldy, int i_last) {
+  KCtrl* c = st.ctrl;
+  const int j = c->conv_first;
+  if (c->beta0 == 0.0 || c->info != 0) return;
+  if (j != 0x7fffffff) {
+    const int m = j - 1;
+    for (int l = threadIdx.x; l < m; l += blockDim.x) st.yk[l] = yk_all[(size_t)j * ldy + l];
+    if (threadIdx.x == 0) {
+      c->conv = 1;
+      c->yk_len = m;
+      c->itx = m;
+      c->errnum = st.errn_all[j];
+      c->errden = st.errd_all[j];
+    }
+  } else if (threadIdx.x == 0 && i_last >= 2) {
+    c->errnum = st.errn_all[i_last];
+    c->errden = st.errd_all[i_last];
   }
 }
 
@@ -875,32 +1139,53 @@ static void spmv_kernel_attrs() {
   if (done) return;
   spmv_smem_attr(k_lz_spmv);
   spmv_smem_attr(k_ar_spmv);
-  cudaFuncSetAttribute(k_lz_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
+  cudaFuncSetAttribute(k_lz_persist<LZ_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
+  cudaFuncSetAttribute(k_lz_persist<LZ_MON_SHIFTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
+  cudaFuncSetAttribute(k_lz_persist<LZ_MON_ESTIMATE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kLzSmemBytes);
   done = true;
 }
 
-// Cooperative grid of the persistent Lanczos kernel: every CTA co-resident.
+// Cooperative grid of a persistent Lanczos kernel: every CTA co-resident.
+template <int MODE>
 static int persist_grid() {
   static int g = 0;
   if (g == 0) {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lz_persist, kSpmvThreads, kLzSmemBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lz_persist<MODE>, kSpmvThreads, kLzSmemBytes);
     if (per < 1) per = 1;
     g = sm_count() * per;
   }
   return g;
 }
 
-static int launch_lz_persist(KState& st, const CsrDev& A, int i_begin, int i_end, cudaStream_t s) {
-  int G = persist_grid();
+// Steps [i_begin, i_end) in one cooperative launch; with a monitor the grid
+// holds the compute CTAs and the monitor block.
+template <int MODE>
+static int launch_lz_persist_mode(KState& st, const CsrDev& A, int i_begin, int i_end, const LzMonitor& mon,
+                                  cudaStream_t s) {
+  const int extra = (MODE == LZ_PLAIN) ? 0 : 1;
+  int G = persist_grid<MODE>() - extra;
+  if (G < 1) {
+    set_last_error("persistent Lanczos: no room for the monitor block");
+    return PSFUN_ERR_CUDA;
+  }
   int tpc = (A.ntiles + G - 1) / G;
   if (tpc < 1) tpc = 1;
   G = (A.ntiles + tpc - 1) / tpc;
   if (G < 1) G = 1;
-  void* args[] = {(void*)&st, (void*)&A, (void*)&i_begin, (void*)&i_end, (void*)&tpc};
-  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_lz_persist, dim3(G), dim3(kSpmvThreads), args, kLzSmemBytes, s));
+  LzMonitor m = mon;
+  void* args[] = {(void*)&st, (void*)&A, (void*)&i_begin, (void*)&i_end, (void*)&tpc, (void*)&m};
+  PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_lz_persist<MODE>, dim3(G + extra), dim3(kSpmvThreads), args,
+                                       kLzSmemBytes, s));
   count_launch();
   return PSFUN_SUCCESS;
+}
+
+static int launch_lz_persist(KState& st, const CsrDev& A, int i_begin, int i_end, cudaStream_t s) {
+  LzMonitor none;
+  memset(&none, 0, sizeof none);
+  return launch_lz_persist_mode<LZ_PLAIN>(st, A, i_begin, i_end, none, s);
 }
 
 static int grid_for(int64_t items, int threads, int per_sm) {
@@ -914,7 +1199,9 @@ static int grid_for(int64_t items, int threads, int per_sm) {
 // Grid and rows per block of k_ar_mgs_sm for n rows, or 0 when the rows of a
 // block do not fit in shared memory.
 static int mgs_sm_plan(int64_t n, int* chunk) {
-  const int G = sm_count();
+  // at least 2048 rows per block: a small basis needs few blocks, and each
+  // sweep's grid barrier costs less with fewer arrivals
+  const int G = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (n + 2047) / 2048));
   int64_t ch = (n + G - 1) / G;
   ch = (ch + 1) & ~(int64_t)1;
   const size_t bytes = kMgsSmFixed + sizeof(double) * (size_t)ch;
@@ -1103,7 +1390,18 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     return PSFUN_SUCCESS;
   };
 
-  if (istop == 2 && !userf && !prof_enabled() && !sai) {
+  // istop = 1 Lanczos whose estimate runs on one block: every step and every
+  // estimate in one persistent launch (the estimate on its monitor block)
+  const bool lz_mon = istop == 1 && !arnoldi && !sai && !userf && dense_blocks(fpk, nl + 1, true) == 1;
+  auto launch_lz_estimating = [&]() -> int {
+    LzMonitor mon;
+    memset(&mon, 0, sizeof mon);
+    mon.fp = fpk;
+    mon.eps = eps;
+    mon.tridiag = 1;
+    return launch_lz_persist_mode<LZ_MON_ESTIMATE>(st, A, 1, nl + 1, mon, s);
+  };
+  if ((istop == 2 || lz_mon) && !userf && !prof_enabled() && !sai) {
     // fixed-length solve: one CUDA graph, captured once per launch key
     // the device arrays of the matrix are part of the key: a handle can be
     // destroyed and another created at the same address
@@ -1111,8 +1409,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       const void* a; const void* x; void* y; const void* V; int64_t n; int nl, arnoldi, keeplast, gs, gv, gm;
       FunParams fp; double scaling;
       const void *irp, *ja, *val, *tiles;
+      int istop; double eps;
     } key;
     memset(&key, 0, sizeof key);
+    key.istop = istop; key.eps = eps;
     key.irp = A.irp; key.ja = A.ja; key.val = A.val; key.tiles = A.tile_desc;
     key.a = a; key.x = x; key.y = y; key.V = st.V; key.n = n; key.nl = nl; key.arnoldi = arnoldi;
     key.keeplast = meth->keeplast; key.gs = gs; key.gv = gv; key.gm = gm; key.fp = fpk; key.scaling = scaling;
@@ -1125,7 +1425,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_prologue(false);
       if (!arnoldi) {
-        if (rc == PSFUN_SUCCESS) rc = launch_lz_persist(st, A, 1, nl + 1, s);  // every step, one launch
+        if (rc == PSFUN_SUCCESS) rc = lz_mon ? launch_lz_estimating() : launch_lz_persist(st, A, 1, nl + 1, s);
       } else {
         for (int i = 2; i <= nl && rc == PSFUN_SUCCESS; ++i) rc = enqueue_step(i);
       }
@@ -1142,12 +1442,12 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     }
     PSF_CUDA(cudaGraphLaunch(meth->graph, s));
     count_launch(meth->graph_kernels);
-  } else if (istop == 2 && !arnoldi) {
-    // fixed-length Lanczos with per-launch timing on: the same single
-    // persistent launch as the graph, timed under the Lanczos slot
+  } else if ((istop == 2 || lz_mon) && !arnoldi && !userf && !sai) {
+    // Lanczos with per-launch timing on: the same single persistent launch as
+    // the graph, timed under the Lanczos slot
     PSF_TRY(enqueue_prologue(false));
     prof_begin(PROF_LZ_SPMV, s);
-    PSF_TRY(launch_lz_persist(st, A, 1, nl + 1, s));
+    PSF_TRY(lz_mon ? launch_lz_estimating() : launch_lz_persist(st, A, 1, nl + 1, s));
     prof_end(PROF_LZ_SPMV, s);
     PSF_TRY(enqueue_epilogue(0));
   } else {
@@ -1155,36 +1455,70 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     if (sai) {  // the inner solves run host-synchronously: stop at once on a zero x
       PSF_CUDA(cudaStreamSynchronize(s));
     }
-    const int max_ahead = 24;
-    // Lanczos with a one-block estimate: the estimate of iteration i needs
-    // only T(1:i-1) and beta_i, so it runs on a second stream while step i's
-    // Lanczos kernel runs (on the SM that kernel leaves free), and step i+1
-    // waits for it.  Step i was computed before the estimate in any case.
-    static cudaStream_t s2 = nullptr;
-    static cudaEvent_t ev_step = nullptr, ev_est = nullptr;
-    const bool overlap = istop == 1 && !arnoldi && !sai && !userf && dense_blocks(fpk, nl + 1, tridiag != 0) == 1;
-    if (overlap && !s2) {
-      PSF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
-      PSF_CUDA(cudaEventCreateWithFlags(&ev_step, cudaEventDisableTiming));
-      PSF_CUDA(cudaEventCreateWithFlags(&ev_est, cudaEventDisableTiming));
+    // Arnoldi with istop = 1 (not SAI, not USERF): the estimates run
+    // concurrently on kParStreams side streams, estimate i once step i-1 is
+    // done, while the steps go on without waiting for them; every estimate
+    // writes its own yk slot and error words, and the first converged
+    // iteration is taken afterwards (k_par_select), as the serial loop would
+    // have stopped there.  Steps computed past it write later basis slots and
+    // columns of H only.  (Lanczos with istop = 1 runs in one launch above,
+    // or, for the dense variants that need a group of blocks, serially here.)
+    const bool par = istop == 1 && arnoldi && !sai && !userf;
+    constexpr int kParStreams = 4;
+    static cudaStream_t side[kParStreams] = {};
+    static cudaEvent_t ev_side[kParStreams] = {};
+    static cudaEvent_t ev_steps[kParStreams] = {};
+    double* yk_all = nullptr;
+    double* par_scr = nullptr;
+    double* par_grp = nullptr;
+    size_t par_fs = 0, grp_d = 0;
+    const size_t ldh_ = (size_t)nl + 1;
+    if (par) {
+      if (!side[0]) {
+        for (int k = 0; k < kParStreams; ++k) {
+          PSF_CUDA(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+          PSF_CUDA(cudaEventCreateWithFlags(&ev_side[k], cudaEventDisableTiming));
+          PSF_CUDA(cudaEventCreateWithFlags(&ev_steps[k], cudaEventDisableTiming));
+        }
+      }
+      // every region starts on a 256-byte boundary (the complex f(H) variants
+      // access their scratch as 16-byte pairs)
+      auto al32 = [](size_t d) { return (d + 31) & ~(size_t)31; };
+      par_fs = al32(fh_scratch_doubles(nl + 1, fp.phiorder) + 64);
+      grp_d = al32((sizeof(DenseGroup) + 7) / 8 + 8);
+      const size_t o_errn = al32(ldh_ * ldh_), o_errd = o_errn + al32(ldh_ + 2), o_scr = o_errd + al32(ldh_ + 2);
+      const size_t o_grp = o_scr + kParStreams * par_fs;
+      const size_t need = o_grp + kParStreams * grp_d + 64;
+      PSF_TRY(meth->par.ensure(sizeof(double) * need));
+      double* pb = meth->par.as<double>();
+      yk_all = pb;
+      st.errn_all = pb + o_errn;
+      st.errd_all = pb + o_errd;
+      par_scr = pb + o_scr;
+      par_grp = pb + o_grp;
+      PSF_CUDA(cudaEventRecord(ev_steps[0], s));  // the side streams start after the prologue
+      for (int k = 0; k < kParStreams; ++k) PSF_CUDA(cudaStreamWaitEvent(side[k], ev_steps[0], 0));
     }
+    const int max_ahead = par ? 3 : 24;
+    int i_last = 0;
     for (int i = 2; i <= nl; ++i) {
       if ((istop == 1 || sai) && hflag[0]) break;
-      if (overlap) {
-        PSF_CUDA(cudaEventRecord(ev_step, s));  // steps 1..i-1 are done
-        PSF_CUDA(cudaStreamWaitEvent(s2, ev_step, 0));
-        int ii = i, td = tridiag;
+      PSF_TRY(enqueue_step(i));
+      if (par) {
+        const int k = i % kParStreams;
+        PSF_CUDA(cudaEventRecord(ev_steps[k], s));  // steps 1..i done
+        PSF_CUDA(cudaStreamWaitEvent(side[k], ev_steps[k], 0));
+        KState ste = st;
+        ste.yk = yk_all + (size_t)i * ldh_;
+        ste.fscratch = par_scr + (size_t)k * par_fs;
+        int ii = i, td = 0;
         double e = eps;
         DenseGroup* g = nullptr;
-        void* args[] = {(void*)&st, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&td, (void*)&g};
-        PSF_TRY(launch_dense((const void*)k_estimate, 1, meth->dgroup.as<DenseGroup>(), &g, args, s2));
-        PSF_CUDA(cudaEventRecord(ev_est, s2));
-        PSF_TRY(enqueue_step(i));
-        PSF_CUDA(cudaStreamWaitEvent(s, ev_est, 0));  // step i+1 sees the convergence decision
-      } else {
-        PSF_TRY(enqueue_step(i));
-      }
-      if (istop == 1 && !overlap) {
+        void* args[] = {(void*)&ste, (void*)&fpk, (void*)&ii, (void*)&e, (void*)&td, (void*)&g};
+        DenseGroup* grp_k = reinterpret_cast<DenseGroup*>(par_grp + (size_t)k * grp_d);
+        PSF_TRY(launch_dense((const void*)k_estimate, dense_blocks(fpk, i, false), grp_k, &g, args, side[k]));
+        i_last = i;
+      } else if (istop == 1) {
         if (sai) {
           {
             double tau = meth->tau;
@@ -1224,6 +1558,15 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
           if (spin > 200000000L) break;
         }
       }
+    }
+    if (par) {  // join the estimates, then take the first converged iteration
+      for (int k = 0; k < kParStreams; ++k) {
+        PSF_CUDA(cudaEventRecord(ev_side[k], side[k]));
+        PSF_CUDA(cudaStreamWaitEvent(s, ev_side[k], 0));
+      }
+      k_par_select<<<1, kDenseThreads, 0, s>>>(st, yk_all, (int)ldh_, i_last);
+      count_launch();
+      PSF_CUDA(cudaGetLastError());
     }
     if (userf) {
       PSF_CUDA(cudaStreamSynchronize(s));
@@ -1357,86 +1700,6 @@ int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, 
 // leading A is applied through the Lanczos relation A V_m = V_{m+1} Tbar_m, so
 // y = eta V_{m+1} (Tbar_m g) is one recombination pass over the basis.
 // ===========================================================================
-struct MsParams {
-  int N;
-  const double* xi;  // 2N
-  const double* c;   // 2N
-  double sign, eta, eps;
-  double* d;      // 2N: LDL pivots of the last step
-  double* phi;    // 2N
-  double* resid;  // N
-  int* mon;       // [0]: the monitor's last step (its own word: the monitor
-                  // of one chunk runs while the next chunk's Lanczos steps do)
-};
-
-// Shifted residuals of Lanczos steps i0..i1-1 (in order; each step's LDL^T
-// update of every shift depends on the previous one).  Stops at the first
-// step at which every shift has converged, or at a breakdown: c->itx is that
-// step and the Lanczos steps computed after it are ignored.
-__global__ void k_ms_monitor(KState st, MsParams mp, int i0, int i1) {
-  // one thread per shift (blockDim.x >= N); the recurrence of each shift
-  // stays in registers over the chunk and a complex division is one
-  // reciprocal of a squared modulus and products
-  __shared__ double red[32];
-  KCtrl* c = st.ctrl;
-  if (c->done) return;
-  const int ibd = c->breakdown ? c->itx : i1;  // a breakdown found at step itx ends the basis there
-  const int j = threadIdx.x;
-  const bool act = j < mp.N;
-  const zc xi = act ? zmk(mp.xi[2 * j], mp.xi[2 * j + 1]) : zmk(0.0, 0.0);
-  zc d = zmk(1.0, 0.0), phi = zmk(0.0, 0.0);
-  if (act && i0 > 1) {
-    d = zmk(mp.d[2 * j], mp.d[2 * j + 1]);
-    phi = zmk(mp.phi[2 * j], mp.phi[2 * j + 1]);
-  }
-  for (int i = i0; i < i1; ++i) {
-    const bool last_valid = i >= ibd;
-    const double alpha = HAT(st, i, i);
-    const double bi = (i >= 2) ? HAT(st, i, i - 1) : 0.0;
-    const double bnext = HAT(st, i + 1, i);
-    double r = 0.0;
-    if (act) {
-      const zc a = zadd(xi, zmk(mp.sign * alpha, 0.0));
-      if (i == 1) {
-        d = a;
-        const double id = 1.0 / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
-        phi = zmk(cuCreal(d) * id, -cuCimag(d) * id);  // 1 / d
-      } else {
-        const double b = mp.sign * bi;
-        // d = a - b^2 / d_prev ; phi = -b phi_prev / d
-        const double ip = (b * b) / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
-        d = zmk(cuCreal(a) - cuCreal(d) * ip, cuCimag(a) + cuCimag(d) * ip);
-        const double id = 1.0 / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
-        const zc num = zmk(-b * cuCreal(phi), -b * cuCimag(phi));
-        phi = zmk((cuCreal(num) * cuCreal(d) + cuCimag(num) * cuCimag(d)) * id,
-                  (cuCimag(num) * cuCreal(d) - cuCreal(num) * cuCimag(d)) * id);
-      }
-      r = bnext * sqrt(cuCreal(phi) * cuCreal(phi) + cuCimag(phi) * cuCimag(phi));
-      mp.resid[j] = r;
-    }
-    const double worst = (blockDim.x == 32) ? warp_max(r) : block_max(r, red);
-    const bool stop = worst < mp.eps || last_valid;
-    if (threadIdx.x == 0) {
-      mp.mon[0] = i;
-      c->errnum = worst;
-      c->errden = 1.0;
-      if (stop) {
-        c->done = 1;
-        c->conv = 1;
-        if (st.host_flag) st.host_flag[0] = 1;
-      }
-    }
-    if (stop || i + 1 == i1) {
-      if (act) {
-        mp.d[2 * j] = cuCreal(d);
-        mp.d[2 * j + 1] = cuCimag(d);
-        mp.phi[2 * j] = cuCreal(phi);
-        mp.phi[2 * j + 1] = cuCimag(phi);
-      }
-      return;
-    }
-  }
-}
 
 // Solves the N shifted tridiagonal systems of dimension m, forms the
 // coefficients of y = eta V_{m+1} Tbar_m g, g = Im(sum_j c_j z_j).
@@ -1613,45 +1876,15 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
   k_init<<<gv, kVecThreads, 0, s>>>(st, b);
   count_launch();
-  // Lanczos steps in chunks of kMsChunk, each one persistent cooperative
-  // launch, followed by the shifted-residual monitor of the chunk; at most
-  // kMsChunk - 1 steps run past convergence.
-  constexpr int kMsChunk = 8;
-  constexpr int kMsOverlapFrom = 32;
-  // Past the first kMsOverlapFrom steps, the monitor of a chunk runs on a
-  // second stream, concurrently with the next chunk's Lanczos steps (it reads
-  // only the chunk's T entries and writes its own words); one more chunk may
-  // then run past convergence, which only long solves can afford.
-  static cudaStream_t s2 = nullptr;
-  static cudaEvent_t ev_lz = nullptr, ev_mon = nullptr;
-  if (!s2) {
-    PSF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
-    PSF_CUDA(cudaEventCreateWithFlags(&ev_lz, cudaEventDisableTiming));
-    PSF_CUDA(cudaEventCreateWithFlags(&ev_mon, cudaEventDisableTiming));
-  }
+  // Every Lanczos step in one persistent cooperative launch; its monitor
+  // block advances the shifted recurrences as the steps are published and
+  // stops the steps at the first step at which every shift has converged.
   PSF_CUDA(cudaMemsetAsync(mp.mon, 0, sizeof(int), s));
-  PSF_CUDA(cudaEventRecord(ev_lz, s));
-  PSF_CUDA(cudaStreamWaitEvent(s2, ev_lz, 0));  // the monitor stream starts after the setup
-  for (int i = 1; i <= nl; i += kMsChunk) {
-    if (hflag[0]) break;
-    const int i1 = std::min(i + kMsChunk, nl + 1);
-    PSF_TRY(launch_lz_persist(st, A, i, i1, s));
-    cudaStream_t smon = s;
-    if (i > kMsOverlapFrom) {
-      PSF_CUDA(cudaEventRecord(ev_lz, s));
-      PSF_CUDA(cudaStreamWaitEvent(s2, ev_lz, 0));
-      smon = s2;
-    }
-    k_ms_monitor<<<1, std::min(1024, 32 * ((N + 31) / 32)), 0, smon>>>(st, mp, i, i1);
-    count_launch();
-    PSF_CUDA(cudaGetLastError());
-    for (long spin = 0; i - hflag[1] > 32 && !hflag[0]; ++spin) {
-      if (cudaStreamQuery(s) == cudaSuccess) break;
-      if (spin > 200000000L) break;
-    }
-  }
-  PSF_CUDA(cudaEventRecord(ev_mon, s2));
-  PSF_CUDA(cudaStreamWaitEvent(s, ev_mon, 0));  // everything after waits for the last monitor
+  LzMonitor mon;
+  memset(&mon, 0, sizeof mon);
+  mon.mp = mp;
+  PSF_TRY(launch_lz_persist_mode<LZ_MON_SHIFTS>(st, A, 1, nl + 1, mon, s));
+  PSF_CUDA(cudaGetLastError());
   KCtrl hc;
   int hmon = 0;
   PSF_CUDA(cudaMemcpyAsync(&hc, st.ctrl, sizeof hc, cudaMemcpyDeviceToHost, s));
@@ -1881,7 +2114,8 @@ __global__ void k_dot_final(const double* part, int nb, double* out) {
 int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps, int itmax,
                         int recompute, double* y, double* grad_x, double* grad_t, double* grad_vals, int* iters) {
   if (!a || !x || !g) return PSFUN_ERR_INVALID_VECT_STATE;
-  if (nquad < 4 || (nquad & 1) || itmax < 2 || t == 0.0) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  // the shift monitor handles up to 1024 shifts (the nodes of half the contour)
+  if (nquad < 4 || nquad > 2048 || (nquad & 1) || itmax < 2 || t == 0.0) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   {
     int sym = 0;
     PSF_TRY(csr_symmetric(a, &sym));
