@@ -79,6 +79,19 @@ def lib():
                               C.c_int, C.POINTER(C.c_int), _dp]
         L.orc_dcg_hist.argtypes = [C.POINTER(OrcCsr), _dp, _dp, C.c_double, C.c_double, _dp, C.c_double, C.c_int,
                                    C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
+        L.orc_bjac_build.argtypes = [C.POINTER(OrcCsr), C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_bjac_free.argtypes = [C.c_void_p]
+        L.orc_bjac_free.restype = None
+        L.orc_bjac_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_bjac_apply.restype = None
+        L.orc_bjac_export.argtypes = [C.c_void_p, _ip, _ip, _dp, _ip, _dp]
+        L.orc_bjac_export.restype = C.c_int64
+        L.orc_dcg_bjac_hist.argtypes = [C.POINTER(OrcCsr), C.c_void_p, _dp, C.c_double, C.c_double, _dp, C.c_double,
+                                        C.c_int, C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
+        L.orc_saiarnoldi_bjac.argtypes = [C.POINTER(OrcSerial), C.POINTER(OrcCsr), C.c_void_p, C.c_double, C.c_int,
+                                          C.c_int, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double), _dp, C.c_int,
+                                          C.POINTER(C.c_int)]
         L.orc_horner.argtypes = [_dp, C.c_int, C.c_double]
         L.orc_horner.restype = C.c_double
         L.orc_ellipkkp.argtypes = [C.c_double, _dp]
@@ -176,6 +189,46 @@ def diag_inv(A: Csr):
     return np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 1.0)
 
 
+BJAC_BLOCK_ROWS = 32  # rows per diagonal block of the BJAC preconditioner
+
+
+class Bjac:
+    """Block-Jacobi ILU(0) factors of A (orc_bjac_build), blocks of bs rows."""
+
+    def __init__(self, A: Csr, bs: int = BJAC_BLOCK_ROWS):
+        self.A = A
+        h = C.c_void_p()
+        info = lib().orc_bjac_build(C.byref(A.s), int(bs), C.byref(h))
+        if info != 0:
+            raise ValueError(f"orc_bjac_build: info={info}")
+        self.h = h
+
+    def apply(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros_like(r)
+        lib().orc_bjac_apply(self.h, _p(r), _p(z))
+        return z
+
+    def factors(self):
+        n = len(self.A.irp) - 1
+        irp = np.zeros(n + 1, dtype=np.int32)
+        lib().orc_bjac_export(self.h, irp.ctypes.data_as(_ip), None, None, None, None)
+        nz = int(irp[-1])
+        ja = np.zeros(nz, dtype=np.int32)
+        val = np.zeros(nz)
+        dpos = np.zeros(n, dtype=np.int32)
+        udinv = np.zeros(n)
+        lib().orc_bjac_export(self.h, irp.ctypes.data_as(_ip), ja.ctypes.data_as(_ip), _p(val),
+                              dpos.ctypes.data_as(_ip), _p(udinv))
+        return dict(irp=irp, ja=ja, val=val, dpos=dpos, udinv=udinv)
+
+    def __del__(self):
+        try:
+            lib().orc_bjac_free(self.h)
+        except Exception:
+            pass
+
+
 def saiarnoldi(fun, A: Csr, x, eps, tau=0.0, prec="NONE", initmax=200, inistop=1, itmax=200, istop=1,
                drop_last=True):
     """psfun_d_saiarnoldi with kmethd 'CG' (krylov/rational/psfun_d_sai.f90)."""
@@ -185,6 +238,12 @@ def saiarnoldi(fun, A: Csr, x, eps, tau=0.0, prec="NONE", initmax=200, inistop=1
     err = C.c_double(0.0)
     res = np.zeros(itmax + 2)
     nres = C.c_int(0)
+    if prec.upper() == "BJAC":
+        P = Bjac(A)
+        info = lib().orc_saiarnoldi_bjac(C.byref(fun), C.byref(A.s), P.h, float(tau), int(initmax), int(inistop),
+                                         _p(y), _p(x), eps, itmax, istop, 1 if drop_last else 0, C.byref(it),
+                                         C.byref(err), _p(res), len(res), C.byref(nres))
+        return dict(y=y, info=info, iter=it.value, err=err.value, res=res[: nres.value].copy())
     dinv = diag_inv(A) if prec.upper() == "DIAG" else None
     info = lib().orc_saiarnoldi(C.byref(fun), C.byref(A.s), _p(dinv) if dinv is not None else None, float(tau),
                                 int(initmax), int(inistop), _p(y), _p(x), eps, itmax, istop, 1 if drop_last else 0,
@@ -193,6 +252,9 @@ def saiarnoldi(fun, A: Csr, x, eps, tau=0.0, prec="NONE", initmax=200, inistop=1
 
 
 def dcg(A: Csr, b, eta, zeta, x0=None, eps=1e-7, itmax=1000, istop=2, prec="NONE"):
+    if prec.upper() == "BJAC":
+        r = dcg_cond(A, b, eta, zeta, x0, eps, itmax, istop, prec)
+        return dict(x=r["x"], info=r["info"], iter=r["iter"], err=r["err"])
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
     dinv = diag_inv(A) if prec.upper() == "DIAG" else None
@@ -218,8 +280,13 @@ def dcg_cond(A: Csr, b, eta, zeta, x0=None, eps=1e-7, itmax=1000, istop=2, prec=
     td = np.zeros(max(itmax, 1))
     tu = np.zeros(max(itmax, 1))
     eh = np.zeros(max(itmax, 1))
-    info = lib().orc_dcg_hist(C.byref(A.s), _p(dinv) if dinv is not None else None, _p(b), eta, zeta, _p(x), eps,
-                              itmax, istop, C.byref(it), C.byref(err), _p(td), _p(tu), C.byref(nt), _p(eh))
+    if prec.upper() == "BJAC":
+        P = Bjac(A)
+        info = lib().orc_dcg_bjac_hist(C.byref(A.s), P.h, _p(b), eta, zeta, _p(x), eps, itmax, istop, C.byref(it),
+                                       C.byref(err), _p(td), _p(tu), C.byref(nt), _p(eh))
+    else:
+        info = lib().orc_dcg_hist(C.byref(A.s), _p(dinv) if dinv is not None else None, _p(b), eta, zeta, _p(x),
+                                  eps, itmax, istop, C.byref(it), C.byref(err), _p(td), _p(tu), C.byref(nt), _p(eh))
     m = nt.value
     cond = 0.0
     if m > 0:

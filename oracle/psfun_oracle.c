@@ -774,6 +774,135 @@ done:
 }
 
 /* ------------------------------------------------------------------------ */
+/* BJAC preconditioner: block Jacobi over the diagonal blocks of bs          */
+/* consecutive rows [bs*k, bs*k + bs), each block factored by ILU(0)          */
+/* (incomplete LU with the block's own sparsity pattern; Saad, Iterative      */
+/* Methods for Sparse Linear Systems, 2nd ed., Algorithm 10.4, the IKJ        */
+/* order).  This is AMG4PSBLAS's 'BJAC' type (block Jacobi, ILU(0) on each    */
+/* block) with one block per bs rows in place of one block per MPI rank.      */
+/* Per row the block's entries are kept in column order with a diagonal slot  */
+/* (0 when A stores none); duplicates are summed; a zero pivot becomes 1, as  */
+/* DIAG's zero diagonal.  Apply: z = U^{-1} L^{-1} r block by block, forward  */
+/* then backward, multiplying by the stored reciprocal pivots.                */
+/* ------------------------------------------------------------------------ */
+struct orc_bjac {
+  int64_t n;
+  int bs;
+  int32_t* irp; /* n + 1 */
+  int32_t* ja;
+  double* val;  /* L below the diagonal slot (unit diagonal), U from it */
+  int32_t* dpos;
+  double* udinv; /* 1 / U(i,i) */
+};
+
+static int cmp_i32d(const void* a, const void* b) {
+  const int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+  return (x > y) - (x < y);
+}
+
+int orc_bjac_build(const orc_csr* A, int bs, orc_bjac** out) {
+  *out = NULL;
+  if (bs < 1) return ORC_ERR_INVALID_ARGS_COMBINATION;
+  const int64_t n = A->n;
+  orc_bjac* P = (orc_bjac*)calloc(1, sizeof(orc_bjac));
+  P->n = n;
+  P->bs = bs;
+  P->irp = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n + 1));
+  P->dpos = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  P->udinv = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  int64_t cap = 0;
+  for (int64_t i = 0; i < n; ++i) cap += (A->irp[i + 1] - A->irp[i]) + 1;
+  P->ja = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cap > 0 ? cap : 1));
+  P->val = (double*)malloc(sizeof(double) * (size_t)(cap > 0 ? cap : 1));
+  int64_t maxrow = 1;
+  for (int64_t i = 0; i < n; ++i)
+    if (A->irp[i + 1] - A->irp[i] + 1 > maxrow) maxrow = A->irp[i + 1] - A->irp[i] + 1;
+  int32_t* cols = (int32_t*)malloc(sizeof(int32_t) * (size_t)maxrow);
+  int64_t pos = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t r0 = (i / bs) * bs, r1 = (r0 + bs < n) ? r0 + bs : n;
+    int m = 0;
+    for (int32_t k = A->irp[i]; k < A->irp[i + 1]; ++k)
+      if (A->ja[k] >= r0 && A->ja[k] < r1) cols[m++] = A->ja[k];
+    cols[m++] = (int32_t)i;
+    qsort(cols, (size_t)m, sizeof(int32_t), cmp_i32d);
+    P->irp[i] = (int32_t)pos;
+    for (int q = 0; q < m; ++q) {
+      if (q > 0 && cols[q] == cols[q - 1]) continue;
+      if (cols[q] == i) P->dpos[i] = (int32_t)pos;
+      P->ja[pos] = cols[q];
+      P->val[pos] = 0.0;
+      ++pos;
+    }
+    /* values: stored entries summed into their slots, in stored order */
+    for (int32_t k = A->irp[i]; k < A->irp[i + 1]; ++k) {
+      const int32_t c = A->ja[k];
+      if (c < r0 || c >= r1) continue;
+      for (int64_t e = P->irp[i]; e < pos; ++e)
+        if (P->ja[e] == c) { P->val[e] += A->val[k]; break; }
+    }
+  }
+  P->irp[n] = (int32_t)pos;
+  free(cols);
+  /* ILU(0), IKJ order: row i eliminates its lower entries in column order */
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t di = P->dpos[i], ie = P->irp[i + 1];
+    for (int32_t e = P->irp[i]; e < di; ++e) {
+      const int32_t c = P->ja[e];
+      const double lic = P->val[e] / P->val[P->dpos[c]];
+      P->val[e] = lic;
+      /* a(i,j) -= l(i,c) u(c,j) for the j > c stored in both rows */
+      int32_t g = e + 1;
+      for (int32_t f = P->dpos[c] + 1; f < P->irp[c + 1]; ++f) {
+        const int32_t j = P->ja[f];
+        while (g < ie && P->ja[g] < j) ++g;
+        if (g < ie && P->ja[g] == j) P->val[g] -= lic * P->val[f];
+      }
+    }
+    if (P->val[di] == 0.0) P->val[di] = 1.0;
+    P->udinv[i] = 1.0 / P->val[di];
+  }
+  *out = P;
+  return 0;
+}
+
+void orc_bjac_free(orc_bjac* P) {
+  if (!P) return;
+  free(P->irp); free(P->ja); free(P->val); free(P->dpos); free(P->udinv); free(P);
+}
+
+/* z = M^{-1} r */
+void orc_bjac_apply(const orc_bjac* P, const double* r, double* z) {
+  const int64_t n = P->n;
+  const int64_t nb = (n + P->bs - 1) / P->bs;
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t r0 = b * P->bs, r1 = (r0 + P->bs < n) ? r0 + P->bs : n;
+    for (int64_t i = r0; i < r1; ++i) {
+      double s = r[i];
+      for (int32_t e = P->irp[i]; e < P->dpos[i]; ++e) s -= P->val[e] * z[P->ja[e]];
+      z[i] = s;
+    }
+    for (int64_t i = r1 - 1; i >= r0; --i) {
+      double s = z[i];
+      for (int32_t e = P->dpos[i] + 1; e < P->irp[i + 1]; ++e) s -= P->val[e] * z[P->ja[e]];
+      z[i] = s * P->udinv[i];
+    }
+  }
+}
+
+/* The factors (for tests): irp (n+1), ja/val (nnz of the factors), dpos, udinv. */
+int64_t orc_bjac_export(const orc_bjac* P, int32_t* irp, int32_t* ja, double* val, int32_t* dpos, double* udinv) {
+  const int64_t nz = P->irp[P->n];
+  if (irp) memcpy(irp, P->irp, sizeof(int32_t) * (size_t)(P->n + 1));
+  if (ja) memcpy(ja, P->ja, sizeof(int32_t) * (size_t)nz);
+  if (val) memcpy(val, P->val, sizeof(double) * (size_t)nz);
+  if (dpos) memcpy(dpos, P->dpos, sizeof(int32_t) * (size_t)P->n);
+  if (udinv) memcpy(udinv, P->udinv, sizeof(double) * (size_t)P->n);
+  return nz;
+}
+
+/* ------------------------------------------------------------------------ */
 /* psfun_dcg_vect, krylov/shifted/psfun_dcg.F90:249-335, with the PSBLAS     */
 /* stopping rule (psb_init_conv / psb_check_conv / psb_end_conv):            */
 /*   istop 1: ||r||_inf <= eps (||A||_inf ||x||_inf + ||b||_inf)             */
@@ -787,18 +916,31 @@ done:
  * the variables keeping their values across restarts), and errnum/errden of
  * every iteration's stopping test (errh, NaN where none ran).  td, tu, errh
  * (capacity itmax) and nt may be NULL. */
-int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
-                 double* x, double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu,
-                 int* nt, double* errh);
+static int dcg_core(const orc_csr* A, const double* prec_diag_inv, const orc_bjac* bj, const double* b,
+                    double eta, double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err,
+                    double* td, double* tu, int* nt, double* errh);
 
 int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
             double* x, double eps, int itmax, int istop, int* iter, double* err) {
-  return orc_dcg_hist(A, prec_diag_inv, b, eta, zeta, x, eps, itmax, istop, iter, err, NULL, NULL, NULL, NULL);
+  return dcg_core(A, prec_diag_inv, NULL, b, eta, zeta, x, eps, itmax, istop, iter, err, NULL, NULL, NULL, NULL);
 }
 
 int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
                  double* x, double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu,
                  int* nt, double* errh) {
+  return dcg_core(A, prec_diag_inv, NULL, b, eta, zeta, x, eps, itmax, istop, iter, err, td, tu, nt, errh);
+}
+
+/* The same with the BJAC preconditioner P (orc_bjac_build). */
+int orc_dcg_bjac_hist(const orc_csr* A, const orc_bjac* P, const double* b, double eta, double zeta, double* x,
+                      double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu, int* nt,
+                      double* errh) {
+  return dcg_core(A, NULL, P, b, eta, zeta, x, eps, itmax, istop, iter, err, td, tu, nt, errh);
+}
+
+static int dcg_core(const orc_csr* A, const double* prec_diag_inv, const orc_bjac* bj, const double* b,
+                    double eta, double zeta, double* x, double eps, int itmax, int istop, int* iter, double* err,
+                    double* td, double* tu, int* nt, double* errh) {
   if (istop < 1 || istop > 2) return ORC_ERR_INVALID_ISTOP;
   if (!b || !x) return ORC_ERR_INVALID_VECT_STATE;
   int64_t n = A->n;
@@ -831,7 +973,9 @@ int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b,
     for (;;) {
       it = it + 1;
       itx = itx + 1;
-      if (prec_diag_inv) {
+      if (bj) {
+        orc_bjac_apply(bj, r, z);
+      } else if (prec_diag_inv) {
         for (int64_t i = 0; i < n; ++i) z[i] = prec_diag_inv[i] * r[i];
       } else {
         memcpy(z, r, sizeof(double) * n);
@@ -891,9 +1035,28 @@ int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b,
 /* estimate converged, applies f to H itself (:346-368).  Both as in the    */
 /* reference.  f is evaluated with scaling 1 (:185-186).                   */
 /* ------------------------------------------------------------------------ */
+static int sai_core(orc_serial* fun, const orc_csr* A, const double* prec_diag_inv, const orc_bjac* bj, double tau,
+                    int initmax, int inistop, double* y, const double* x, double eps, int itmax, int istop,
+                    int drop_last, int* iter, double* err, double* res, int res_cap, int* nres);
+
 int orc_saiarnoldi(orc_serial* fun, const orc_csr* A, const double* prec_diag_inv, double tau, int initmax,
                    int inistop, double* y, const double* x, double eps, int itmax, int istop, int drop_last,
                    int* iter, double* err, double* res, int res_cap, int* nres) {
+  return sai_core(fun, A, prec_diag_inv, NULL, tau, initmax, inistop, y, x, eps, itmax, istop, drop_last, iter, err,
+                  res, res_cap, nres);
+}
+
+/* The same with the BJAC preconditioner P on the inner CG. */
+int orc_saiarnoldi_bjac(orc_serial* fun, const orc_csr* A, const orc_bjac* P, double tau, int initmax, int inistop,
+                        double* y, const double* x, double eps, int itmax, int istop, int drop_last, int* iter,
+                        double* err, double* res, int res_cap, int* nres) {
+  return sai_core(fun, A, NULL, P, tau, initmax, inistop, y, x, eps, itmax, istop, drop_last, iter, err, res,
+                  res_cap, nres);
+}
+
+static int sai_core(orc_serial* fun, const orc_csr* A, const double* prec_diag_inv, const orc_bjac* bj, double tau,
+                    int initmax, int inistop, double* y, const double* x, double eps, int itmax, int istop,
+                    int drop_last, int* iter, double* err, double* res, int res_cap, int* nres) {
   if (istop < 1 || istop > 2) return ORC_ERR_INVALID_ISTOP; /* :127-133 */
   if (!x || !y) return ORC_ERR_INVALID_VECT_STATE;         /* :148-157 */
   int64_t n = A->n;
@@ -931,7 +1094,8 @@ int orc_saiarnoldi(orc_serial* fun, const orc_csr* A, const double* prec_diag_in
     itx = itx + 1;
     int cit = 0;
     double cerr = 0.0;
-    if (orc_dcg(A, prec_diag_inv, V_(i - 1), 1.0, tau, w, eps, initmax, inistop, &cit, &cerr) != 0) {
+    if (dcg_core(A, prec_diag_inv, bj, V_(i - 1), 1.0, tau, w, eps, initmax, inistop, &cit, &cerr, NULL, NULL, NULL,
+                 NULL) != 0) {
       info = ORC_ERR_FROM_SUBROUTINE_NON;
       goto done;
     }

@@ -75,6 +75,25 @@ int orc_lanczos(orc_serial* fun, const orc_csr* A, double* y, const double* x, d
 /* --- shifted CG ------------------------------------------------------------ */
 int orc_dcg(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
             double* x, double eps, int itmax, int istop, int* iter, double* err);
+int orc_dcg_hist(const orc_csr* A, const double* prec_diag_inv, const double* b, double eta, double zeta,
+                 double* x, double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu,
+                 int* nt, double* errh);
+
+/* --- BJAC preconditioner (block Jacobi, ILU(0) blocks of bs rows) --------- */
+typedef struct orc_bjac orc_bjac;
+int orc_bjac_build(const orc_csr* A, int bs, orc_bjac** out);
+void orc_bjac_free(orc_bjac* P);
+void orc_bjac_apply(const orc_bjac* P, const double* r, double* z);
+int64_t orc_bjac_export(const orc_bjac* P, int32_t* irp, int32_t* ja, double* val, int32_t* dpos, double* udinv);
+int orc_dcg_bjac_hist(const orc_csr* A, const orc_bjac* P, const double* b, double eta, double zeta, double* x,
+                      double eps, int itmax, int istop, int* iter, double* err, double* td, double* tu, int* nt,
+                      double* errh);
+int orc_saiarnoldi(orc_serial* fun, const orc_csr* A, const double* prec_diag_inv, double tau, int initmax,
+                   int inistop, double* y, const double* x, double eps, int itmax, int istop, int drop_last,
+                   int* iter, double* err, double* res, int res_cap, int* nres);
+int orc_saiarnoldi_bjac(orc_serial* fun, const orc_csr* A, const orc_bjac* P, double tau, int initmax, int inistop,
+                        double* y, const double* x, double eps, int itmax, int istop, int drop_last, int* iter,
+                        double* err, double* res, int res_cap, int* nres);
 
 /* --- elliptic / quadrature ------------------------------------------------- */
 double orc_horner(const double* coeffs, int n, double x);

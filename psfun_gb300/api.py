@@ -224,7 +224,8 @@ class PsfunDKrylov:
 
     def precinit(self, ptype: str) -> int:
         """meth%precinit(ctxt, ptype, info) (psfun_d_prec_init,
-        krylov/psfun_d_krylov_mod.F90:326-361): 'NOPREC'/'NONE' or 'DIAG'."""
+        krylov/psfun_d_krylov_mod.F90:326-361): 'NOPREC'/'NONE', 'DIAG' or 'BJAC'
+        (block Jacobi, ILU(0) on the diagonal blocks of 32 rows)."""
         return _lib().psfun_gpu_krylov_precinit(self.handle, ptype.encode())
 
     def precbuild(self, a: CsrMatrix) -> int:
@@ -396,7 +397,7 @@ def expm_adjoint(a: CsrMatrix, t: float, x, g=None, nquad: int = 32, eps: float 
 def psb_krylov(method: str, a: CsrMatrix, prec: str, b, eta: float, zeta: float, x, eps: float,
                itmax: int = 1000, istop: int = 2, itrace: int = 0, cond: bool = False):
     """psb_krylov(method,a,prec,b,eta,zeta,x,eps,desc_a,info,itmax,iter,err,itrace,istop,cond)
-    for (eta A + zeta I) x = b (psfun_dkrylov_vect).  prec is 'NONE' or 'DIAG'.
+    for (eta A + zeta I) x = b (psfun_dkrylov_vect).  prec is 'NONE', 'DIAG' or 'BJAC'.
     x is the initial guess.  Returns (x, info, iter, err), and cond as a fifth
     element when cond=True (the reference's optional condition estimate)."""
     it = C.c_int(0)

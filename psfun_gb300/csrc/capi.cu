@@ -355,6 +355,11 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
 int psfun_gpu_csr_destroy(psfun_csr* a) {
   if (!a) return PSFUN_SUCCESS;
   if (a->T) psfun_gpu_csr_destroy(a->T);
+  if (a->bj_val) cudaFree(a->bj_val);
+  if (a->bj_col) cudaFree(a->bj_col);
+  if (a->bj_rowoff) cudaFree(a->bj_rowoff);
+  if (a->bj_cnt) cudaFree(a->bj_cnt);
+  if (a->bj_udinv) cudaFree(a->bj_udinv);
   if (a->irp) cudaFree(a->irp);
   if (a->ja) cudaFree(a->ja);
   if (a->val) cudaFree(a->val);
@@ -385,8 +390,7 @@ int psfun_gpu_csr_is_symmetric(psfun_csr* a, int* sym) {
 
 namespace psf {
 
-// The matrix back on the host (0-based CSR).
-static int csr_download(psfun_csr* a, std::vector<int32_t>& irp, std::vector<int32_t>& ja, std::vector<double>& val) {
+int csr_download(psfun_csr* a, std::vector<int32_t>& irp, std::vector<int32_t>& ja, std::vector<double>& val) {
   irp.resize(a->n + 1);
   ja.resize(a->nnz);
   val.resize(a->nnz);
@@ -681,6 +685,7 @@ int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char
     const std::string v = upper_key(val);
     if (v == "NONE" || v == "NOPREC") meth->prec = 0;
     else if (v == "DIAG") meth->prec = 1;
+    else if (v == "BJAC") meth->prec = 2;
     else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
     return PSFUN_SUCCESS;
   }
@@ -691,8 +696,10 @@ int psfun_gpu_krylov_precinit(psfun_krylov* meth, const char* ptype) {
   const std::string v = upper_key(ptype);
   if (v == "NONE" || v == "NOPREC") meth->prec = 0;
   else if (v == "DIAG") meth->prec = 1;
+  else if (v == "BJAC") meth->prec = 2;
   else {
-    psf::set_last_error("precinit: preconditioner type '" + v + "' is not available (NOPREC, NONE and DIAG are)");
+    psf::set_last_error("precinit: preconditioner type '" + v +
+                        "' is not available (NOPREC, NONE, DIAG and BJAC are)");
     return PSFUN_ERR_FROM_SUBROUTINE;
   }
   return PSFUN_SUCCESS;
@@ -701,6 +708,7 @@ int psfun_gpu_krylov_precbuild(psfun_krylov* meth, psfun_csr* a) {
   psf::NvtxRange nvtx_range("psfun_gpu_krylov_precbuild");
   if (!meth || !a) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   if (meth->prec == 1) PSF_TRY(psf::csr_build_diag_inv(a));
+  if (meth->prec == 2) PSF_TRY(psf::csr_build_bjac(a));
   return PSFUN_SUCCESS;
 }
 int psfun_gpu_krylov_set_real(psfun_krylov* meth, const char* what, double val) {

@@ -6,8 +6,10 @@
 // psb_end_conv, documented in the PSBLAS user guide):
 //   istop 1: ||r||_inf <= eps * (||A||_inf ||x||_inf + ||b||_inf)
 //   istop 2: ||r||_2   <= eps * ||b||_2
-// and the iteration also ends once itx >= itmax.  Preconditioners: NONE and
-// DIAG (Jacobi from the diagonal of A, the shifted.inp:8 choice).
+// and the iteration also ends once itx >= itmax.  Preconditioners: NONE,
+// DIAG (Jacobi from the diagonal of A, the shifted.inp:8 choice) and BJAC
+// (AMG4PSBLAS's block Jacobi with ILU(0) blocks, here blocks of kBjacRows
+// consecutive rows in place of one block per MPI rank).
 //
 // The restart and all iterations run in one persistent cooperative kernel
 // (k_cg_persist below); the host only relaunches it after a breakdown.
@@ -38,6 +40,12 @@ struct CgState {
   double *x, *r, *p, *q, *z;
   const double* b;
   const double* dinv;
+  // BJAC factors (bj_val null unless BJAC): the warp layout of psfun_csr
+  const double* bj_val;
+  const uint8_t* bj_col;
+  const int32_t* bj_rowoff;
+  const uchar2* bj_cnt;
+  const double* bj_udinv;
   double* part;   // partial sums (3 per block)
   CgCtrl* c;
   volatile int* host_flag;
@@ -56,11 +64,60 @@ struct EpiResid {
   PSF_DEVINL void operator()(int r, double s) {
     const double v = fma(-st->zeta, st->x[r], fma(-st->eta, s, st->b[r]));
     st->r[r] = v;
+    if (st->bj_val) return;  // BJAC: z and r.z after the block solves
     const double zz = st->dinv ? st->dinv[r] * v : v;
     st->z[r] = zz;
     acc = fma(v, zz, acc);
   }
 };
+
+// BJAC: z = U^{-1} L^{-1} r on the diagonal blocks that start in the rows
+// [rb, re) of this CTA.  A warp takes a group of 32 consecutive blocks, one
+// per lane, so that each load of the factors is 32 consecutive values; a
+// lane keeps its block's 32 entries of z in a local array (forward sweep,
+// then backward with the reciprocal pivots).  A block can end in the next
+// CTA's rows, so the caller has completed r with a grid barrier.  Returns the
+// thread's partial r.z.
+PSF_DEVINL double bjac_solve_blocks(const CgState& st, int rb, int re) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int64_t kb0 = (rb + kBjacRows - 1) / kBjacRows, kb1 = (re + kBjacRows - 1) / kBjacRows;
+  double acc = 0.0;
+  if (kb0 >= kb1) return acc;
+  const int64_t g0 = kb0 / 32, g1 = (kb1 - 1) / 32 + 1;
+  for (int64_t g = g0 + warp; g < g1; g += nwarps) {
+    const int64_t b = g * 32 + lane;
+    const bool mine = b >= kb0 && b < kb1;
+    const int64_t row0 = b * kBjacRows;
+    double zl[kBjacRows];
+#pragma unroll
+    for (int k = 0; k < kBjacRows; ++k) zl[k] = (mine && row0 + k < st.n) ? st.r[row0 + k] : 0.0;
+    const int32_t* ro = st.bj_rowoff + g * kBjacRows;
+    const uchar2* cn = st.bj_cnt + g * kBjacRows;
+    for (int r = 0; r < kBjacRows; ++r) {  // forward: unit lower L
+      const int64_t o = (int64_t)ro[r] * 32 + lane;
+      const int nl = cn[r].x;
+      double s = zl[r];
+      for (int e = 0; e < nl; ++e) s = fma(-st.bj_val[o + 32 * e], zl[st.bj_col[o + 32 * e]], s);
+      zl[r] = s;
+    }
+    for (int r = kBjacRows - 1; r >= 0; --r) {  // backward: U, reciprocal pivots
+      const int nl = cn[r].x, nu = cn[r].y;
+      const int64_t o = ((int64_t)ro[r] + nl) * 32 + lane;
+      double s = zl[r];
+      for (int e = 0; e < nu; ++e) s = fma(-st.bj_val[o + 32 * e], zl[st.bj_col[o + 32 * e]], s);
+      zl[r] = s * st.bj_udinv[((g * kBjacRows) + r) * 32 + lane];
+    }
+    if (mine) {
+#pragma unroll
+      for (int k = 0; k < kBjacRows; ++k)
+        if (row0 + k < st.n) {
+          st.z[row0 + k] = zl[k];
+          acc = fma(st.r[row0 + k], zl[k], acc);
+        }
+    }
+  }
+  return acc;
+}
 
 // ||b||_inf, ||b||_2
 __global__ void __launch_bounds__(kCgThreads) k_cg_bnorm(CgState st) {
@@ -134,6 +191,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
   auto drain = [&]() { pipe_drain(sm, pc, passes * (unsigned)(t1 - t0)); };
   auto gsync = [&]() -> bool { return grid_sync_to(&c->bar, (++nb) * (unsigned)G, &c->err); };
   const int bd = blockDim.x;
+  const bool bj = st.bj_val != nullptr;
   // ---- restart: r = b - eta A x - zeta x ; z = D r ; rho = r.z (:256-260)
   {
     EpiResid epi{&st, 0.0};
@@ -142,9 +200,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
       return;
     }
     ++passes;
-    block_sum_store_512(epi.acc, sm.vals, sm.red, &part[bid]);
+    if (!bj) block_sum_store_512(epi.acc, sm.vals, sm.red, &part[bid]);
   }
   if (!gsync()) { drain(); return; }
+  if (bj) {  // z = M^{-1} r once r is complete, then rho = r.z
+    block_sum_store_512(bjac_solve_blocks(st, rb, re), sm.vals, sm.red, &part[bid]);
+    if (!gsync()) { drain(); return; }
+  }
   {
     const double S = partials_sum_to0(part, G, sm.red);
     if (threadIdx.x == 0) {
@@ -230,9 +292,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
       st.x[r] = xv;
       const double rv = fma(-alpha, qv, ro);
       st.r[r] = rv;
-      const double zv = st.dinv ? dv * rv : rv;
-      st.z[r] = zv;
-      a_rz = fma(rv, zv, a_rz);
+      if (!bj) {
+        const double zv = st.dinv ? dv * rv : rv;
+        st.z[r] = zv;
+        a_rz = fma(rv, zv, a_rz);
+      }
       if (st.istop == 1) {
         a_r = fmax(a_r, fabs(rv));
         a_x = fmax(a_x, fabs(xv));
@@ -258,7 +322,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
       }
       for (; r < re; r += bd) upd(r, st.p[r], st.x[r], st.q[r], st.r[r], st.dinv ? st.dinv[r] : 1.0);
     }
-    block_sum_store_512(a_rz, sm.vals, sm.red, &part[2 * G + bid]);
+    if (!bj) block_sum_store_512(a_rz, sm.vals, sm.red, &part[2 * G + bid]);
     if (st.istop == 1) {
       block_max_store_512(a_r, sm.vals, sm.red, &part[3 * G + bid]);
       block_max_store_512(a_x, sm.vals, sm.red, &part[4 * G + bid]);
@@ -266,6 +330,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_cg_persist(CgState st, CsrDev 
       block_sum_store_512(a_r, sm.vals, sm.red, &part[3 * G + bid]);
     }
     if (!gsync()) { drain(); return; }
+    if (bj) {  // z = M^{-1} r once r is complete, then the partial r.z
+      __syncthreads();  // the norm reductions above are done with vals/red
+      block_sum_store_512(bjac_solve_blocks(st, rb, re), sm.vals, sm.red, &part[2 * G + bid]);
+      if (!gsync()) { drain(); return; }
+    }
     {
       const double s_rz = partials_sum_to0(part + 2 * G, G, sm.red);
       double s_r, s_x = 0.0;
@@ -362,6 +431,146 @@ int csr_build_diag_inv(psfun_csr* a) {
   return PSFUN_SUCCESS;
 }
 
+// BJAC: ILU(0) of each diagonal block of kBjacRows consecutive rows, built
+// on the host from the matrix's own arrays and cached on the handle.  Per row
+// the block's entries in column order with a diagonal slot (0 when A stores
+// none), duplicates summed; incomplete LU in the IKJ order (Saad, Iterative
+// Methods for Sparse Linear Systems, 2nd ed., Algorithm 10.4): row i
+// eliminates its lower entries in column order, l(i,c) = a(i,c) / u(c,c) and
+// a(i,j) -= l(i,c) u(c,j) for the j > c stored in both rows; a zero pivot
+// becomes 1 (as DIAG's zero diagonal).  The factors are then laid out for the
+// warp solve (see psfun_csr).
+int csr_build_bjac(psfun_csr* a) {
+  if (a->bj_val) return PSFUN_SUCCESS;
+  std::vector<int32_t> irp, ja;
+  std::vector<double> val;
+  PSF_TRY(csr_download(a, irp, ja, val));
+  const int64_t n = a->n;
+  std::vector<int32_t> birp(n + 1), bja, bdpos(n > 0 ? n : 1);
+  std::vector<double> bval, budinv(n > 0 ? n : 1);
+  bja.reserve(ja.size() + n);
+  bval.reserve(ja.size() + n);
+  std::vector<int32_t> cols;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t r0 = (i / kBjacRows) * kBjacRows, r1 = std::min<int64_t>(n, r0 + kBjacRows);
+    cols.clear();
+    for (int32_t k = irp[i]; k < irp[i + 1]; ++k)
+      if (ja[k] >= r0 && ja[k] < r1) cols.push_back(ja[k]);
+    cols.push_back((int32_t)i);
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    birp[i] = (int32_t)bja.size();
+    for (int32_t c : cols) {
+      if (c == i) bdpos[i] = (int32_t)bja.size();
+      bja.push_back(c);
+      bval.push_back(0.0);
+    }
+    for (int32_t k = irp[i]; k < irp[i + 1]; ++k) {  // stored entries summed into their slots, in stored order
+      const int32_t c = ja[k];
+      if (c < r0 || c >= r1) continue;
+      for (size_t e = birp[i]; e < bja.size(); ++e)
+        if (bja[e] == c) { bval[e] += val[k]; break; }
+    }
+  }
+  birp[n] = (int32_t)bja.size();
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t di = bdpos[i], ie = birp[i + 1];
+    for (int32_t e = birp[i]; e < di; ++e) {
+      const int32_t c = bja[e];
+      const double lic = bval[e] / bval[bdpos[c]];
+      bval[e] = lic;
+      int32_t g = e + 1;
+      for (int32_t f = bdpos[c] + 1; f < birp[c + 1]; ++f) {
+        const int32_t j = bja[f];
+        while (g < ie && bja[g] < j) ++g;
+        if (g < ie && bja[g] == j) bval[g] -= lic * bval[f];
+      }
+    }
+    if (bval[di] == 0.0) bval[di] = 1.0;
+    budinv[i] = 1.0 / bval[di];
+  }
+  // warp layout: groups of 32 blocks, one lane per block
+  const int64_t nblk = (n + kBjacRows - 1) / kBjacRows, ngrp = (nblk + 31) / 32;
+  std::vector<int32_t> rowoff((size_t)ngrp * kBjacRows);
+  std::vector<uchar2> cnt((size_t)ngrp * kBjacRows);
+  int64_t slots = 0;
+  for (int64_t g = 0; g < ngrp; ++g)
+    for (int r = 0; r < kBjacRows; ++r) {
+      int ml = 0, mu = 0;
+      for (int l = 0; l < 32; ++l) {
+        const int64_t i = (g * 32 + l) * kBjacRows + r;
+        if (i >= n) continue;
+        ml = std::max(ml, bdpos[i] - birp[i]);
+        mu = std::max(mu, birp[i + 1] - bdpos[i] - 1);
+      }
+      if (ml > 255 || mu > 255) {
+        set_last_error("csr_build_bjac: a block row holds more than 255 entries on one side of the diagonal");
+        return PSFUN_ERR_INVALID_MATRIX;
+      }
+      rowoff[g * kBjacRows + r] = (int32_t)slots;
+      cnt[g * kBjacRows + r] = make_uchar2((unsigned char)ml, (unsigned char)mu);
+      slots += ml + mu;
+    }
+  if (slots * 32 > 0x7fffffffLL) {
+    set_last_error("csr_build_bjac: factors too large for 32-bit slot offsets");
+    return PSFUN_ERR_INVALID_MATRIX;
+  }
+  std::vector<double> wval((size_t)std::max<int64_t>(slots, 1) * 32, 0.0);
+  std::vector<uint8_t> wcol((size_t)std::max<int64_t>(slots, 1) * 32, 0);
+  std::vector<double> wud((size_t)ngrp * kBjacRows * 32, 0.0);
+  for (int64_t g = 0; g < ngrp; ++g)
+    for (int r = 0; r < kBjacRows; ++r) {
+      const int64_t o = rowoff[g * kBjacRows + r];
+      const int ml = cnt[g * kBjacRows + r].x;
+      for (int l = 0; l < 32; ++l) {
+        const int64_t blk = g * 32 + l, i = blk * kBjacRows + r;
+        if (i >= n) continue;
+        const int64_t base = blk * kBjacRows;
+        int e = 0;
+        for (int32_t k = birp[i]; k < bdpos[i]; ++k, ++e) {
+          wval[(size_t)(o + e) * 32 + l] = bval[k];
+          wcol[(size_t)(o + e) * 32 + l] = (uint8_t)(bja[k] - base);
+        }
+        e = 0;
+        for (int32_t k = bdpos[i] + 1; k < birp[i + 1]; ++k, ++e) {
+          wval[(size_t)(o + ml + e) * 32 + l] = bval[k];
+          wcol[(size_t)(o + ml + e) * 32 + l] = (uint8_t)(bja[k] - base);
+        }
+        wud[(size_t)(g * kBjacRows + r) * 32 + l] = budinv[i];
+      }
+    }
+  cudaStream_t s = stream();
+  auto fail = [&](cudaError_t e) {
+    (void)cudaGetLastError();
+    set_last_error(std::string("csr_build_bjac: ") + cudaGetErrorString(e));
+    cudaFree(a->bj_val); cudaFree(a->bj_col); cudaFree(a->bj_rowoff); cudaFree(a->bj_cnt); cudaFree(a->bj_udinv);
+    a->bj_val = nullptr; a->bj_col = nullptr; a->bj_rowoff = nullptr; a->bj_cnt = nullptr; a->bj_udinv = nullptr;
+    return e == cudaErrorMemoryAllocation ? PSFUN_ERR_ALLOC_DEALLOC : PSFUN_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&a->bj_val, sizeof(double) * wval.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->bj_col, wcol.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->bj_rowoff, sizeof(int32_t) * rowoff.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->bj_cnt, sizeof(uchar2) * cnt.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&a->bj_udinv, sizeof(double) * wud.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMemcpyAsync(a->bj_val, wval.data(), sizeof(double) * wval.size(), cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return fail(e);
+  if ((e = cudaMemcpyAsync(a->bj_col, wcol.data(), wcol.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return fail(e);
+  if ((e = cudaMemcpyAsync(a->bj_rowoff, rowoff.data(), sizeof(int32_t) * rowoff.size(), cudaMemcpyHostToDevice,
+                           s)) != cudaSuccess)
+    return fail(e);
+  if ((e = cudaMemcpyAsync(a->bj_cnt, cnt.data(), sizeof(uchar2) * cnt.size(), cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return fail(e);
+  if ((e = cudaMemcpyAsync(a->bj_udinv, wud.data(), sizeof(double) * wud.size(), cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return fail(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(e);
+  return PSFUN_SUCCESS;
+}
+
 // Smallest and largest eigenvalue of the symmetric tridiagonal matrix with
 // diagonal d and off-diagonal e, by bisection on Sturm counts (the number of
 // negative pivots of the LDL^T factorisation of T - x I equals the number of
@@ -414,6 +623,7 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   PSF_TRY(ctrlb.ensure(sizeof(CgCtrl) + 64));
   PSF_TRY(partb.ensure(sizeof(double) * 3 * 4096));
   if (prec == 1) PSF_TRY(csr_build_diag_inv(a));
+  if (prec == 2) PSF_TRY(csr_build_bjac(a));
   CgState st;
   st.n = n;
   st.istop = istop;
@@ -429,6 +639,11 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
   st.q = st.p + ld;
   st.z = st.q + ld;
   st.dinv = (prec == 1) ? a->diag_inv : nullptr;
+  st.bj_val = (prec == 2) ? a->bj_val : nullptr;
+  st.bj_col = a->bj_col;
+  st.bj_rowoff = a->bj_rowoff;
+  st.bj_cnt = a->bj_cnt;
+  st.bj_udinv = a->bj_udinv;
   st.part = partb.as<double>();
   st.c = ctrlb.as<CgCtrl>();
   st.hist = nullptr;
@@ -541,6 +756,7 @@ static int parse_prec(const char* ptype, int* prec) {
   while (!k.empty() && k.back() == ' ') k.pop_back();
   if (k == "NONE" || k == "NOPREC") { *prec = 0; return 1; }
   if (k == "DIAG" || k == "JACOBI") { *prec = 1; return 1; }
+  if (k == "BJAC") { *prec = 2; return 1; }
   return 0;
 }
 

@@ -104,6 +104,19 @@ struct psfun_csr {
   int2* tile_desc = nullptr;   // per tile {first row, first stored entry}, ntiles + 1 entries
   int32_t max_tile_rows = 0;
   std::vector<double> h_diag;  // diagonal of A (host copy, for DIAG)
+  // BJAC preconditioner (lazy): ILU(0) factors of the diagonal blocks of
+  // kBjacRows consecutive rows, laid out for a warp that solves 32 blocks at
+  // once (lane = block): for block group g (blocks 32 g .. 32 g + 31) and row
+  // r of the blocks, the row's L then U entries as slots of 32 lanes
+  // (bj_val: value, bj_col: column within the block; zero padding to the
+  // group's longest row), bj_rowoff[32 g + r] the first slot, bj_cnt[32 g + r]
+  // the L and U slot counts, bj_udinv[(32 g + r) * 32 + lane] the reciprocal
+  // pivot.
+  double* bj_val = nullptr;
+  uint8_t* bj_col = nullptr;
+  int32_t* bj_rowoff = nullptr;
+  uchar2* bj_cnt = nullptr;
+  double* bj_udinv = nullptr;
   int sym = -1;                // A == A^T (pattern and values): 1 yes, 0 no, -1 not yet checked
   psfun_csr* T = nullptr;      // A^T as its own handle, built on first use (nonsymmetric A)
   psf::CsrDev dev() const {
@@ -157,6 +170,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
                         int* res_len);
 int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, double* y_dev, const double* x_dev);
 int csr_build_diag_inv(psfun_csr* a);
+constexpr int kBjacRows = 32;  // rows per diagonal block of the BJAC preconditioner
+int csr_build_bjac(psfun_csr* a);
+// The matrix back on the host (0-based CSR).
+int csr_download(psfun_csr* a, std::vector<int32_t>& irp, std::vector<int32_t>& ja, std::vector<double>& val);
 int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, double* x, double eps, int itmax,
               int istop, int* iter, double* err, int itrace = 0, double* cond = nullptr);
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,

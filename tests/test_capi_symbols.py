@@ -54,8 +54,9 @@ def test_precinit_types_without_gpu(lib):
     import psfun_gb300 as pg
     k = pg.PsfunDKrylov()
     assert k.precinit("NOPREC") == 0 and k.precinit("diag") == 0 and k.precinit("NONE") == 0
-    assert k.precinit("BJAC") == pg.api.ERR_FROM_SUBROUTINE
-    assert b"BJAC" in lib.psfun_gpu_last_error()
+    assert k.precinit("bjac") == 0
+    assert k.precinit("ML") == pg.api.ERR_FROM_SUBROUTINE
+    assert b"ML" in lib.psfun_gpu_last_error()
 
 
 def test_plot_residual_history(lib, tmp_path):

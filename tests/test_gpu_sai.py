@@ -27,7 +27,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("tau,istop,prec", [(0.0, 1, "NONE"), (0.0, 1, "DIAG"), (-1.0, 1, "NONE"),
-                                            (0.0, 2, "NONE")])
+                                            (0.0, 2, "NONE"), (0.0, 1, "BJAC")])
 def test_sai_vs_oracle(lib, orc, tau, istop, prec):
     A = -matrices.laplacian_2d(20)
     x = matrices.unit(np.random.default_rng(3).standard_normal(A.shape[0]))
@@ -75,6 +75,25 @@ def test_precinit_precbuild_diag(lib):
     a = pg.CsrMatrix.from_scipy(A)
     assert meth.set("KNAME", "SAIARNOLDI") == 0
     assert meth.precinit("DIAG") == 0 and meth.precbuild(a) == 0
+    r = meth.apply(fun, a, x, 1e-10, itmax=40, istop=1)
+    assert r.info == 0 and lazy.info == 0 and r.iter == lazy.iter
+    assert np.array_equal(r.y, lazy.y)
+
+
+def test_precinit_precbuild_bjac(lib):
+    """precinit('BJAC') + precbuild(a): the block-Jacobi ILU(0) factors built
+    before apply give the same result as building them on the first inner
+    solve."""
+    import psfun_gb300 as pg
+    A = -matrices.laplacian_2d(20)
+    x = matrices.unit(np.random.default_rng(5).standard_normal(A.shape[0]))
+    lazy = run_gpu(A, x, 1e-10, 0.0, 1, 40, "BJAC")
+    fun = pg.PsfunDSerial()
+    assert fun.set("VARIANT", "GENPADE") == 0
+    meth = pg.PsfunDKrylov()
+    a = pg.CsrMatrix.from_scipy(A)
+    assert meth.set("KNAME", "SAIARNOLDI") == 0
+    assert meth.precinit("BJAC") == 0 and meth.precbuild(a) == 0
     r = meth.apply(fun, a, x, 1e-10, itmax=40, istop=1)
     assert r.info == 0 and lazy.info == 0 and r.iter == lazy.iter
     assert np.array_equal(r.y, lazy.y)
