@@ -266,8 +266,30 @@ typedef struct {
 int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count, const psfun_batch_item* items,
                              double eps, int itmax, int istop, int* iters, double* errs, int* infos);
 
+/* No counterpart in the reference: the quadrature sum of a psfun_z_quadrature
+ * (quadratures/psfun_z_quadrature_mod.F90:42-55, the sum formed by
+ * psfun_gpu_z_quadrature_apply) for many instances in the same persistent
+ * launch as psfun_gpu_d_krylov_batch: per item and right-hand side
+ *   y = eta A Im(sum_j c_j (xi_j I + sign A)^{-1} x)
+ * with the item's own N shifts sharing the pair's Lanczos basis (the shifted
+ * residuals monitored every step, stop when all are below eps, at most itmax
+ * steps).  A must be symmetric (returns 111 otherwise). */
+typedef struct {
+  psfun_csr* a;     /* instance matrix (symmetric) */
+  int nrhs;         /* right-hand sides, 1..4, the same for every item */
+  const double* x;  /* device, n x nrhs column-major */
+  double* y;        /* device, n x nrhs column-major */
+  int N;            /* shifts, 1..1024 */
+  const double* xi; /* host, N interleaved complex shifts */
+  const double* c;  /* host, N interleaved complex weights */
+  double eta;
+  double sign;
+} psfun_quad_item;
+int psfun_gpu_z_quadrature_batch(int count, const psfun_quad_item* items, double eps, int itmax, int* iters,
+                                 double* errs, int* infos);
+
 /* ------------------------------------------------------------------------ */
-/* Adjoint of y = exp(t A) x, A symmetric (no counterpart in the reference).  */
+/* Adjoint of y = exp(t A) x (no counterpart in the reference).              */
 /* ------------------------------------------------------------------------ */
 /* Nodes / weights of the N-point optimized Talbot rule (Trefethen, Weideman,
  * Schmelzer, BIT 46 (2006)): exp(M) b ~ Re sum_k c_k (z_k I - M)^{-1} b over
@@ -275,12 +297,16 @@ int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count, c
 int psfun_gpu_talbot_rule(int N, double* z, double* c);
 /* Given g = dL/dy, computes (device pointers; any output may be NULL)
  *   y        = exp(tA) x
- *   grad_x   = exp(tA) g                       (second Lanczos run)
+ *   grad_x   = exp(tA^T) g                     (second Krylov run)
  *   *grad_t  = g^T A y                         (host scalar)
  *   grad_vals[k] = dL/dA_ij for the k-th stored entry (i,j) of A:
  *              t Re sum_k c_k [(z_k - tA)^{-1} g]_i [(z_k - tA)^{-1} x]_j
  * with the nquad-point Talbot rule; the shifted solutions share the two
- * Lanczos bases (stopped when every shifted FOM residual < eps).
+ * Lanczos bases (stopped when every shifted FOM residual < eps).  For a
+ * nonsymmetric A (checked once per handle) the two bases come from Arnoldi
+ * on A and on A^T (EXP/GENPADE, istop 1 with tolerance eps, at most itmax
+ * steps), grad_x = exp(tA^T) g, and grad_vals from Van Loan's block
+ * exponential of the two projected matrices (nquad is not used).
  * recompute = 1 keeps one basis in memory and rebuilds the forward one.
  * iters[2] receives the two Krylov dimensions. */
 int psfun_gpu_d_expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps,

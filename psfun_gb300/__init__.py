@@ -17,6 +17,7 @@ from .api import (  # noqa: F401
     hhtmethod1,
     talbot_rule,
     krylov_batch,
+    quadrature_batch,
     horner,
     psb_krylov,
 )

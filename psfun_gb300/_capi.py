@@ -23,6 +23,12 @@ class BatchItem(C.Structure):
                 ("scaling", C.c_double)]
 
 
+class QuadItem(C.Structure):
+    """psfun_quad_item"""
+    _fields_ = [("a", C.c_void_p), ("nrhs", C.c_int), ("x", C.c_void_p), ("y", C.c_void_p), ("N", C.c_int),
+                ("xi", C.c_void_p), ("c", C.c_void_p), ("eta", C.c_double), ("sign", C.c_double)]
+
+
 # name -> (restype, argtypes)
 PROTOS = {
     "psfun_gpu_version": (C.c_char_p, []),
@@ -62,6 +68,8 @@ PROTOS = {
                                                   C.POINTER(C.c_int), dp, dp, C.c_int, C.POINTER(C.c_int)]),
     "psfun_gpu_d_krylov_batch": (C.c_int, [vp, vp, C.c_int, C.POINTER(BatchItem), C.c_double, C.c_int, C.c_int,
                                             C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]),
+    "psfun_gpu_z_quadrature_batch": (C.c_int, [C.c_int, C.POINTER(QuadItem), C.c_double, C.c_int, C.POINTER(C.c_int),
+                                                dp, C.POINTER(C.c_int)]),
     "psfun_gpu_talbot_rule": (C.c_int, [C.c_int, dp, dp]),
     "psfun_gpu_d_expm_adjoint_device": (C.c_int, [vp, C.c_double, vp, vp, C.c_int, C.c_double, C.c_int, C.c_int, vp,
                                                   vp, dp, vp, C.POINTER(C.c_int)]),

@@ -356,6 +356,38 @@ def krylov_batch(meth: "PsfunDKrylov", fun: "PsfunDSerial", items, eps: float, i
     return info, infos.reshape(count, R), iters.reshape(count, R), errs.reshape(count, R)
 
 
+def quadrature_batch(items, eps: float = 1e-10, itmax: int = 2000):
+    """The quadrature sum y = eta A Im(sum_j c_j (xi_j I + sign A)^{-1} x) for
+    items [(CsrMatrix, X, Y, PsfunZQuadrature), ...] in one persistent launch
+    (the quadrature's own poles xi, weights c, eta and sign per item).  X, Y:
+    CUDA float64 tensors of shape (nrhs, n), the same nrhs for every item.
+    Returns (info, infos, iters, errs) with the per-pair arrays shaped
+    (count, nrhs)."""
+    count = len(items)
+    arr = (_capi.QuadItem * count)()
+    keep = []
+    R = int(items[0][1].shape[0])
+    for k, (a, X, Y, q) in enumerate(items):
+        if not (_is_device(X) and _is_device(Y)):
+            raise TypeError("quadrature_batch takes CUDA tensors")
+        N = len(q.xi)
+        xi = np.empty(2 * N)
+        xi[0::2], xi[1::2] = np.real(q.xi), np.imag(q.xi)
+        cw = np.empty(2 * N)
+        cw[0::2], cw[1::2] = np.real(q.c), np.imag(q.c)
+        keep += [xi, cw]
+        arr[k] = _capi.QuadItem(a.handle, int(X.shape[0]), X.data_ptr(), Y.data_ptr(), N, xi.ctypes.data,
+                                cw.ctypes.data, float(q.eta), float(q.sign))
+    iters = np.zeros(count * R, dtype=np.int32)
+    errs = np.zeros(count * R)
+    infos = np.zeros(count * R, dtype=np.int32)
+    _sync_stream()
+    info = _lib().psfun_gpu_z_quadrature_batch(count, arr, float(eps), int(itmax),
+                                               iters.ctypes.data_as(C.POINTER(C.c_int)), _dp(errs),
+                                               infos.ctypes.data_as(C.POINTER(C.c_int)))
+    return info, infos.reshape(count, R), iters.reshape(count, R), errs.reshape(count, R)
+
+
 def talbot_rule(N: int = 32):
     """Nodes z_k and weights c_k (N/2 of each) of the optimized Talbot rule:
     exp(M) b ~ Re sum_k c_k (z_k I - M)^{-1} b."""
@@ -369,9 +401,11 @@ def talbot_rule(N: int = 32):
 
 def expm_adjoint(a: CsrMatrix, t: float, x, g=None, nquad: int = 32, eps: float = 1e-15, itmax: int = 300,
                  recompute: bool = False, want=("y", "grad_x", "grad_t", "grad_vals")):
-    """y = exp(tA) x and, given g = dL/dy, the gradients dL/dx = exp(tA) g,
+    """y = exp(tA) x and, given g = dL/dy, the gradients dL/dx = exp(tA^T) g,
     dL/dt = g^T A y and dL/dA on the CSR pattern of A (one value per stored
-    entry).  x, g: CUDA float64 tensors.  Returns a dict of CUDA tensors / floats."""
+    entry).  Symmetric A: two Lanczos bases and the nquad-point Talbot rule;
+    nonsymmetric A: Arnoldi on A and A^T and Van Loan's block exponential.
+    x, g: CUDA float64 tensors.  Returns a dict of CUDA tensors / floats."""
     import torch
     out = {}
     y = torch.empty_like(x) if "y" in want else None

@@ -63,6 +63,14 @@ struct BInst {
   const double* X;
   double* Y;
   unsigned* cnt;  // [0] phase tile counter, [1] active pairs
+  // quadrature item (N > 0): y = eta A Im(sum_j c_j (xi_j I + sign A)^{-1} x)
+  // over the instance's Lanczos basis, in place of f(tA)x
+  int N;
+  int pad2;
+  const double* xi;  // 2N: shifts (interleaved complex)
+  const double* cw;  // 2N: weights
+  double eta, qsign;
+  double* msd;       // R * 4N: per pair and shift the LDL^T pivot d and phi of the last step
 };
 
 struct BatchArgs {
@@ -346,6 +354,196 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
   }
 }
 
+// ---- quadrature items ------------------------------------------------------
+// Step i of the shifted systems (xi_j I + sign T_i) of every live pair, the
+// LDL^T recurrence of the single-instance monitor (one thread per pair and
+// shift): d = a - b^2 / d_prev, phi = -b phi_prev / d with a = xi_j + sign
+// alpha_i, b = sign beta_i; relative residual beta_{i+1} |phi|.  The pair
+// stops at the first step at which every shift's residual is below eps (m = i),
+// at a breakdown (m = i, as converged) or after step nl (m = nl).
+template <int R>
+PSF_DEVINL void finalize_quad(const BInst& I, int i, const BatchArgs& B, const double* tot) {
+  const int nl = B.nl;
+  __shared__ unsigned long long worst[kBatchMaxRhs];  // max residual (non-negative doubles order as integers)
+  __shared__ int live_q[kBatchMaxRhs];
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < R; ++q) {
+      worst[q] = 0ull;
+      PairState& P = I.ps[q];
+      live_q[q] = !P.done;
+      if (P.done) continue;
+      const double sc = pa(I, q, PA_S, nl)[i];
+      const double wn = sqrt(tot[q]);
+      pa(I, q, PA_BETA, nl)[i + 1] = sc * wn;
+      pa(I, q, PA_S, nl)[i + 1] = 1.0 / ldexp(wn, ilog2_normal(sc));
+      P.itx = i;
+    }
+  }
+  __syncthreads();
+  for (int task = threadIdx.x; task < R * I.N; task += blockDim.x) {
+    const int q = task / I.N, j = task - q * I.N;
+    if (!live_q[q]) continue;
+    const double alpha = pa(I, q, PA_ALPHA, nl)[i];
+    const double bi = (i >= 2) ? pa(I, q, PA_BETA, nl)[i] : 0.0;
+    const double bnext = pa(I, q, PA_BETA, nl)[i + 1];
+    double* st = I.msd + ((size_t)q * I.N + j) * 4;
+    const zc a = zadd(zmk(I.xi[2 * j], I.xi[2 * j + 1]), zmk(I.qsign * alpha, 0.0));
+    zc d, phi;
+    if (i == 1) {
+      d = a;
+      const double id = 1.0 / (cuCreal(a) * cuCreal(a) + cuCimag(a) * cuCimag(a));
+      phi = zmk(cuCreal(a) * id, -cuCimag(a) * id);
+    } else {
+      const zc dp = zmk(st[0], st[1]), pp = zmk(st[2], st[3]);
+      const double b = I.qsign * bi;
+      const double ip = (b * b) / (cuCreal(dp) * cuCreal(dp) + cuCimag(dp) * cuCimag(dp));
+      d = zmk(cuCreal(a) - cuCreal(dp) * ip, cuCimag(a) + cuCimag(dp) * ip);
+      const double id = 1.0 / (cuCreal(d) * cuCreal(d) + cuCimag(d) * cuCimag(d));
+      const zc num = zmk(-b * cuCreal(pp), -b * cuCimag(pp));
+      phi = zmk((cuCreal(num) * cuCreal(d) + cuCimag(num) * cuCimag(d)) * id,
+                (cuCimag(num) * cuCreal(d) - cuCreal(num) * cuCimag(d)) * id);
+    }
+    st[0] = cuCreal(d);
+    st[1] = cuCimag(d);
+    st[2] = cuCreal(phi);
+    st[3] = cuCimag(phi);
+    const double r = fabs(bnext) * sqrt(cuCreal(phi) * cuCreal(phi) + cuCimag(phi) * cuCimag(phi));
+    atomicMax(&worst[q], (unsigned long long)__double_as_longlong(r));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int live = 0;
+    for (int q = 0; q < R; ++q) {
+      if (!live_q[q]) continue;
+      PairState& P = I.ps[q];
+      const double w = __longlong_as_double((long long)worst[q]);
+      pa(I, q, PA_RS, nl)[i + 1] = w;
+      P.errnum = w;
+      P.errden = 1.0;
+      const bool breakdown = fabs(pa(I, q, PA_BETA, nl)[i + 1]) < 1e-16;
+      if (w < B.eps || breakdown) {
+        P.done = 1;
+        P.conv = 1;
+        P.yk_len = i;
+      } else if (i + 1 > nl) {
+        P.done = 1;
+        P.yk_len = i;
+      } else {
+        ++live;
+      }
+    }
+    if (live == 0 && I.cnt[1] != 0) atomicSub(B.active, 1u);
+    I.cnt[1] = live;
+  }
+}
+
+// The quadrature item's assembly coefficients: per pair the N shifted
+// tridiagonal systems (xi_j I + sign T_m) z_j = beta0 e1 by banded
+// elimination with adjacent-row pivoting (one thread per pair and shift, rows
+// of U in the pair's scratch), g = Im(sum_j c_j z_j), h = Tbar_m g (m + 1
+// entries) and coef_r = eta h_r s_{r+1}: y = eta V_{m+1} Tbar_m g.
+template <int R>
+PSF_DEVINL void final_quad(const BInst& I, const BatchArgs& B) {
+  const int nl = B.nl;
+  const size_t stride = (size_t)(nl + 2);
+  __shared__ int bad[kBatchMaxRhs];
+  if (threadIdx.x < R) bad[threadIdx.x] = 0;
+  __syncthreads();
+  for (int task = threadIdx.x; task < R * I.N; task += blockDim.x) {
+    const int q = task / I.N, j = task - q * I.N;
+    const PairState& P = I.ps[q];
+    if (P.info || P.beta0 == 0.0) continue;
+    const int m = P.yk_len;
+    const double* al = pa(I, q, PA_ALPHA, nl);
+    const double* be = pa(I, q, PA_BETA, nl);
+    const zc xi = zmk(I.xi[2 * j], I.xi[2 * j + 1]);
+    zc* U = reinterpret_cast<zc*>(I.cram) + ((size_t)q * I.N + j) * 5 * stride;  // 4 m rows of U
+    zc* z = U + 4 * stride;                                                       // m
+    auto diag = [&](int k) { return zadd(xi, zmk(I.qsign * al[k + 1], 0.0)); };
+    auto off = [&](int k) { return zmk(k + 1 < m ? I.qsign * be[k + 2] : 0.0, 0.0); };
+    zc a0 = diag(0), a1 = off(0), a2 = zmk(0.0, 0.0), bk = zmk(P.beta0, 0.0);
+    zc q0 = zmk(0.0, 0.0), q1 = q0, q2 = q0, qb = q0;
+    if (m > 1) { q0 = off(0); q1 = diag(1); q2 = off(1); }
+    int fail = 0;
+    for (int k = 0; k < m - 1; ++k) {
+      zc n0 = zmk(0.0, 0.0), n1 = n0, n2 = n0;
+      if (k + 2 < m) { n0 = off(k + 1); n1 = diag(k + 2); n2 = off(k + 2); }
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      const double nq = cuCreal(q0) * cuCreal(q0) + cuCimag(q0) * cuCimag(q0);
+      if (na < nq) {
+        zc tt;
+        tt = a0; a0 = q0; q0 = tt;
+        tt = a1; a1 = q1; q1 = tt;
+        tt = a2; a2 = q2; q2 = tt;
+        tt = bk; bk = qb; qb = tt;
+      }
+      const double np = (na < nq) ? nq : na;
+      if (np == 0.0) { fail = 1; break; }
+      const double inv = 1.0 / np;
+      const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
+                       (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
+      U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      a0 = zsub(q1, zmul(l, a1));
+      a1 = zsub(q2, zmul(l, a2));
+      a2 = zmk(0.0, 0.0);
+      bk = zsub(qb, zmul(l, bk));
+      q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
+    }
+    if (!fail && cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) fail = 1;
+    if (fail) { atomicOr(&bad[q], 1); continue; }
+    U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
+    zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);
+    for (int k = m - 1; k >= 0; --k) {
+      const zc v0 = U[4 * k], v1 = U[4 * k + 1], v2 = U[4 * k + 2], vb = U[4 * k + 3];
+      const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+      zc sv = zsub(vb, zmul(v1, x1));
+      sv = zsub(sv, zmul(v2, x2));
+      const zc xk = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
+                        (cuCimag(sv) * cuCreal(v0) - cuCreal(sv) * cuCimag(v0)) * inv);
+      z[k] = xk;
+      x2 = x1;
+      x1 = xk;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < R && bad[threadIdx.x]) I.ps[threadIdx.x].info = PSFUN_ERR_FROM_SUBROUTINE_NON;
+  __syncthreads();
+  // g_k = Im(sum_j c_j z_j[k]) into the pair's PA_YK; then the coefficients
+  for (int task = threadIdx.x; task < R * (nl + 1); task += blockDim.x) {
+    const int q = task / (nl + 1), k = task - q * (nl + 1);
+    const PairState& P = I.ps[q];
+    if (P.info || P.beta0 == 0.0 || k >= P.yk_len) continue;
+    double acc = 0.0;
+    for (int j = 0; j < I.N; ++j) {
+      const zc* z = reinterpret_cast<const zc*>(I.cram) + ((size_t)q * I.N + j) * 5 * stride + 4 * stride;
+      acc += cuCimag(zmul(zmk(I.cw[2 * j], I.cw[2 * j + 1]), z[k]));
+    }
+    pa(I, q, PA_YK, nl)[k] = acc;
+  }
+  __syncthreads();
+  for (int task = threadIdx.x; task < R * (nl + 2); task += blockDim.x) {
+    const int q = task / (nl + 2), r = task - q * (nl + 2);
+    const PairState& P = I.ps[q];
+    const int m = P.yk_len;
+    if (P.info || P.beta0 == 0.0 || r > m) continue;
+    const double* al = pa(I, q, PA_ALPHA, nl);
+    const double* be = pa(I, q, PA_BETA, nl);
+    const double* g = pa(I, q, PA_YK, nl);
+    double h = 0.0;
+    if (r < m) h = al[r + 1] * g[r];
+    if (r >= 1) h = fma(be[r + 1], g[r - 1], h);
+    if (r + 1 < m) h = fma(be[r + 2], g[r + 1], h);
+    pa(I, q, PA_COEF, nl)[r] = I.eta * h * pa(I, q, PA_S, nl)[r + 1];
+  }
+  __syncthreads();
+  if (threadIdx.x < R) {
+    PairState& P = I.ps[threadIdx.x];
+    P.nterms = (P.info || P.beta0 == 0.0) ? 0 : P.yk_len + 1;
+    P.itx = P.yk_len;
+  }
+  __syncthreads();
+}
+
 // Finalisation by the last CTA of an instance (deterministic tile order).
 template <int R>
 PSF_DEVINL void finalize(const BInst& I, int ph, int i, const BatchArgs& B, double* red) {
@@ -391,6 +589,10 @@ PSF_DEVINL void finalize(const BInst& I, int ph, int i, const BatchArgs& B, doub
   // and the estimate with T(1:i), beta_{i+1}
   __shared__ int est_q[kBatchMaxRhs];
   __shared__ int nest;
+  if (I.N > 0) {
+    finalize_quad<R>(I, i, B, tot);
+    return;
+  }
   if (threadIdx.x == 0) {
     nest = 0;
     for (int q = 0; q < R; ++q) {
@@ -453,6 +655,10 @@ PSF_DEVINL void finalize(const BInst& I, int ph, int i, const BatchArgs& B, doub
 // Final f and assembly coefficients of every pair (block per instance).
 template <int R>
 PSF_DEVINL void final_pairs(const BInst& I, const BatchArgs& B, double* red) {
+  if (I.N > 0) {
+    final_quad<R>(I, B);
+    return;
+  }
   const int nl = B.nl;
   __shared__ int mq[kBatchMaxRhs];
   __shared__ int need;
@@ -843,6 +1049,146 @@ static int batch_launch(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, c
 
 }  // namespace psf
 
+namespace psf {
+
+// One batch item, from either entry point: f(tA)X (N = 0) or the quadrature
+// sum over N shifts.
+struct BatchDesc {
+  psfun_csr* a;
+  const double* x;
+  double* y;
+  double scaling;
+  int N;
+  const double* xi;  // host, 2N
+  const double* c;   // host, 2N
+  double eta, sign;
+};
+
+static int batch_run(DevBuf* wsbuf, int keeplast, int count, const std::vector<BatchDesc>& items, int R, double eps,
+                     int itmax, int istop, int* iters, double* errs, int* infos) {
+  const int nl = itmax;
+  cudaStream_t s = stream();
+  // workspace: one allocation, carved per instance
+  std::vector<BInst> hinst(count);
+  size_t off = 0;
+  int tiles = 0;
+  auto carve = [&](size_t doubles) {
+    const size_t o = off;
+    off += (doubles + 31) & ~(size_t)31;
+    return o;
+  };
+  std::vector<size_t> oV(count), oU(count), oS(count), oP(count), oC(count), oPS(count), oCnt(count), oQ2(count);
+  for (int k = 0; k < count; ++k) {
+    psfun_csr* a = items[k].a;
+    BInst& I = hinst[k];
+    memset(&I, 0, sizeof I);
+    I.A = a->dev();
+    I.n = (int)a->n;
+    I.R = R;
+    I.tile_begin = tiles;
+    I.ntiles = a->ntiles;
+    I.t = items[k].scaling;
+    I.ldv = ((int64_t)a->n * R + 31) & ~(int64_t)31;
+    I.X = items[k].x;
+    I.Y = items[k].y;
+    tiles += a->ntiles;
+    oV[k] = carve((size_t)(nl + 1) * I.ldv);
+    oU[k] = carve((size_t)I.ldv);
+    oS[k] = carve((size_t)R * PA_N * (nl + 2));
+    oP[k] = carve((size_t)2 * a->ntiles * R);
+    oC[k] = carve((size_t)R * std::max(7, items[k].N) * 5 * (nl + 2) * 2);
+    oQ2[k] = carve(items[k].N > 0 ? (size_t)4 * items[k].N + (size_t)R * 4 * items[k].N : 0);
+    oPS[k] = carve((sizeof(PairState) * R + 7) / 8);
+    oCnt[k] = carve(2);
+  }
+  const size_t oInst = carve((sizeof(BInst) * count + 7) / 8);
+  const size_t oQ = carve(2 * (size_t)nl + 8);
+  const size_t oMisc = carve(8);
+  const size_t oTI = carve(((size_t)tiles + 1) / 2);
+  DevBuf& ws = *wsbuf;  // the method handle's scratch, reused for the batch
+  PSF_TRY(ws.ensure(sizeof(double) * off));
+  double* base = ws.as<double>();
+  // zero pair state, counters, queues; V needs no clearing
+  for (int k = 0; k < count; ++k) {
+    PSF_CUDA(cudaMemsetAsync(base + oS[k], 0, sizeof(double) * (oP[k] - oS[k]), s));
+    PSF_CUDA(cudaMemsetAsync(base + oPS[k], 0, sizeof(double) * (oInst > oPS[k] ? (oCnt[k] + 2 - oPS[k]) : 0), s));
+  }
+  PSF_CUDA(cudaMemsetAsync(base + oQ, 0, sizeof(double) * (oMisc + 8 - oQ), s));
+  for (int k = 0; k < count; ++k) {
+    BInst& I = hinst[k];
+    I.V = base + oV[k];
+    I.u = base + oU[k];
+    I.scal = base + oS[k];
+    I.part = base + oP[k];
+    I.cram = base + oC[k];
+    I.ps = reinterpret_cast<PairState*>(base + oPS[k]);
+    I.cnt = reinterpret_cast<unsigned*>(base + oCnt[k]);
+    I.N = items[k].N;
+    if (I.N > 0) {  // shifts and weights, then the pairs' recurrence state
+      double* q = base + oQ2[k];
+      PSF_CUDA(cudaMemcpyAsync(q, items[k].xi, sizeof(double) * 2 * I.N, cudaMemcpyHostToDevice, s));
+      PSF_CUDA(cudaMemcpyAsync(q + 2 * I.N, items[k].c, sizeof(double) * 2 * I.N, cudaMemcpyHostToDevice, s));
+      I.xi = q;
+      I.cw = q + 2 * I.N;
+      I.eta = items[k].eta;
+      I.qsign = items[k].sign;
+      I.msd = q + 4 * I.N;
+    }
+  }
+  BInst* dinst = reinterpret_cast<BInst*>(base + oInst);
+  PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * count, cudaMemcpyHostToDevice, s));
+  unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
+  std::vector<int> tile_inst((size_t)std::max(tiles, 1));
+  for (int k = 0; k < count; ++k)
+    for (int t = 0; t < hinst[k].ntiles; ++t) tile_inst[(size_t)hinst[k].tile_begin + t] = k;
+  int* dti = reinterpret_cast<int*>(base + oTI);
+  PSF_CUDA(cudaMemcpyAsync(dti, tile_inst.data(), sizeof(int) * (size_t)tiles, cudaMemcpyHostToDevice, s));
+  BatchArgs B;
+  B.inst = dinst;
+  B.count = count;
+  B.total_tiles = tiles;
+  B.nl = nl;
+  B.istop = istop;
+  B.keeplast = keeplast;
+  B.eps = eps;
+  B.queue = reinterpret_cast<unsigned*>(base + oQ);
+  B.bar = misc;
+  B.err = reinterpret_cast<int*>(misc + 2);
+  B.active = misc + 3;
+  B.tile_inst = dti;
+  const unsigned active = (unsigned)count;
+  PSF_CUDA(cudaMemcpyAsync(B.active, &active, sizeof active, cudaMemcpyHostToDevice, s));
+  int rc;
+  switch (R) {
+    case 1: rc = batch_launch<1>(B, hinst, dinst, s, 1); break;
+    case 2: rc = batch_launch<2>(B, hinst, dinst, s, 1); break;
+    case 3: rc = batch_launch<3>(B, hinst, dinst, s, 1); break;
+    default: rc = batch_launch<4>(B, hinst, dinst, s, 1); break;
+  }
+  if (rc != PSFUN_SUCCESS) return rc;
+  int herr = 0;
+  PSF_CUDA(cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  std::vector<PairState> hps((size_t)count * R);
+  for (int k = 0; k < count; ++k)
+    PSF_CUDA(cudaMemcpyAsync(&hps[(size_t)k * R], hinst[k].ps, sizeof(PairState) * R, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (herr & DEVERR_TIMEOUT) {
+    set_last_error("device-side wait timed out");
+    return PSFUN_ERR_DEVICE_TIMEOUT;
+  }
+  int worst = PSFUN_SUCCESS;
+  for (size_t p = 0; p < hps.size(); ++p) {
+    const PairState& P = hps[p];
+    if (iters) iters[p] = P.itx;
+    if (errs) errs[p] = (P.errden > 0.0) ? P.errnum / P.errden : P.errnum;
+    if (infos) infos[p] = P.info;
+    if (P.info && worst == PSFUN_SUCCESS) worst = P.info;
+  }
+  return worst;
+}
+
+}  // namespace psf
+
 using namespace psf;
 
 extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, int count,
@@ -882,111 +1228,31 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
       return PSFUN_ERR_INVALID_ARGS_COMBINATION;
     }
   }
-  const int nl = itmax;
-  cudaStream_t s = stream();
-  // workspace: one allocation, carved per instance
-  std::vector<BInst> hinst(count);
-  size_t off = 0;
-  int tiles = 0;
-  auto carve = [&](size_t doubles) {
-    const size_t o = off;
-    off += (doubles + 31) & ~(size_t)31;
-    return o;
-  };
-  std::vector<size_t> oV(count), oU(count), oS(count), oP(count), oC(count), oPS(count), oCnt(count);
-  for (int k = 0; k < count; ++k) {
-    psfun_csr* a = items[k].a;
-    BInst& I = hinst[k];
-    memset(&I, 0, sizeof I);
-    I.A = a->dev();
-    I.n = (int)a->n;
-    I.R = R;
-    I.tile_begin = tiles;
-    I.ntiles = a->ntiles;
-    I.t = items[k].scaling;
-    I.ldv = ((int64_t)a->n * R + 31) & ~(int64_t)31;
-    I.X = items[k].x;
-    I.Y = items[k].y;
-    tiles += a->ntiles;
-    oV[k] = carve((size_t)(nl + 1) * I.ldv);
-    oU[k] = carve((size_t)I.ldv);
-    oS[k] = carve((size_t)R * PA_N * (nl + 2));
-    oP[k] = carve((size_t)2 * a->ntiles * R);
-    oC[k] = carve((size_t)R * 7 * 5 * (nl + 2) * 2);
-    oPS[k] = carve((sizeof(PairState) * R + 7) / 8);
-    oCnt[k] = carve(2);
-  }
-  const size_t oInst = carve((sizeof(BInst) * count + 7) / 8);
-  const size_t oQ = carve(2 * (size_t)nl + 8);
-  const size_t oMisc = carve(8);
-  const size_t oTI = carve(((size_t)tiles + 1) / 2);
-  DevBuf& ws = meth->scratch;  // reuse the handle's scratch for the batch
-  PSF_TRY(ws.ensure(sizeof(double) * off));
-  double* base = ws.as<double>();
-  // zero pair state, counters, queues; V needs no clearing
-  for (int k = 0; k < count; ++k) {
-    PSF_CUDA(cudaMemsetAsync(base + oS[k], 0, sizeof(double) * (oP[k] - oS[k]), s));
-    PSF_CUDA(cudaMemsetAsync(base + oPS[k], 0, sizeof(double) * (oInst > oPS[k] ? (oCnt[k] + 2 - oPS[k]) : 0), s));
-  }
-  PSF_CUDA(cudaMemsetAsync(base + oQ, 0, sizeof(double) * (oMisc + 8 - oQ), s));
-  for (int k = 0; k < count; ++k) {
-    BInst& I = hinst[k];
-    I.V = base + oV[k];
-    I.u = base + oU[k];
-    I.scal = base + oS[k];
-    I.part = base + oP[k];
-    I.cram = base + oC[k];
-    I.ps = reinterpret_cast<PairState*>(base + oPS[k]);
-    I.cnt = reinterpret_cast<unsigned*>(base + oCnt[k]);
-  }
-  BInst* dinst = reinterpret_cast<BInst*>(base + oInst);
-  PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * count, cudaMemcpyHostToDevice, s));
-  unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
-  std::vector<int> tile_inst((size_t)std::max(tiles, 1));
+  std::vector<psf::BatchDesc> desc(count);
   for (int k = 0; k < count; ++k)
-    for (int t = 0; t < hinst[k].ntiles; ++t) tile_inst[(size_t)hinst[k].tile_begin + t] = k;
-  int* dti = reinterpret_cast<int*>(base + oTI);
-  PSF_CUDA(cudaMemcpyAsync(dti, tile_inst.data(), sizeof(int) * (size_t)tiles, cudaMemcpyHostToDevice, s));
-  BatchArgs B;
-  B.inst = dinst;
-  B.count = count;
-  B.total_tiles = tiles;
-  B.nl = nl;
-  B.istop = istop;
-  B.keeplast = meth->keeplast;
-  B.eps = eps;
-  B.queue = reinterpret_cast<unsigned*>(base + oQ);
-  B.bar = misc;
-  B.err = reinterpret_cast<int*>(misc + 2);
-  B.active = misc + 3;
-  B.tile_inst = dti;
-  const unsigned active = (unsigned)count;
-  PSF_CUDA(cudaMemcpyAsync(B.active, &active, sizeof active, cudaMemcpyHostToDevice, s));
-  int rc;
-  switch (R) {
-    case 1: rc = batch_launch<1>(B, hinst, dinst, s, 1); break;
-    case 2: rc = batch_launch<2>(B, hinst, dinst, s, 1); break;
-    case 3: rc = batch_launch<3>(B, hinst, dinst, s, 1); break;
-    default: rc = batch_launch<4>(B, hinst, dinst, s, 1); break;
+    desc[k] = psf::BatchDesc{items[k].a, items[k].x, items[k].y, items[k].scaling, 0, nullptr, nullptr, 0.0, 0.0};
+  return psf::batch_run(&meth->scratch, meth->keeplast, count, desc, R, eps, itmax, istop, iters, errs, infos);
+}
+
+extern "C" int psfun_gpu_z_quadrature_batch(int count, const psfun_quad_item* items, double eps, int itmax,
+                                            int* iters, double* errs, int* infos) {
+  psf::NvtxRange nvtx_range("psfun_gpu_z_quadrature_batch");
+  if (count < 1 || !items || itmax < 2) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  const int R = items[0].nrhs;
+  if (R < 1 || R > kBatchMaxRhs) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+  std::vector<psf::BatchDesc> desc(count);
+  for (int k = 0; k < count; ++k) {
+    const psfun_quad_item& q = items[k];
+    if (!q.a || q.nrhs != R || q.N < 1 || q.N > 1024 || !q.xi || !q.c) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    if (!q.x || !q.y) return PSFUN_ERR_INVALID_VECT_STATE;
+    int sym = 0;  // the shared Lanczos basis needs A = A^T
+    PSF_TRY(csr_symmetric(q.a, &sym));
+    if (!sym) {
+      set_last_error("quadrature batch item " + std::to_string(k) + ": the multi-shift Lanczos needs a symmetric matrix");
+      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    }
+    desc[k] = psf::BatchDesc{q.a, q.x, q.y, 1.0, q.N, q.xi, q.c, q.eta, q.sign};
   }
-  if (rc != PSFUN_SUCCESS) return rc;
-  int herr = 0;
-  PSF_CUDA(cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  std::vector<PairState> hps((size_t)count * R);
-  for (int k = 0; k < count; ++k)
-    PSF_CUDA(cudaMemcpyAsync(&hps[(size_t)k * R], hinst[k].ps, sizeof(PairState) * R, cudaMemcpyDeviceToHost, s));
-  PSF_CUDA(cudaStreamSynchronize(s));
-  if (herr & DEVERR_TIMEOUT) {
-    set_last_error("device-side wait timed out");
-    return PSFUN_ERR_DEVICE_TIMEOUT;
-  }
-  int worst = PSFUN_SUCCESS;
-  for (size_t p = 0; p < hps.size(); ++p) {
-    const PairState& P = hps[p];
-    if (iters) iters[p] = P.itx;
-    if (errs) errs[p] = (P.errden > 0.0) ? P.errnum / P.errden : P.errnum;
-    if (infos) infos[p] = P.info;
-    if (P.info && worst == PSFUN_SUCCESS) worst = P.info;
-  }
-  return worst;
+  static psf::DevBuf ws;  // workspace of the quadrature batches
+  return psf::batch_run(&ws, 0, count, desc, R, eps, itmax, 1, iters, errs, infos);
 }

@@ -2111,6 +2111,180 @@ __global__ void k_dot_final(const double* part, int nb, double* out) {
   if (threadIdx.x == 0) *out = v;
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of y = exp(tA) x for a nonsymmetric A.  Two Arnoldi runs (the
+// forward one on A and x, the adjoint one on A^T and g; EXP/GENPADE, istop 1,
+// all of the converged estimate's coefficients kept) give
+//   y      = beta_x V_x exp(t H_x) e1,       grad_x = exp(tA^T) g = beta_g V_g exp(t H_g) e1,
+// and, from dL/dA = t int_0^1 exp((1-s) tA^T) g (exp(s tA) x)^T ds with both
+// exponentials replaced by their Krylov approximations,
+//   dL/dA  ~ V_g R V_x^T,   R = t beta_g beta_x [exp(B)]_12,
+//   B = [[t H_g, e1 e1^T], [0, t H_x^T]]       (Van Loan's block formula),
+// a dense exponential of order m_g + m_x on the device, then the tall product
+// P = W_g R'' and the SDDMM on the pattern of A as in the symmetric path.
+// ---------------------------------------------------------------------------
+
+// E = exp(B) for the block matrix B above (in scratch after the Pade work).
+__global__ void __launch_bounds__(kDenseThreads) k_adj_vanloan(const double* Hg, int ldg, int mg, const double* Hx,
+                                                               int ldx, int mx, double* scratch, int* status,
+                                                               DenseGroup* grp) {
+  PSF_DENSE_KERNEL_ENTRY(grp, status);
+  const int M = mg + mx;
+  const size_t MM = (size_t)M * M;
+  double* E = scratch + 4 * MM;
+  double* B = scratch + 5 * MM;
+  for (size_t e = threadIdx.x; e < MM; e += blockDim.x) {
+    const int j = (int)(e / M), i = (int)(e - (size_t)j * M);
+    double v = 0.0;
+    if (i < mg && j < mg) v = Hg[i + (size_t)j * ldg];
+    else if (i >= mg && j >= mg) v = Hx[(j - mg) + (size_t)(i - mg) * ldx];
+    else if (i == 0 && j == mg) v = 1.0;
+    B[e] = v;
+  }
+  __syncthreads();
+  const int rc = cta_dgpadm(6, M, 1.0, B, M, E, scratch, sm);
+  if (threadIdx.x == 0) *status = rc;
+  dense_group_end(sm, status);
+}
+
+// R''[p][q] = t beta_g beta_x E[p, mg + q] s_g[p+1] s_x[q+1] (the scales of
+// the stored, unnormalised basis slots)
+__global__ void k_adj_vanloan_R(const double* E, int M, int mg, int mx, double t, const KCtrl* cg, const KCtrl* cx,
+                                const double* sg, const double* sx, double* R) {
+  const double f = t * cg->beta0 * cx->beta0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < mg * mx; e += gridDim.x * blockDim.x) {
+    const int p = e / mx, q = e - p * mx;
+    R[e] = f * E[p + (size_t)(mg + q) * M] * sg[p + 1] * sx[q + 1];
+  }
+}
+
+static int expm_adjoint_arnoldi(psfun_csr* a, double t, const double* x, const double* g, double eps, int itmax,
+                                int recompute, double* y, double* grad_x, double* grad_t, double* grad_vals,
+                                int* iters) {
+  static psfun_krylov* arx = nullptr;
+  static psfun_krylov* arg = nullptr;
+  static psfun_serial* fexp = nullptr;
+  if (!arx) {
+    arx = new psfun_krylov();
+    arg = new psfun_krylov();
+    fexp = new psfun_serial();
+    for (psfun_krylov* k : {arx, arg}) {
+      set_fstr(k->kname, "ARNOLDI");
+      set_fstr(k->kmethd, "CG");
+      k->keeplast = 1;  // all coefficients of the converged estimate
+    }
+    set_fstr(fexp->fname, "EXP");
+    set_fstr(fexp->variant, "GENPADE");
+  }
+  fexp->scaling = t;  // the Krylov spaces of tA and tA^T
+  psfun_krylov* wg = recompute ? arx : arg;
+  cudaStream_t s = stream();
+  const int64_t n = a->n;
+  const int64_t ld = (n + 31) & ~(int64_t)31;
+  static DevBuf tmpv, adj, pbuf;
+  PSF_TRY(tmpv.ensure(sizeof(double) * ld * 2));
+  double* ytmp = y ? y : tmpv.as<double>();
+  double* Ay = tmpv.as<double>() + ld;
+  const int ldh = itmax + 1;
+  // saved forward quantities: H_x (its ldh columns), the scales, the control word
+  const size_t o_s = ((size_t)ldh * ldh + 31) & ~(size_t)31, o_c = o_s + (((size_t)ldh + 2 + 31) & ~(size_t)31);
+  PSF_TRY(adj.ensure(sizeof(double) * (o_c + 64) + sizeof(KCtrl) * 2 + 4096));
+  double* Hx_save = adj.as<double>();
+  double* sx_save = Hx_save + o_s;
+  KCtrl* cx_save = reinterpret_cast<KCtrl*>(Hx_save + o_c);
+  double* gt = reinterpret_cast<double*>(cx_save + 2);
+  auto small_of = [&](psfun_krylov* k) { return k->small.as<double>(); };
+  auto run = [&](psfun_krylov* k, psfun_csr* m, const double* v, double* out, KCtrl* hc) -> int {
+    int it = 0;
+    double er = 0.0;
+    PSF_TRY(krylov_apply_device(k, fexp, m, out, v, eps, itmax, 0, 1, &it, &er, nullptr, 0, nullptr));
+    PSF_CUDA(cudaMemcpy(hc, k->ctrl.ptr, sizeof(KCtrl), cudaMemcpyDeviceToHost));
+    return PSFUN_SUCCESS;
+  };
+  KCtrl hx, hg;
+  PSF_TRY(run(arx, a, x, ytmp, &hx));
+  const int mx = hx.nterms;
+  if (!grad_x && !grad_t && !grad_vals) {
+    if (iters) { iters[0] = mx; iters[1] = 0; }
+    return PSFUN_SUCCESS;
+  }
+  PSF_CUDA(cudaMemcpyAsync(Hx_save, small_of(arx), sizeof(double) * (size_t)ldh * ldh, cudaMemcpyDeviceToDevice, s));
+  PSF_CUDA(cudaMemcpyAsync(sx_save, small_of(arx) + (size_t)ldh * ldh, sizeof(double) * (ldh + 2),
+                           cudaMemcpyDeviceToDevice, s));
+  PSF_CUDA(cudaMemcpyAsync(cx_save, arx->ctrl.ptr, sizeof(KCtrl), cudaMemcpyDeviceToDevice, s));
+  if (grad_t) {  // dL/dt = g^T A y, before a recomputation reuses y's workspace
+    PSF_TRY(spmv_device(a, 1.0, ytmp, 0.0, Ay));
+    const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+    const int nb = std::min(gv, 4000);
+    static DevBuf part;
+    PSF_TRY(part.ensure(sizeof(double) * 4096));
+    k_dot_partial<<<nb, kVecThreads, 0, s>>>(g, Ay, n, part.as<double>());
+    k_dot_final<<<1, 256, 0, s>>>(part.as<double>(), nb, gt);
+    count_launch(2);
+    PSF_CUDA(cudaMemcpyAsync(grad_t, gt, sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  psfun_csr* aT = nullptr;
+  PSF_TRY(csr_transpose(a, &aT));
+  double* gx_out = grad_x ? grad_x : tmpv.as<double>();  // exp(tA^T) g
+  PSF_TRY(run(wg, aT, g, gx_out, &hg));
+  const int mg = hg.nterms;
+  if (grad_vals) {
+    if (mx < 1 || mg < 1) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+    const int M = mg + mx;
+    static DevBuf scr, stat, grp;
+    PSF_TRY(scr.ensure(sizeof(double) * (fh_scratch_doubles(M, 1) + 64)));
+    PSF_TRY(stat.ensure(sizeof(int) * 4));
+    PSF_TRY(grp.ensure(sizeof(DenseGroup) + 64));
+    PSF_TRY(pbuf.ensure(sizeof(double) * ((size_t)mx * ld + (size_t)mg * mx + 64)));
+    double* P = pbuf.as<double>();
+    double* R = P + (size_t)mx * ld;
+    PSF_CUDA(cudaMemsetAsync(stat.ptr, 0xff, sizeof(int), s));
+    {
+      const double* hgp = small_of(wg);
+      const double* hxp = Hx_save;
+      int ldg_ = ldh, mg_ = mg, ldx_ = ldh, mx_ = mx;
+      double* sp = scr.as<double>();
+      int* st_ = stat.as<int>();
+      DenseGroup* gg = nullptr;
+      void* args[] = {(void*)&hgp, (void*)&ldg_, (void*)&mg_, (void*)&hxp, (void*)&ldx_, (void*)&mx_,
+                      (void*)&sp, (void*)&st_, (void*)&gg};
+      PSF_TRY(launch_dense((const void*)k_adj_vanloan, dense_group_blocks(M), grp.as<DenseGroup>(), &gg, args, s));
+    }
+    const double* E = scr.as<double>() + 4 * (size_t)M * M;
+    k_adj_vanloan_R<<<std::max(1, std::min(1024, (mg * mx + 255) / 256)), 256, 0, s>>>(
+        E, M, mg, mx, t, wg->ctrl.as<KCtrl>(), cx_save, small_of(wg) + (size_t)ldh * ldh, sx_save, R);
+    const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+    k_adj_P<<<gv, kVecThreads, sizeof(double) * mg * kAdjChunk, s>>>(wg->V.as<double>(), wg->ldv, mg, R, mx, n, P,
+                                                                       ld);
+    count_launch(2);
+    const double* Wx = arx->V.as<double>();
+    int64_t ldx = arx->ldv;
+    if (recompute) {  // rebuild the forward basis over the adjoint one
+      KCtrl hx2;
+      PSF_TRY(run(arx, a, x, tmpv.as<double>(), &hx2));
+      if (hx2.nterms != mx) {
+        set_last_error("recomputed forward basis differs");
+        return PSFUN_ERR_INTERNAL;
+      }
+      Wx = arx->V.as<double>();
+      ldx = arx->ldv;
+    }
+    k_adj_sddmm<<<gv, kVecThreads, 0, s>>>(a->dev(), P, ld, Wx, ldx, mx, grad_vals);
+    count_launch();
+    int hs = -1;
+    PSF_CUDA(cudaMemcpyAsync(&hs, stat.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PSF_CUDA(cudaStreamSynchronize(s));
+    if (hs != 0) {
+      set_last_error("expm adjoint: the dense block exponential failed");
+      return PSFUN_ERR_FROM_SUBROUTINE_NON;
+    }
+  }
+  PSF_CUDA(cudaGetLastError());
+  PSF_CUDA(cudaStreamSynchronize(s));
+  if (iters) { iters[0] = mx; iters[1] = mg; }
+  return PSFUN_SUCCESS;
+}
+
 int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g, int nquad, double eps, int itmax,
                         int recompute, double* y, double* grad_x, double* grad_t, double* grad_vals, int* iters) {
   if (!a || !x || !g) return PSFUN_ERR_INVALID_VECT_STATE;
@@ -2119,10 +2293,7 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
   {
     int sym = 0;
     PSF_TRY(csr_symmetric(a, &sym));
-    if (!sym) {
-      set_last_error("expm adjoint: the Lanczos bases need a symmetric matrix");
-      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
-    }
+    if (!sym) return expm_adjoint_arnoldi(a, t, x, g, eps, itmax, recompute, y, grad_x, grad_t, grad_vals, iters);
   }
   const int Nq = nquad / 2;
   std::vector<double> zc_h(2 * Nq), cw_h(2 * Nq), xi_h(2 * Nq);

@@ -26,6 +26,19 @@ module psfun_gb300_cabi
     real(c_double) :: scaling
   end type
 
+  ! psfun_quad_item of the header
+  type, bind(C) :: psfun_quad_item
+    type(c_ptr)    :: a
+    integer(c_int) :: nrhs
+    type(c_ptr)    :: x
+    type(c_ptr)    :: y
+    integer(c_int) :: N
+    type(c_ptr)    :: xi
+    type(c_ptr)    :: c
+    real(c_double) :: eta
+    real(c_double) :: sign
+  end type
+
   ! status codes (PSBLAS info values, plus the three without a PSBLAS counterpart)
   integer(c_int), parameter :: PSFUN_SUCCESS = 0
   integer(c_int), parameter :: PSFUN_ERR_INVALID_ARGS_COMBINATION = 111
@@ -369,6 +382,17 @@ module psfun_gb300_cabi
       type(psfun_batch_item), intent(in) :: items(*)
       real(c_double), value :: eps
       integer(c_int), value :: itmax, istop
+      integer(c_int), intent(out) :: iters(*)
+      real(c_double), intent(out) :: errs(*)
+      integer(c_int), intent(out) :: infos(*)
+    end function
+    integer(c_int) function psfun_gpu_z_quadrature_batch(count, items, eps, itmax, iters, errs, infos) &
+         bind(C, name="psfun_gpu_z_quadrature_batch")
+      import :: c_int, c_double, psfun_quad_item
+      integer(c_int), value :: count
+      type(psfun_quad_item), intent(in) :: items(*)
+      real(c_double), value :: eps
+      integer(c_int), value :: itmax
       integer(c_int), intent(out) :: iters(*)
       real(c_double), intent(out) :: errs(*)
       integer(c_int), intent(out) :: infos(*)

@@ -3,8 +3,9 @@ on the CPU.  No Fortran compiler is available, so the ISO_C_BINDING interface
 module is checked by reading it: every entry point of include/psfun_gb300.h has
 a bind(C) interface with the same name, the same number of arguments and
 argument-by-argument compatible types (value scalars, arrays, handles,
-strings, function pointers), the bind(C) psfun_batch_item matches the header's
-struct field by field, and the shim calls only bound entry points."""
+strings, function pointers), the bind(C) psfun_batch_item and psfun_quad_item
+match the header's structs field by field, and the shim calls only bound
+entry points."""
 import re
 from pathlib import Path
 
@@ -54,6 +55,7 @@ FTYPE = {
     "integer(c_int)": "int", "integer(c_int64_t)": "int64_t", "integer(c_int32_t)": "int32_t",
     "integer(c_long_long)": "long long", "real(c_double)": "double", "complex(c_double_complex)": "double",
     "character(kind=c_char)": "char", "type(psfun_batch_item)": "psfun_batch_item",
+    "type(psfun_quad_item)": "psfun_quad_item",
 }
 
 
@@ -122,14 +124,21 @@ def test_every_entry_point_is_bound_with_matching_arguments():
         assert fret == want, (name, cret, fret)
 
 
-def test_batch_item_layout():
-    hdr = re.search(r"typedef struct \{(.*?)\} psfun_batch_item;", HEADER.read_text(), flags=re.S).group(1)
+def struct_fields(name):
+    hdr = re.search(r"typedef struct \{([^{}]*)\} " + name + ";", HEADER.read_text()).group(1)
     hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
     cfields = [f.split()[-1].lstrip("*") for f in hdr.split(";") if f.strip()]
-    src = CABI.read_text()
-    body = re.search(r"type, bind\(C\) :: psfun_batch_item(.*?)end type", src, flags=re.S).group(1)
+    body = re.search(r"type, bind\(C\) :: " + name + r"\n(.*?)end type", CABI.read_text(), flags=re.S).group(1)
     ffields = [line.split("::")[1].strip() for line in body.splitlines() if "::" in line]
+    return cfields, ffields
+
+
+def test_batch_item_layout():
+    cfields, ffields = struct_fields("psfun_batch_item")
     assert cfields == ffields == ["a", "nrhs", "x", "y", "scaling"]
+    cfields, ffields = struct_fields("psfun_quad_item")
+    assert [f.lower() for f in cfields] == [f.lower() for f in ffields] == ["a", "nrhs", "x", "y", "n", "xi", "c",
+                                                                           "eta", "sign"]
 
 
 def test_shim_calls_only_bound_entry_points():

@@ -99,6 +99,52 @@ def test_adjoint_recompute_equals_stored(lib):
     assert torch.equal(r1["grad_x"], r2["grad_x"])
 
 
+def dense_frechet_grad(Ad, t, x, g):
+    """dL/dA for L = g^T exp(tA) x: t [expm([[tA^T, g x^T], [0, tA^T]])]_12."""
+    n = Ad.shape[0]
+    B = np.zeros((2 * n, 2 * n))
+    B[:n, :n] = t * Ad.T
+    B[n:, n:] = t * Ad.T
+    B[:n, n:] = np.outer(g, x)
+    return t * sl.expm(B)[:n, n:]
+
+
+@pytest.mark.parametrize("N,t", [(24, -1e-3), (32, -2e-3)])
+def test_adjoint_nonsymmetric_vs_dense_frechet(lib, N, t):
+    """Nonsymmetric A (2-D upwind convection-diffusion): y and grad_x =
+    exp(tA^T) g from Arnoldi on A and A^T, grad_t, and dL/dA on the pattern
+    through the Van Loan block exponential, against the dense block-expm
+    Frechet derivative."""
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    A = matrices.convdiff_2d(N)
+    rng = np.random.default_rng(N)
+    x, g = rng.standard_normal(N * N), rng.standard_normal(N * N)
+    a = pg.CsrMatrix.from_scipy(A)
+    assert not a.is_symmetric()
+    xd, gd = torch.tensor(x, device="cuda"), torch.tensor(g, device="cuda")
+    r = pg.expm_adjoint(a, t, xd, gd, eps=1e-15, itmax=200)
+    torch.cuda.synchronize()
+    Ad = A.toarray()
+    E = sl.expm(t * Ad)
+    y = r["y"].cpu().numpy()
+    assert np.linalg.norm(y - E @ x) / np.linalg.norm(E @ x) < 1e-12
+    gx = r["grad_x"].cpu().numpy()
+    assert np.linalg.norm(gx - E.T @ g) / np.linalg.norm(E.T @ g) < 1e-12
+    gt_ref = g @ (Ad @ (E @ x))
+    assert abs(r["grad_t"] - gt_ref) <= 1e-11 * abs(gt_ref)
+    G = dense_frechet_grad(Ad, t, x, g)
+    Ac = A.tocsr()
+    rows = np.repeat(np.arange(N * N), np.diff(Ac.indptr))
+    ref = G[rows, Ac.indices]
+    got = r["grad_vals"].cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-10 * np.max(np.abs(ref))
+    # recomputing the forward basis gives the same gradients
+    r2 = pg.expm_adjoint(a, t, xd, gd, eps=1e-15, itmax=200, recompute=True)
+    torch.cuda.synchronize()
+    assert torch.equal(r["grad_vals"], r2["grad_vals"]) and torch.equal(r["grad_x"], r2["grad_x"])
+
+
 class ExpmAction:
     """Test-harness torch.autograd.Function: y = exp(t A(theta)) x."""
 
@@ -132,11 +178,13 @@ class ExpmAction:
 def test_autograd_full_size_vs_finite_differences(lib):
     """512 x 512 grid, L = 1/2 ||exp(-0.1 A(theta)) x - y*||^2.
 
-    Central differences with h = 1e-6 carry their own FP64 rounding floor of
-    about eps * L / h (L ~ 4.5e3 here, i.e. ~5e-6 on each derivative), so a
-    coordinate is accepted when |fd - grad| <= 1e-6 |grad| + 20 eps L / h.
-    Directional differences along random dense directions have a signal far
-    above that floor and are held to 1e-6 relative."""
+    Every check uses central differences at steps d and 2d combined by
+    Richardson extrapolation (the d^2 term cancels), so the step can be large
+    enough (d = 1e-3) that the FD's own FP64 rounding floor, about
+    eps * L / d (L ~ 4.5e3 here, i.e. ~1e-9), sits far below the gradients:
+    64 random coordinates of theta and 16 of x are held to
+    |fd - grad| <= 1e-6 |grad| + 20 eps L / d, and directional derivatives
+    along random dense directions to 1e-6 relative."""
     torch = pytest.importorskip("torch")
     import psfun_gb300 as pg
     cfg = matrices.grid_graph_adjoint()
@@ -169,21 +217,22 @@ def test_autograd_full_size_vs_finite_differences(lib):
     th0 = cfg["theta"].copy()
     gth = theta.grad.cpu().numpy()
     rng = np.random.default_rng(11)
-    rel = []
-    for e in rng.choice(len(ei), size=64, replace=False):
-        tp, tm = th0.copy(), th0.copy()
-        tp[e] += h
-        tm[e] -= h
-        fd = fd_of(y_of(tp, x, t0), y_of(tm, x, t0))
-        assert abs(fd - gth[e]) <= 1e-6 * abs(gth[e]) + floor, (e, fd, gth[e])
-        rel.append(abs(fd - gth[e]) / abs(gth[e]))
-    # directional derivatives: a larger step along a unit-variance direction
-    # lifts the signal far above the rounding floor; Richardson extrapolation
-    # of central differences at d and 2d cancels the d^2 term
+
+    # Richardson extrapolation of central differences at d and 2d
     def dirfd(yfun, d):
         f1 = fd_of(*yfun(d)) * (h / d)
         f2 = fd_of(*yfun(2 * d)) * (h / (2 * d))
         return (4 * f1 - f2) / 3
+
+    d = 1e-3
+    floor = 20 * 2.220446049250313e-16 * Lval / d
+    rel = []
+    for e in rng.choice(len(ei), size=64, replace=False):
+        unit = np.zeros(len(ei))
+        unit[e] = 1.0
+        fd = dirfd(lambda dd: (y_of(th0 + dd * unit, x, t0), y_of(th0 - dd * unit, x, t0)), d)
+        assert abs(fd - gth[e]) <= 1e-6 * abs(gth[e]) + floor, (e, fd, gth[e])
+        rel.append(abs(fd - gth[e]) / abs(gth[e]))
 
     for k in range(3):
         v = rng.standard_normal(len(ei))
@@ -192,10 +241,9 @@ def test_autograd_full_size_vs_finite_differences(lib):
         assert abs(fd - ad) <= 1e-6 * abs(ad), (k, fd, ad)
     gx = xv.grad.cpu().numpy()
     for j in rng.choice(n, size=16, replace=False):
-        xp, xm = x.clone(), x.clone()
-        xp[j] += h
-        xm[j] -= h
-        fd = fd_of(y_of(th0, xp, t0), y_of(th0, xm, t0))
+        ej_ = torch.zeros_like(x)
+        ej_[j] = 1.0
+        fd = dirfd(lambda dd: (y_of(th0, x + dd * ej_, t0), y_of(th0, x - dd * ej_, t0)), d)
         assert abs(fd - gx[j]) <= 1e-6 * abs(gx[j]) + floor, (j, fd, gx[j])
     v = torch.tensor(rng.standard_normal(n), device=dev)
     fd = dirfd(lambda d: (y_of(th0, x + d * v, t0), y_of(th0, x - d * v, t0)), 1e-3)

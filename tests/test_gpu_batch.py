@@ -101,3 +101,48 @@ def test_batch_zero_rhs_and_errors(lib):
     fun.set("VARIANT", "CHBSYM")
     meth.set("KNAME", "ARNOLDI")
     assert pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)[0] == 111
+
+
+def test_quadrature_batch_matches_single(lib):
+    """Quadrature items (each its own HHT poles and weights, f(z) = z^{-1/2}) in
+    one batched launch against the single-instance quadrature sum, pair by
+    pair: the same number of Lanczos steps and the same result (1e-10)."""
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    rng = np.random.default_rng(5)
+    mats = [(matrices.laplacian_2d(s), s) for s in (12, 30, 47)]
+    mats += [(matrices.rgg_knn_laplacian(n, 8, rng, shift=0.5), None) for n in (500, 3000)]
+    items = []
+    for k, (A, side) in enumerate(mats):
+        if side is not None:
+            lam = lambda j: 4.0 * np.sin(np.pi * j / (2.0 * (side + 1))) ** 2
+            bounds = [2 * lam(1), 2 * lam(side)]
+        else:
+            bounds = [0.5, float(abs(A).sum(axis=1).max())]
+        q = pg.PsfunZQuadrature()
+        assert q.computepoles(pg.hhtmethod1, lambda z: 1.0 / np.sqrt(z), 12 + 4 * k, rparams=bounds) == 0
+        a = pg.CsrMatrix.from_scipy(A)
+        q.setmatrix(a)
+        X = torch.tensor(rng.standard_normal((2, A.shape[0])), device="cuda")
+        items.append((a, X, torch.zeros_like(X), q))
+    info, infos, iters, errs = pg.quadrature_batch(items, eps=1e-10, itmax=2000)
+    torch.cuda.synchronize()
+    assert info == 0 and not infos.any()
+    for k, (a, X, Y, q) in enumerate(items):
+        for r in range(2):
+            y1, inf1, it1, err1 = q.apply(X[r].cpu().numpy(), eps=1e-10, itmax=2000)
+            assert inf1 == 0
+            assert iters[k, r] == it1, (k, r, iters[k, r], it1)
+            yb = Y[r].cpu().numpy()
+            assert np.linalg.norm(yb - y1) <= 1e-10 * np.linalg.norm(y1), (k, r)
+            assert errs[k, r] < 1e-10
+
+
+def test_quadrature_batch_refuses_nonsymmetric(lib):
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    q = pg.PsfunZQuadrature()
+    assert q.computepoles(pg.hhtmethod1, lambda z: 1.0 / np.sqrt(z), 8, rparams=[1.0, 10.0]) == 0
+    a = pg.CsrMatrix.from_scipy(matrices.convdiff_2d(8))
+    X = torch.ones((1, 64), dtype=torch.float64, device="cuda")
+    assert pg.quadrature_batch([(a, X, torch.zeros_like(X), q)])[0] == 111
