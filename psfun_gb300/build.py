@@ -21,7 +21,7 @@ LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libpsfun_gb300.so"
 INCLUDE = PKG.parent / "include"
 
-SOURCES = ["capi.cu", "krylov.cu", "cg.cu", "batch.cu", "quadrule.cpp"]
+SOURCES = ["capi.cu", "krylov.cu", "cg.cu", "batch.cu", "batch_arnoldi.cu", "quadrule.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1203,11 +1203,26 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
     while (n > 0 && kn[n - 1] == ' ') --n;
     kn[n] = 0;
   }
-  if (strcmp(kn, "LANCZOS") != 0) {
-    set_last_error("the batched path implements LANCZOS");
+  if (strcmp(kn, "LANCZOS") != 0 && strcmp(kn, "ARNOLDI") != 0) {
+    set_last_error("the batched path implements LANCZOS and ARNOLDI");
     return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   }
   if (istop < 1 || istop > 2) return PSFUN_ERR_INVALID_ISTOP;
+  if (strcmp(kn, "ARNOLDI") == 0) {  // any matrix, any device-side f (batch_arnoldi.cu)
+    FunParams fpa;
+    if (!parse_fun(fun, &fpa) || fpa.fname == FN_USERF) {
+      set_last_error("the batched Arnoldi evaluates the device-side functions (not USERF)");
+      return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    }
+    if (itmax < 2) return PSFUN_ERR_FROM_SUBROUTINE_NON;
+    const int Ra = items[0].nrhs;
+    if (Ra < 1 || Ra > kBatchMaxRhs) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+    for (int k = 0; k < count; ++k) {
+      if (!items[k].a || items[k].nrhs != Ra) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
+      if (!items[k].x || !items[k].y) return PSFUN_ERR_INVALID_VECT_STATE;
+    }
+    return batch_arnoldi(meth, fpa, count, items, eps, itmax, istop, iters, errs, infos);
+  }
   FunParams fp;
   if (!parse_fun(fun, &fp) || fp.fname != FN_EXP || (fp.variant != VAR_CHBSYM && fp.variant != VAR_CHBGEN)) {
     set_last_error("the batched path evaluates EXP with the CHBSYM/CHBGEN rational");

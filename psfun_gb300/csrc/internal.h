@@ -179,6 +179,9 @@ int cg_device(psfun_csr* a, int prec, const double* b, double eta, double zeta, 
 int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* c, double eta, double sign,
                       const double* x, double* y, double eps, int itmax, int* iter, double* err);
 int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y);
+// psfun_gpu_d_krylov_batch with KNAME 'ARNOLDI' (batch_arnoldi.cu)
+int batch_arnoldi(psfun_krylov* meth, const FunParams& fp, int count, const psfun_batch_item* items, double eps,
+                  int itmax, int istop, int* iters, double* errs, int* infos);
 // Whether A equals A^T entry by entry (same stored pattern, equal values),
 // checked once per handle on the host and cached: *sym = 1 or 0.
 int csr_symmetric(psfun_csr* a, int* sym);

@@ -99,7 +99,7 @@ def test_batch_zero_rhs_and_errors(lib):
     fun.set("VARIANT", "GENPADE")
     assert pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)[0] == 111
     fun.set("VARIANT", "CHBSYM")
-    meth.set("KNAME", "ARNOLDI")
+    meth.set("KNAME", "SAIARNOLDI")
     assert pg.krylov_batch(meth, fun, [(a, X, Y, 0.5)], 1e-10, itmax=30)[0] == 111
 
 
@@ -146,3 +146,72 @@ def test_quadrature_batch_refuses_nonsymmetric(lib):
     a = pg.CsrMatrix.from_scipy(matrices.convdiff_2d(8))
     X = torch.ones((1, 64), dtype=torch.float64, device="cuda")
     assert pg.quadrature_batch([(a, X, torch.zeros_like(X), q)])[0] == 111
+
+
+def arnoldi_items(R, seed=11):
+    rng = np.random.default_rng(seed)
+    mats = [matrices.convdiff_2d(N) for N in (12, 20, 33)]
+    mats += [matrices.laplacian_2d(15), matrices.rgg_knn_laplacian(500, 8, rng)]
+    out = []
+    for A in mats:
+        X = rng.standard_normal((R, A.shape[0]))
+        t = -float(rng.uniform(1.0, 8.0)) / float(abs(A).sum(axis=1).max())
+        out.append((A, X, t))
+    return out
+
+
+@pytest.mark.parametrize("istop", [1, 2])
+@pytest.mark.parametrize("fname,variant", [("EXP", "GENPADE"), ("PHI", "")])
+def test_batch_arnoldi_matches_plain(lib, orc, istop, fname, variant):
+    """KNAME 'ARNOLDI' in the batched launch (nonsymmetric and symmetric
+    instances, two right-hand sides each) against the plain Arnoldi drop-in
+    on t A for every pair and against the oracle: the same iteration count
+    and the same result (1e-10)."""
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    eps, itmax, R = 1e-10, 40, 2
+    items = arnoldi_items(R)
+    handles = []
+    for A, X, t in items:
+        Xd = torch.tensor(X, device="cuda")
+        handles.append((pg.CsrMatrix.from_scipy(A), Xd, torch.zeros_like(Xd), t))
+    fun = pg.PsfunDSerial()
+    assert fun.set("FNAME", fname) == 0 and fun.set("VARIANT", variant) == 0
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "ARNOLDI")
+    info, infos, iters, errs = pg.krylov_batch(meth, fun, handles, eps, itmax=itmax, istop=istop)
+    torch.cuda.synchronize()
+    assert info == 0 and not infos.any(), (info, infos, lib.psfun_gpu_last_error())
+    for k, ((A, X, t), (a, Xd, Yd, _)) in enumerate(zip(items, handles)):
+        Y = Yd.cpu().numpy()
+        fk = pg.PsfunDSerial()
+        fk.set("FNAME", fname); fk.set("VARIANT", variant); fk.set("SCALING", t)
+        for q in range(R):
+            r = pg.PsfunDKrylov()
+            r.set("KNAME", "ARNOLDI")
+            p = r.apply(fk, a, X[q], eps, itmax=itmax, istop=istop)
+            o = orc.krylov("ARNOLDI", orc.serial(fname, variant, t), orc.Csr.from_scipy(A), X[q], eps, itmax=itmax,
+                           istop=istop)
+            assert p.info == 0 and o["info"] == 0
+            assert iters[k, q] == p.iter == o["iter"], (k, q, iters[k, q], p.iter, o["iter"])
+            assert np.linalg.norm(Y[q] - p.y) <= 1e-10 * np.linalg.norm(p.y), (k, q)
+            assert np.linalg.norm(Y[q] - o["y"]) <= 1e-10 * np.linalg.norm(o["y"]), (k, q)
+
+
+def test_batch_arnoldi_zero_rhs_and_userf(lib):
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    a = pg.CsrMatrix.from_scipy(matrices.convdiff_2d(10))
+    X = torch.zeros((2, 100), dtype=torch.float64, device="cuda")
+    X[1] = 1.0
+    Y = torch.full_like(X, 7.0)
+    fun = pg.PsfunDSerial()
+    fun.set("VARIANT", "GENPADE")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "ARNOLDI")
+    info, infos, iters, errs = pg.krylov_batch(meth, fun, [(a, X, Y, -1e-3)], 1e-10, itmax=30)
+    torch.cuda.synchronize()
+    assert info == 0 and iters[0, 0] == 0 and not Y[0].any() and torch.isfinite(Y[1]).all()
+    fu = pg.PsfunDSerial()
+    fu.set("FNAME", "USERF"); fu.set("VARIANT", "SYM"); fu.set("FPOINTER", lambda v, k: float(np.exp(v)))
+    assert pg.krylov_batch(meth, fu, [(a, X, Y, -1e-3)], 1e-10, itmax=30)[0] == 111
