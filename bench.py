@@ -330,10 +330,118 @@ def bench_cg(torch, pg, peak_gbs: float, reps: int = 3):
     assert info == 0, info
     b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
     nbytes = it * (b_spmv + 88 * n)
+
+    def solve_bjac():
+        x0.zero_()
+        return pg.psb_krylov("CG", a, "BJAC", b, 1.0, 0.5, x0, 1e-10, itmax=5000, istop=2)
+
+    dtb, (xb, infob, itb, errb) = _time_dev(torch, solve_bjac, reps)
+    assert infob == 0, infob
     return {"workload": "3-D 7-point Laplacian 128^3 (n=2,097,152), (A + 0.5 I) x = b, CG with DIAG, eps 1e-10",
             "ms_per_solve": 1e3 * dt, "iterations": int(it), "relative_residual": float(err),
             "us_per_iteration": 1e6 * dt / max(it, 1), "algorithmic_bytes_per_solve": nbytes,
-            "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs}
+            "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs,
+            "bjac": {"ms_per_solve": 1e3 * dtb, "iterations": int(itb), "relative_residual": float(errb),
+                     "us_per_iteration": 1e6 * dtb / max(itb, 1),
+                     "note": "BJAC: block Jacobi with ILU(0) on the diagonal blocks of 32 rows"}}
+
+
+def bench_batched_arnoldi(torch, pg, reps: int = 2):
+    """32 uneven nonsymmetric instances (2-D upwind convection-diffusion,
+    side ~ U{32..256}, beta = (b, b/2) with b ~ U[5, 100]), 2 right-hand sides
+    each, y = exp(t A) x with t = -c / ||A||_inf, c ~ U[1, 8], Arnoldi
+    EXP/GENPADE, eps 1e-8, istop 1, m <= 60 (seed 12): the batched launch
+    against the plain Arnoldi drop-in per pair."""
+    from psfun_gb300 import matrices
+    rng = np.random.default_rng(12)
+    items, probs = [], []
+    for _ in range(32):
+        N = int(rng.integers(32, 257))
+        bb = float(rng.uniform(5.0, 100.0))
+        A = matrices.convdiff_2d(N, beta=(bb, bb / 2))
+        t = -float(rng.uniform(1.0, 8.0)) / float(abs(A).sum(axis=1).max())
+        X = torch.tensor(rng.standard_normal((2, A.shape[0])), device="cuda")
+        items.append((pg.CsrMatrix.from_scipy(A), X, torch.zeros_like(X), t))
+        probs.append(A)
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", "GENPADE")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "ARNOLDI")
+    dt_b, (info, infos, iters, errs) = _time_dev(
+        torch, lambda: pg.krylov_batch(meth, fun, items, 1e-8, itmax=60, istop=1), reps)
+    assert info == 0, info
+    pm = pg.PsfunDKrylov()
+    pm.set("KNAME", "ARNOLDI")
+    funs = []
+    for (a, X, Y, t) in items:
+        f = pg.PsfunDSerial()
+        f.set("FNAME", "EXP")
+        f.set("VARIANT", "GENPADE")
+        f.set("SCALING", t)
+        funs.append(f)
+    outs = []
+
+    def plain():
+        outs.clear()
+        for (a, X, Y, t), f in zip(items, funs):
+            for q in range(X.shape[0]):
+                outs.append(pm.apply(f, a, X[q], 1e-8, itmax=60, istop=1))
+
+    dt_p, _ = _time_dev(torch, plain, 1)
+    worst, j = 0.0, 0
+    for (a, X, Y, t) in items:
+        for q in range(X.shape[0]):
+            worst = max(worst, float(torch.linalg.norm(Y[q] - outs[j].y) / torch.linalg.norm(outs[j].y)))
+            j += 1
+    npairs = 2 * len(items)
+    return {"workload": "32 uneven 2-D convection-diffusion instances (side U{32..256}), 2 RHS each, exp(tA)X, "
+                        "Arnoldi EXP/GENPADE, eps 1e-8, istop 1, m<=60",
+            "batched_ms": 1e3 * dt_b, "plain_ms": 1e3 * dt_p, "speedup_vs_plain": dt_p / dt_b,
+            "batched_solves_per_s": npairs / dt_b, "max_rel_diff_batched_vs_plain": worst,
+            "mean_iters": float(np.mean(iters)), "max_iters": int(np.max(iters))}
+
+
+def bench_quad_batch(torch, pg, reps: int = 2):
+    """64 uneven SPD instances x 4 right-hand sides (2-D Laplacians of side
+    U{32..128} and shifted kNN graph Laplacians of 1k-16k nodes) with
+    A^{-1/2} X by the HHT rule, N = 16 shifts per instance on each instance's
+    spectral bounds, eps 1e-8: the batched launch
+    (psfun_gpu_z_quadrature_batch) against the single-instance quadrature sum
+    per right-hand side."""
+    from psfun_gb300 import matrices
+    probs = matrices.uneven_spd_batch()
+    items = []
+    for p in probs:
+        q = pg.PsfunZQuadrature()
+        q.computepoles(pg.hhtmethod1, lambda z: 1.0 / np.sqrt(z), 16, rparams=p.params["bounds"])
+        a = pg.CsrMatrix.from_scipy(p.A)
+        q.setmatrix(a)
+        X = torch.tensor(p.x, device="cuda")
+        items.append((a, X, torch.zeros_like(X), q))
+    dt_b, (info, infos, iters, errs) = _time_dev(torch, lambda: pg.quadrature_batch(items, 1e-8, 1500), reps)
+    assert info == 0, info
+    outs = []
+
+    def plain():
+        outs.clear()
+        for (a, X, Y, q) in items:
+            for r in range(X.shape[0]):
+                outs.append(q.apply(X[r], eps=1e-8, itmax=1500))
+
+    dt_p, _ = _time_dev(torch, plain, 1)
+    worst, j = 0.0, 0
+    for (a, X, Y, q) in items:
+        for r in range(X.shape[0]):
+            y1 = outs[j][0]
+            worst = max(worst, float(torch.linalg.norm(Y[r] - y1) / torch.linalg.norm(y1)))
+            j += 1
+    npairs = sum(int(X.shape[0]) for _, X, _, _ in items)
+    return {"workload": "64 uneven SPD instances (2-D Laplacians side U{32..128}, kNN graph Laplacians + 0.05 I, "
+                        "n 1k-16k) x 4 RHS, A^{-1/2}X by HHT with 16 shifts per instance, eps 1e-8, itmax 1500",
+            "batched_ms": 1e3 * dt_b, "plain_ms": 1e3 * dt_p, "speedup_vs_plain": dt_p / dt_b,
+            "batched_solves_per_s": npairs / dt_b, "max_rel_diff_batched_vs_plain": worst,
+            "mean_iters": float(np.mean(iters)), "max_iters": int(np.max(iters))}
 
 
 def bench_laplace2d(torch, pg, reps: int = 20):
@@ -506,6 +614,8 @@ def run_only(name: str) -> int:
           "adjoint": lambda: bench_adjoint(torch, pg),
           "cg": lambda: bench_cg(torch, pg, peak),
           "batched": lambda: bench_batched(torch, pg),
+          "batched_arnoldi": lambda: bench_batched_arnoldi(torch, pg),
+          "quad_batch": lambda: bench_quad_batch(torch, pg),
           "serial": lambda: bench_serial(torch, pg),
           "sai": lambda: bench_sai(torch, pg),
           "laplace2d": lambda: bench_laplace2d(torch, pg)}[name]
@@ -523,7 +633,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batched (64-instance) comparison")
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
-    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "serial", "sai", "laplace2d"],
+    ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "batched_arnoldi",
+                                       "quad_batch", "serial", "sai", "laplace2d"],
                     help="run one secondary workload alone and print its result (for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -712,6 +823,9 @@ def main():
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_secondary:
         line["batched"] = bench_batched(torch, pg)
+        torch.cuda.empty_cache()
+        line["batched_arnoldi"] = bench_batched_arnoldi(torch, pg)
+        line["quad_batch"] = bench_quad_batch(torch, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base, ro = cpu_baseline(A, x)
         line["cpu_baseline"] = base

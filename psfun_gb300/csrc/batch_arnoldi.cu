@@ -329,25 +329,35 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
     return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   }
   std::vector<BaUnit> hu(nu);
-  int64_t rows = 0;
-  for (int k = 0; k < count; ++k) rows += items[k].a->n * R;
-  // blocks in proportion to the rows, at least one per unit, at most gmax
-  std::vector<int> nblk(nu);
-  int G = 0;
-  for (int k = 0; k < count; ++k)
-    for (int q = 0; q < R; ++q) {
-      const int64_t n = items[k].a->n;
-      int nbk = (int)std::max<int64_t>(1, (int64_t)((double)(gmax - nu) * (double)n / (double)std::max<int64_t>(rows, 1)));
-      nbk = (int)std::min<int64_t>(nbk, std::max<int64_t>(1, (n + 63) / 64));
-      nblk[k * R + q] = nbk;
-      G += nbk;
-    }
-  while (G > gmax) {  // rounding left too many: take from the largest
-    int big = (int)(std::max_element(nblk.begin(), nblk.end()) - nblk.begin());
-    if (nblk[big] <= 1) break;
-    --nblk[big];
-    --G;
+  int64_t rows = 0, nmax = 0;
+  for (int k = 0; k < count; ++k) {
+    rows += items[k].a->n * R;
+    nmax = std::max<int64_t>(nmax, items[k].a->n);
   }
+  // Blocks of the step kernel per unit: in proportion to the rows, at least
+  // one per unit, at most gmax in all, and no fewer than `rpb` rows per block.
+  // More blocks bring more of the GPU to a sweep; fewer make each sweep's grid
+  // barrier cheaper.  rpb is chosen by timing the first steps once per batch shape.
+  std::vector<int> nblk(nu);
+  auto partition = [&](int rpb) {
+    int G = 0;
+    for (int k = 0; k < count; ++k)
+      for (int q = 0; q < R; ++q) {
+        const int64_t n = items[k].a->n;
+        int nbk = (int)std::max<int64_t>(
+            1, (int64_t)((double)(gmax - nu) * (double)n / (double)std::max<int64_t>(rows, 1)));
+        nbk = (int)std::min<int64_t>(nbk, std::max<int64_t>(1, (n + rpb - 1) / rpb));
+        nblk[k * R + q] = nbk;
+        G += nbk;
+      }
+    while (G > gmax) {  // rounding left too many: take from the largest
+      int big = (int)(std::max_element(nblk.begin(), nblk.end()) - nblk.begin());
+      if (nblk[big] <= 1) break;
+      --nblk[big];
+      --G;
+    }
+    return G;
+  };
   // workspace: one allocation, carved per unit at 256-byte boundaries
   size_t off = 0;
   auto carve = [&](size_t doubles) {
@@ -370,131 +380,173 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
     uo[u].scr = carve(fsz);
   }
   const size_t oUnits = carve((sizeof(BaUnit) * nu + 7) / 8);
-  const size_t oPart = carve(2 * (size_t)G + 8);
-  const size_t oMap = carve(((size_t)G + 1) / 2 + 1);
+  const size_t oPart = carve(2 * (size_t)gmax + 8);
+  const size_t oMap = carve(((size_t)gmax + 1) / 2 + 1);
   const size_t oE1 = carve(nl + 2);
   const size_t oMisc = carve(8);
   DevBuf& ws = meth->scratch;  // the method handle's scratch, reused for the batch
   PSF_TRY(ws.ensure(sizeof(double) * off));
   double* base = ws.as<double>();
-  int b = 0;
-  std::vector<int> blk_unit(G);
-  for (int u = 0; u < nu; ++u) {
-    const int k = u / R, q = u % R;
-    const psfun_csr* a = items[k].a;
-    BaUnit& U = hu[u];
-    memset(&U, 0, sizeof U);
-    U.A = a->dev();
-    U.n = a->n;
-    U.ldv = (a->n + 31) & ~(int64_t)31;
-    U.t = items[k].scaling;
-    U.V = base + uo[u].V;
-    U.H = base + uo[u].H;
-    U.s = base + uo[u].s;
-    U.rs = base + uo[u].rs;
-    U.yk = base + uo[u].yk;
-    U.coef = base + uo[u].coef;
-    U.scr = base + uo[u].scr;
-    U.x = items[k].x + (size_t)q * a->n;
-    U.y = items[k].y + (size_t)q * a->n;
-    U.b0 = b;
-    U.b1 = b + nblk[u];
-    for (int j = U.b0; j < U.b1; ++j) blk_unit[j] = u;
-    b = U.b1;
-    PSF_CUDA(cudaMemsetAsync(U.H, 0, sizeof(double) * (size_t)ldh * ldh, s));
-    PSF_CUDA(cudaMemsetAsync(U.s, 0, sizeof(double) * 4 * ((nl + 2 + 31) & ~31), s));
-  }
-  BaUnit* du = reinterpret_cast<BaUnit*>(base + oUnits);
-  PSF_CUDA(cudaMemcpyAsync(du, hu.data(), sizeof(BaUnit) * nu, cudaMemcpyHostToDevice, s));
-  int* dmap = reinterpret_cast<int*>(base + oMap);
-  PSF_CUDA(cudaMemcpyAsync(dmap, blk_unit.data(), sizeof(int) * G, cudaMemcpyHostToDevice, s));
-  std::vector<double> e1(nl + 2, 0.0);
-  e1[0] = 1.0;
-  PSF_CUDA(cudaMemcpyAsync(base + oE1, e1.data(), sizeof(double) * (nl + 2), cudaMemcpyHostToDevice, s));
-  unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
-  PSF_CUDA(cudaMemsetAsync(misc, 0, sizeof(double) * 8, s));
-  static volatile int* hflag = nullptr;
-  static int* dflag = nullptr;
-  if (!hflag) {
-    int* p = nullptr;
-    PSF_CUDA(cudaHostAlloc((void**)&p, 4 * sizeof(int), cudaHostAllocMapped));
-    hflag = p;
-    PSF_CUDA(cudaHostGetDevicePointer((void**)&dflag, p, 0));
-  }
-  hflag[0] = nu;
-  hflag[1] = 0;
-  BaArgs B;
-  B.u = du;
-  B.count = nu;
-  B.nl = nl;
-  B.ldh = ldh;
-  B.istop = istop;
-  B.keeplast = meth->keeplast;
-  B.eps = eps;
-  B.fp = fp;
-  B.blk_unit = dmap;
-  B.part = base + oPart;
-  B.bar = misc;
-  B.err = reinterpret_cast<int*>(misc + 1);
-  B.step = reinterpret_cast<int*>(misc + 2);
-  B.e1 = base + oE1;
-  B.host_flag = dflag;
-  const int two = 2;
-  PSF_CUDA(cudaMemcpyAsync(B.step, &two, sizeof(int), cudaMemcpyHostToDevice, s));
-  {
-    void* args[] = {(void*)&B};
-    PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ba_init, dim3(G), dim3(kBaThreads), args, 0, s));
-    count_launch();
-  }
-  // one Arnoldi step of every unit, captured once and replayed
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  {
-    PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    void* args[] = {(void*)&B};
-    cudaError_t e = cudaMemsetAsync(B.bar, 0, sizeof(unsigned), s);
-    if (e == cudaSuccess)
-      e = cudaLaunchCooperativeKernel((void*)k_ba_step, dim3(G), dim3(kBaThreads), args, 0, s);
-    if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_estimate, dim3(nu), dim3(kBaThreads), args, 0, s);
-    if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_next, dim3(1), dim3(256), args, 0, s);
-    cudaError_t ec = cudaStreamEndCapture(s, &graph);
-    if (e != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      PSF_CUDA(e);
+  // One solve with the partition of rpb (a tuning run stops after
+  // tune_steps steps and reports the time of its steps in *tune_ms).
+  auto solve = [&](int rpb, int tune_steps, float* tune_ms) -> int {
+    const int G = partition(rpb);
+    int b = 0;
+    std::vector<int> blk_unit(G);
+    for (int u = 0; u < nu; ++u) {
+      const int k = u / R, q = u % R;
+      const psfun_csr* a = items[k].a;
+      BaUnit& U = hu[u];
+      memset(&U, 0, sizeof U);
+      U.A = a->dev();
+      U.n = a->n;
+      U.ldv = (a->n + 31) & ~(int64_t)31;
+      U.t = items[k].scaling;
+      U.V = base + uo[u].V;
+      U.H = base + uo[u].H;
+      U.s = base + uo[u].s;
+      U.rs = base + uo[u].rs;
+      U.yk = base + uo[u].yk;
+      U.coef = base + uo[u].coef;
+      U.scr = base + uo[u].scr;
+      U.x = items[k].x + (size_t)q * a->n;
+      U.y = items[k].y + (size_t)q * a->n;
+      U.b0 = b;
+      U.b1 = b + nblk[u];
+      for (int j = U.b0; j < U.b1; ++j) blk_unit[j] = u;
+      b = U.b1;
+      PSF_CUDA(cudaMemsetAsync(U.H, 0, sizeof(double) * (size_t)ldh * ldh, s));
+      PSF_CUDA(cudaMemsetAsync(U.s, 0, sizeof(double) * 4 * ((nl + 2 + 31) & ~31), s));
     }
-    PSF_CUDA(ec);
-    cudaError_t ei = cudaGraphInstantiate(&gexec, graph, 0);
-    cudaGraphDestroy(graph);
-    PSF_CUDA(ei);
-  }
-  const int max_ahead = 3;
-  int rc = PSFUN_SUCCESS;
-  for (int i = 2; i <= nl; ++i) {
-    if (hflag[0] == 0) break;  // every unit has stopped
-    cudaError_t e = cudaGraphLaunch(gexec, s);
-    if (e != cudaSuccess) {
-      (void)cudaGetLastError();
-      set_last_error(std::string("batched Arnoldi: cudaGraphLaunch: ") + cudaGetErrorString(e));
-      rc = PSFUN_ERR_CUDA;
-      break;
+    BaUnit* du = reinterpret_cast<BaUnit*>(base + oUnits);
+    PSF_CUDA(cudaMemcpyAsync(du, hu.data(), sizeof(BaUnit) * nu, cudaMemcpyHostToDevice, s));
+    int* dmap = reinterpret_cast<int*>(base + oMap);
+    PSF_CUDA(cudaMemcpyAsync(dmap, blk_unit.data(), sizeof(int) * G, cudaMemcpyHostToDevice, s));
+    std::vector<double> e1(nl + 2, 0.0);
+    e1[0] = 1.0;
+    PSF_CUDA(cudaMemcpyAsync(base + oE1, e1.data(), sizeof(double) * (nl + 2), cudaMemcpyHostToDevice, s));
+    unsigned* misc = reinterpret_cast<unsigned*>(base + oMisc);
+    PSF_CUDA(cudaMemsetAsync(misc, 0, sizeof(double) * 8, s));
+    static volatile int* hflag = nullptr;
+    static int* dflag = nullptr;
+    if (!hflag) {
+      int* p = nullptr;
+      PSF_CUDA(cudaHostAlloc((void**)&p, 4 * sizeof(int), cudaHostAllocMapped));
+      hflag = p;
+      PSF_CUDA(cudaHostGetDevicePointer((void**)&dflag, p, 0));
     }
-    count_launch(3);
-    for (long spin = 0; i - hflag[1] > max_ahead && hflag[0] != 0; ++spin) {
-      if (cudaStreamQuery(s) == cudaSuccess) break;
-      if (spin > 200000000L) break;
+    hflag[0] = nu;
+    hflag[1] = 0;
+    BaArgs B;
+    B.u = du;
+    B.count = nu;
+    B.nl = nl;
+    B.ldh = ldh;
+    B.istop = istop;
+    B.keeplast = meth->keeplast;
+    B.eps = eps;
+    B.fp = fp;
+    B.blk_unit = dmap;
+    B.part = base + oPart;
+    B.bar = misc;
+    B.err = reinterpret_cast<int*>(misc + 1);
+    B.step = reinterpret_cast<int*>(misc + 2);
+    B.e1 = base + oE1;
+    B.host_flag = dflag;
+    const int two = 2;
+    PSF_CUDA(cudaMemcpyAsync(B.step, &two, sizeof(int), cudaMemcpyHostToDevice, s));
+    {
+      void* args[] = {(void*)&B};
+      PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ba_init, dim3(G), dim3(kBaThreads), args, 0, s));
+      count_launch();
     }
+    // one Arnoldi step of every unit, captured once and replayed
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    {
+      PSF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      void* args[] = {(void*)&B};
+      cudaError_t e = cudaMemsetAsync(B.bar, 0, sizeof(unsigned), s);
+      if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((void*)k_ba_step, dim3(G), dim3(kBaThreads), args, 0, s);
+      if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_estimate, dim3(nu), dim3(kBaThreads), args, 0, s);
+      if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_next, dim3(1), dim3(256), args, 0, s);
+      cudaError_t ec = cudaStreamEndCapture(s, &graph);
+      if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        PSF_CUDA(e);
+      }
+      PSF_CUDA(ec);
+      cudaError_t ei = cudaGraphInstantiate(&gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      PSF_CUDA(ei);
+    }
+    const int max_ahead = 3;
+    int rc = PSFUN_SUCCESS;
+    static cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (tune_steps > 0) {
+      if (!ev0) {
+        PSF_CUDA(cudaEventCreate(&ev0));
+        PSF_CUDA(cudaEventCreate(&ev1));
+      }
+      PSF_CUDA(cudaEventRecord(ev0, s));
+    }
+    const int i_stop = (tune_steps > 0) ? std::min(nl, 1 + tune_steps) : nl;
+    for (int i = 2; i <= i_stop; ++i) {
+      if (hflag[0] == 0) break;  // every unit has stopped
+      cudaError_t e = cudaGraphLaunch(gexec, s);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_last_error(std::string("batched Arnoldi: cudaGraphLaunch: ") + cudaGetErrorString(e));
+        rc = PSFUN_ERR_CUDA;
+        break;
+      }
+      count_launch(3);
+      for (long spin = 0; i - hflag[1] > max_ahead && hflag[0] != 0; ++spin) {
+        if (cudaStreamQuery(s) == cudaSuccess) break;
+        if (spin > 200000000L) break;
+      }
+    }
+    cudaGraphExecDestroy(gexec);
+    PSF_TRY(rc);
+    if (tune_steps > 0) {
+      PSF_CUDA(cudaEventRecord(ev1, s));
+      PSF_CUDA(cudaEventSynchronize(ev1));
+      PSF_CUDA(cudaEventElapsedTime(tune_ms, ev0, ev1));
+      return PSFUN_SUCCESS;
+    }
+    {
+      void* args[] = {(void*)&B};
+      PSF_CUDA(cudaLaunchKernel((void*)k_ba_final, dim3(nu), dim3(kBaThreads), args, 0, s));
+      PSF_CUDA(cudaLaunchKernel((void*)k_ba_recombine, dim3(G), dim3(kBaThreads), args, 0, s));
+      count_launch(2);
+    }
+    return PSFUN_SUCCESS;
+  };
+
+  // rows per block: timed once per batch shape (count, pairs, size buckets)
+  static std::vector<std::pair<std::vector<int64_t>, int>> tuned;
+  auto bucket = [](int64_t v) { int b = 0; while (v > 1) { v >>= 1; ++b; } return (int64_t)b; };
+  const std::vector<int64_t> key = {count, R, bucket(rows), bucket(nmax), bucket(nl), (int64_t)fp.fname,
+                                    (int64_t)fp.variant};
+  int rpb = 0;
+  for (const auto& t : tuned)
+    if (t.first == key) rpb = t.second;
+  if (!rpb) {
+    const int cand[] = {64, 256, 1024, 4096};
+    float best = 0.0f;
+    for (int c : cand) {
+      float ms = 0.0f;
+      PSF_TRY(solve(c, std::min(8, nl - 1), &ms));
+      if (!rpb || ms < best) { best = ms; rpb = c; }
+    }
+    tuned.emplace_back(key, rpb);
   }
-  cudaGraphExecDestroy(gexec);
-  PSF_TRY(rc);
-  {
-    void* args[] = {(void*)&B};
-    PSF_CUDA(cudaLaunchKernel((void*)k_ba_final, dim3(nu), dim3(kBaThreads), args, 0, s));
-    PSF_CUDA(cudaLaunchKernel((void*)k_ba_recombine, dim3(G), dim3(kBaThreads), args, 0, s));
-    count_launch(2);
-  }
+  PSF_TRY(solve(rpb, 0, nullptr));
   int herr = 0;
-  PSF_CUDA(cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  PSF_CUDA(cudaMemcpyAsync(hu.data(), du, sizeof(BaUnit) * nu, cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaMemcpyAsync(&herr, reinterpret_cast<unsigned*>(base + oMisc) + 1, sizeof(int),
+                           cudaMemcpyDeviceToHost, s));
+  PSF_CUDA(cudaMemcpyAsync(hu.data(), base + oUnits, sizeof(BaUnit) * nu, cudaMemcpyDeviceToHost, s));
   PSF_CUDA(cudaStreamSynchronize(s));
   if (herr & DEVERR_TIMEOUT) {
     set_last_error("device-side wait timed out");

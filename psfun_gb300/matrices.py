@@ -209,6 +209,31 @@ def uneven_batch(count: int = 64, nrhs: int = 4, scale: float = 1.0):
     return out
 
 
+def uneven_spd_batch(count: int = 64, nrhs: int = 4):
+    """64 uneven SPD instances for the quadrature batch: 32 2-D Laplacians
+    (side ~ U{32..128}) and 32 kNN random-geometric-graph Laplacians + 0.05 I
+    (n log-uniform in [1024, 16384]), each with its spectral bounds in
+    params["bounds"] (analytic for the grids, [0.05, max row sum] for the
+    graphs)."""
+    rng = np.random.default_rng(13)
+    out = []
+    for i in range(count):
+        if i < count // 2:
+            side = int(rng.integers(32, 129))
+            A = laplacian_2d(side)
+            lam = lambda j: 4.0 * math.sin(math.pi * j / (2.0 * (side + 1))) ** 2
+            bounds = [2.0 * lam(1), 2.0 * lam(side)]
+            kind = f"lap2d-{side}"
+        else:
+            n = int(round(math.exp(rng.uniform(math.log(1024), math.log(16384)))))
+            A = rgg_knn_laplacian(n, 8, rng, shift=0.05)
+            bounds = [0.05, float(abs(A).sum(axis=1).max())]
+            kind = f"rgg-{n}"
+        X = rng.standard_normal((nrhs, A.shape[0]))
+        out.append(Problem(kind, A, X, dict(bounds=bounds)))
+    return out
+
+
 def grid_graph_adjoint(N: int = 512):
     rng = np.random.default_rng(4)
     ei, ej = grid_edges(N)
