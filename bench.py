@@ -419,7 +419,7 @@ def bench_quad_batch(torch, pg, reps: int = 2):
         q.setmatrix(a)
         X = torch.tensor(p.x, device="cuda")
         items.append((a, X, torch.zeros_like(X), q))
-    dt_b, (info, infos, iters, errs) = _time_dev(torch, lambda: pg.quadrature_batch(items, 1e-8, 1500), reps)
+    dt_b, (info, infos, iters, errs) = _time_dev(torch, lambda: pg.quadrature_batch(items, 1e-8, 600), reps)
     assert info == 0, info
     outs = []
 
@@ -427,7 +427,7 @@ def bench_quad_batch(torch, pg, reps: int = 2):
         outs.clear()
         for (a, X, Y, q) in items:
             for r in range(X.shape[0]):
-                outs.append(q.apply(X[r], eps=1e-8, itmax=1500))
+                outs.append(q.apply(X[r], eps=1e-8, itmax=600))
 
     dt_p, _ = _time_dev(torch, plain, 1)
     worst, j = 0.0, 0
@@ -438,7 +438,7 @@ def bench_quad_batch(torch, pg, reps: int = 2):
             j += 1
     npairs = sum(int(X.shape[0]) for _, X, _, _ in items)
     return {"workload": "64 uneven SPD instances (2-D Laplacians side U{32..128}, kNN graph Laplacians + 0.05 I, "
-                        "n 1k-16k) x 4 RHS, A^{-1/2}X by HHT with 16 shifts per instance, eps 1e-8, itmax 1500",
+                        "n 1k-16k) x 4 RHS, A^{-1/2}X by HHT with 16 shifts per instance, eps 1e-8, itmax 600",
             "batched_ms": 1e3 * dt_b, "plain_ms": 1e3 * dt_p, "speedup_vs_plain": dt_p / dt_b,
             "batched_solves_per_s": npairs / dt_b, "max_rel_diff_batched_vs_plain": worst,
             "mean_iters": float(np.mean(iters)), "max_iters": int(np.max(iters))}
@@ -600,8 +600,9 @@ def run_reference(args):
     return 0
 
 
-def run_only(name: str) -> int:
-    """One secondary workload on cuda:0, its result as one JSON line."""
+def run_only(name: str, scale: float = 1.0) -> int:
+    """One secondary workload on cuda:0, its result as one JSON line (`scale`
+    shrinks the 64-instance batch of "batched" for profiling captures)."""
     import torch
     torch.cuda.set_device(0)
     import psfun_gb300 as pg
@@ -613,7 +614,7 @@ def run_only(name: str) -> int:
           "multishift": lambda: bench_multishift(torch, pg, peak),
           "adjoint": lambda: bench_adjoint(torch, pg),
           "cg": lambda: bench_cg(torch, pg, peak),
-          "batched": lambda: bench_batched(torch, pg),
+          "batched": lambda: bench_batched(torch, pg, scale=scale),
           "batched_arnoldi": lambda: bench_batched_arnoldi(torch, pg),
           "quad_batch": lambda: bench_quad_batch(torch, pg),
           "serial": lambda: bench_serial(torch, pg),
@@ -636,11 +637,13 @@ def main():
     ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "batched_arnoldi",
                                        "quad_batch", "serial", "sai", "laplace2d"],
                     help="run one secondary workload alone and print its result (for profiling captures)")
+    ap.add_argument("--scale", type=float, default=1.0, help="with --only batched: instance sizes x scale "
+                                                             "(smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.only:
-        return run_only(args.only)
+        return run_only(args.only, args.scale)
 
     import torch
     rank, world, local = dist_info()

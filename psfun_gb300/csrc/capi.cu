@@ -308,6 +308,7 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
   a->h_diag.assign(n, 0.0);
   for (int64_t i = 0; i < n; ++i) {
     double s = 0.0;
+    a->max_row = std::max<int32_t>(a->max_row, hirp[i + 1] - hirp[i]);
     for (int32_t k = hirp[i]; k < hirp[i + 1]; ++k) {
       s += fabs(val[k]);
       if (hja[k] == i) a->h_diag[i] += val[k];

@@ -61,9 +61,13 @@ __host__ __device__ inline size_t fh_scratch_doubles(int m, int phiorder) {
 
 // A group of co-resident blocks (one cooperative launch) sharing one dense
 // f(H) evaluation: block 0 runs the evaluation and posts its heavy parts
-// here, a matrix product (kind 0: each block computes a share of the 4-row
-// strips) or the seven pole solves of CRAM on a full H (kind 1: block r
-// solves the poles r, r + G, ...); blocks 1..G-1 only serve those jobs
+// here, a matrix product (kind 0: each block computes a share of the
+// entries), the seven pole solves of CRAM on a full H (kind 1: block r
+// solves the poles r, r + G, ...) or the substitutions of a factored linear
+// system (kind 2: each block a share of the right-hand sides; B = m pivot
+// rows as int, then from B + m the reciprocals of U's diagonal; ldb = the
+// right-hand sides, C and ldc = their matrix); blocks 1..G-1
+// only serve those jobs
 // (dense_helper).  In global memory, zeroed by the host before each launch.
 // All waits are bounded: a wait that gives up sets err, which the kernel
 // reports as DEVERR_TIMEOUT.
@@ -92,43 +96,25 @@ struct DenseSmem {
 
 // ---- real building blocks --------------------------------------------------
 
-// Tasks [t0, t1) of C = alpha * A * B (m x m): task t is the 4-row strip
-// t mod nrb of column t / nrb.  alpha is folded into B(l,j) and the sum over
-// l runs in order, the operation order of the reference BLAS DGEMM, so every
-// entry is the same whichever block computes it.
+// Tasks [t0, t1) of C = alpha * A * B (m x m): task t is the entry
+// (t mod m, t / m), so that a warp reads 32 consecutive rows of A and one
+// entry of B per l.  alpha is folded into B(l,j) and the sum over l runs in
+// order, the operation order of the reference BLAS DGEMM, so every entry is
+// the same whichever block computes it.  One entry per thread: a GB300 SM
+// sub-partition retires one FP64 warp instruction per 64 clocks whatever the
+// active lanes, so the product's time is its number of warp instructions
+// over the sub-partitions that hold them, and single entries spread them
+// over the most warps.
 PSF_DEVINL void gemm_tasks(int m, double alpha, const double* A, int lda, const double* B, int ldb, double* C,
                            int ldc, int t0, int t1) {
-  const int nrb = (m + 3) >> 2;
   for (int task = t0 + (int)threadIdx.x; task < t1; task += blockDim.x) {
-    const int j = task / nrb;
-    const int i0 = (task - j * nrb) << 2;
-    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
-    const double* a = A + i0;
+    const int j = task / m;
+    const int i = task - j * m;
+    const double* a = A + i;
     const double* b = B + (size_t)j * ldb;
-    if (i0 + 3 < m) {
-      for (int l = 0; l < m; ++l) {
-        const double t = alpha * b[l];
-        const double* al = a + (size_t)l * lda;
-        c0 = fma(t, al[0], c0);
-        c1 = fma(t, al[1], c1);
-        c2 = fma(t, al[2], c2);
-        c3 = fma(t, al[3], c3);
-      }
-      double* c = C + i0 + (size_t)j * ldc;
-      c[0] = c0; c[1] = c1; c[2] = c2; c[3] = c3;
-    } else {
-      for (int l = 0; l < m; ++l) {
-        const double t = alpha * b[l];
-        const double* al = a + (size_t)l * lda;
-        c0 = fma(t, al[0], c0);
-        if (i0 + 1 < m) c1 = fma(t, al[1], c1);
-        if (i0 + 2 < m) c2 = fma(t, al[2], c2);
-      }
-      double* c = C + i0 + (size_t)j * ldc;
-      c[0] = c0;
-      if (i0 + 1 < m) c[1] = c1;
-      if (i0 + 2 < m) c[2] = c2;
-    }
+    double c = 0.0;
+    for (int l = 0; l < m; ++l) c = fma(alpha * b[l], a[(size_t)l * lda], c);
+    C[i + (size_t)j * ldc] = c;
   }
 }
 
@@ -179,7 +165,7 @@ PSF_DEVINL void group_wait(DenseSmem& sm) {
 // share and waits for the others').
 PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, int lda, const double* B, int ldb,
                          double* C, int ldc) {
-  const int T = ((m + 3) >> 2) * m;
+  const int T = m * m;
   if (!sm.grp) {
     gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, 0, T);
     __syncthreads();
@@ -190,6 +176,59 @@ PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, in
   gemm_share(T, gridDim.x, 0, &t0, &t1);
   gemm_tasks(m, alpha, A, lda, B, ldb, C, ldc, t0, t1);
   group_wait(sm);
+}
+
+// Columns [c0, c1) of B := U^{-1} L^{-1} P B, with the factors that
+// cta_gesv leaves in A (unit L below the diagonal, U on and above it) and its
+// row exchanges piv[k].  The block's threads run over the entries of its
+// columns, one barrier per elimination step: first the exchanges and the
+// forward elimination in the order of the factorisation, then the
+// column-oriented back substitution of the reference BLAS DTRSM (step k
+// scales b(k) by rdiag(k) = 1 / u(k,k) and subtracts b(k) u(i,k) from the
+// rows above).
+// The scaled b(k) is formed by every thread that needs it and stored one step
+// later, when no thread reads it, so that a step needs one barrier.
+PSF_DEVINL void lu_solve_cols(int m, const double* A, int lda, const int* piv, const double* rdiag, double* B, int ldb,
+                              int c0, int c1) {
+  const int nc = c1 - c0;
+  if (nc <= 0 || m < 1) return;
+  for (int k = 0; k < m; ++k) {
+    const int p = piv[k];
+    if (p != k)
+      for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+        double* b = B + (size_t)j * ldb;
+        const double t = b[k]; b[k] = b[p]; b[p] = t;
+      }
+    __syncthreads();
+    const int rows = m - k - 1;
+    const double* lk = A + (size_t)k * lda;
+    for (int t = threadIdx.x; t < rows * nc; t += blockDim.x) {
+      const int jj = t / rows, i = k + 1 + (t - jj * rows);
+      double* b = B + (size_t)(c0 + jj) * ldb;
+      b[i] = fma(-lk[i], b[k], b[i]);
+    }
+    __syncthreads();
+  }
+  for (int k = m - 1; k >= 0; --k) {
+    const double rk = rdiag[k];
+    const double* uk = A + (size_t)k * lda;
+    const int rows = k + ((k + 1 < m) ? 1 : 0);  // rows 0..k-1, and row k+1's store
+    for (int t = threadIdx.x; t < rows * nc; t += blockDim.x) {
+      const int jj = t / rows, i = t - jj * rows;
+      double* b = B + (size_t)(c0 + jj) * ldb;
+      if (i < k) {
+        b[i] = fma(-uk[i], b[k] * rk, b[i]);
+      } else {  // the previous step's b(k+1), read by no thread of this step
+        b[k + 1] = b[k + 1] * rdiag[k + 1];
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+    double* b = B + (size_t)j * ldb;
+    b[0] = b[0] * rdiag[0];
+  }
+  __syncthreads();
 }
 
 static __device__ bool cram_pole_block(int m, double t, const double* H, int ldh, const double* x, int p, double* scratch);
@@ -221,8 +260,13 @@ PSF_DEVINL void dense_helper(DenseGroup* g) {
     const int m = vg->m;
     if (vg->kind == 0) {
       int t0, t1;
-      gemm_share(((m + 3) >> 2) * m, gridDim.x, blockIdx.x, &t0, &t1);
+      gemm_share(m * m, gridDim.x, blockIdx.x, &t0, &t1);
       gemm_tasks(m, vg->alpha, vg->A, vg->lda, vg->B, vg->ldb, vg->C, vg->ldc, t0, t1);
+    } else if (vg->kind == 2) {
+      int c0, c1;
+      gemm_share(vg->ldb, gridDim.x, blockIdx.x, &c0, &c1);
+      const int* piv = reinterpret_cast<const int*>(vg->B);
+      lu_solve_cols(m, vg->A, vg->lda, piv, vg->B + m, vg->C, vg->ldc, c0, c1);
     } else {
       const double t = vg->alpha;
       const double* H = vg->A;
@@ -413,6 +457,69 @@ PSF_DEVINL bool cta_gesv(int m, int nrhs, double* A, int lda, double* B, int ldb
   return true;
 }
 
+// Solve A X = B like cta_gesv (DGESV semantics), for the Pade step: the
+// factorisation of A alone by block 0, with the multipliers of a column
+// formed by one reciprocal of its pivot as LAPACK DGETF2 does, the pivot
+// rows into ws (int) and the reciprocals of U's diagonal into ws + m
+// (2 m doubles in all); then the substitutions (lu_solve_cols) for all the
+// right-hand sides by this block or, with a group, shared over its blocks.
+// Returns false on an exactly zero pivot.
+PSF_DEVINL bool cta_lu_solve(int m, int nrhs, double* A, int lda, double* B, int ldb, double* ws, DenseSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int* piv = reinterpret_cast<int*>(ws);
+  double* rdiag = ws + m;
+  if (m < 1) { __syncthreads(); return true; }
+  // The reciprocal of each pivot is formed by lane 0 of warp 0 as soon as the
+  // pivot is found, while the other warps finish the step's update: an FP64
+  // division is a chain of about ten dependent FP64 instructions.
+  if (threadIdx.x < 32) {
+    warp_pivot(m, 0, A, lda, sm);
+    if (threadIdx.x == 0) sm.dv[3] = 1.0 / sm.dv[1];
+  }
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    const int p = sm.iv[0];
+    const double piv_v = sm.dv[1], akk = sm.dv[2], rp = sm.dv[3];
+    if (sm.iv[1]) { __syncthreads(); return false; }
+    if (threadIdx.x == 0) piv[k] = p;
+    if (p != k) {
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        if (j == k) continue;
+        double* a = A + (size_t)j * lda;
+        const double t = a[k]; a[k] = a[p]; a[p] = t;
+      }
+      if (threadIdx.x == 0) A[k + (size_t)k * lda] = piv_v;
+    }
+    double* lk = A + (size_t)k * lda;
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) lk[i] = ((i == p) ? akk : lk[i]) * rp;
+    __syncthreads();
+    for (int j = k + 1 + warp; j < m; j += nw) {
+      double* col = A + (size_t)j * lda;
+      const double akj = col[k];
+      for (int i = k + 1 + lane; i < m; i += 32) col[i] = fma(-lk[i], akj, col[i]);
+      if (j == k + 1) {  // warp 0: the pivot of the next step and its reciprocal
+        __syncwarp();
+        warp_pivot(m, k + 1, A, lda, sm);
+        __syncwarp();
+        if (lane == 0) sm.dv[3] = 1.0 / sm.dv[1];
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < m; k += blockDim.x) rdiag[k] = 1.0 / A[k + (size_t)k * lda];
+  __syncthreads();
+  if (!sm.grp || nrhs < 2 * (int)gridDim.x) {
+    lu_solve_cols(m, A, lda, piv, rdiag, B, ldb, 0, nrhs);
+    return true;
+  }
+  group_post(sm, 2, m, 0.0, A, lda, ws, nrhs, B, ldb);
+  int c0, c1;
+  gemm_share(nrhs, gridDim.x, 0, &c0, &c1);
+  lu_solve_cols(m, A, lda, piv, rdiag, B, ldb, c0, c1);
+  group_wait(sm);
+  return true;
+}
+
 // r8mat_fss (r8lib.f90:12806): row-normalising elimination used by SASQ.
 PSF_DEVINL bool cta_fss(int n, double* a, int nb, double* b, DenseSmem& sm) {
   for (int jcol = 0; jcol < n; ++jcol) {
@@ -509,7 +616,8 @@ PSF_DEVINL int cta_dgpadm(int ideg, int m, double t, const double* H, int ldh, d
   }
   for (size_t e = threadIdx.x; e < mm; e += blockDim.x) q[e] -= p[e];
   __syncthreads();
-  if (!cta_gesv(m, m, q, m, p, m, sm)) return DEVERR_SINGULAR;
+  // h2 is free from here: the pivot rows and diagonal reciprocals of the solve
+  if (!(m >= 2 ? cta_lu_solve(m, m, q, m, p, m, h2, sm) : cta_gesv(m, m, q, m, p, m, sm))) return DEVERR_SINGULAR;
   for (size_t e = threadIdx.x; e < mm; e += blockDim.x) p[e] *= 2.0;
   __syncthreads();
   for (int j = threadIdx.x; j < m; j += blockDim.x) p[j + (size_t)j * m] += 1.0;

@@ -103,6 +103,7 @@ struct psfun_csr {
   unsigned* sched = nullptr;   // SpMV tile work counter + blocks-done counter (zero between launches)
   int2* tile_desc = nullptr;   // per tile {first row, first stored entry}, ntiles + 1 entries
   int32_t max_tile_rows = 0;
+  int32_t max_row = 0;         // longest row (stored entries)
   std::vector<double> h_diag;  // diagonal of A (host copy, for DIAG)
   // BJAC preconditioner (lazy): ILU(0) factors of the diagonal blocks of
   // kBjacRows consecutive rows, laid out for a warp that solves 32 blocks at

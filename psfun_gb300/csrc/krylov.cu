@@ -500,7 +500,8 @@ __global__ void __launch_bounds__(kMgsThreads) k_ar_mgs(KState st, int i) {
 constexpr int kMgsSmThreads = 512;
 constexpr size_t kMgsSmFixed = sizeof(double) * (kMgsSmThreads + 32 + 8);
 
-__global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base) {
+__global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base,
+                                                               CsrDev A, double scaling, int fuse) {
   extern __shared__ __align__(16) double mgs_sm[];
   double* vals = mgs_sm;               // kMgsSmThreads
   double* red = vals + kMgsSmThreads;  // 32
@@ -520,13 +521,67 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
   double* __restrict__ w = WAT(st, i) + r0;
   double* part = st.partials;
   unsigned nb = bar_base;
-  {  // load the rows of w; dot with v_1
+  {  // the rows of w (loaded, or with fuse their SpMV formed here); dot with v_1
     const double* __restrict__ wk = WAT(st, 1) + r0;
     double acc = 0.0;
-    for (int l = threadIdx.x; l < nloc; l += bd) {
-      const double v = w[l];
-      wl[l] = v;
-      acc = fma(wk[l], v, acc);
+    if (fuse) {
+      // w = scaling s_{i-1} A W_{i-1} (psfun_d_arnoldi.f90:202), each row's
+      // entries summed in order as k_ar_spmv does; saves that launch and the
+      // write and read of w
+      const double f = scaling * st.s[i - 1];
+      const double* __restrict__ x = WAT(st, i - 1);
+      int l = threadIdx.x;
+      // four rows per thread at a time: their row pointers, entries and
+      // gathers are issued together, so that the loads' latency overlaps
+      for (; l + 3 * bd < nloc; l += 4 * bd) {
+        int kb[4], ke[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          kb[q] = A.irp[r0 + l + q * bd];
+          ke[q] = A.irp[r0 + l + q * bd + 1];
+        }
+        int len = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) len = max(len, ke[q] - kb[q]);
+        double sr[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int t = 0; t < len; t += 4) {
+          double vv[4][4], xv[4][4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int k = kb[q] + t + u;
+              const bool on = k < ke[q];
+              vv[q][u] = on ? A.val[k] : 0.0;
+              xv[q][u] = on ? __ldg(x + A.ja[k]) : 0.0;
+            }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (kb[q] + t + u < ke[q]) sr[q] = fma(vv[q][u], xv[q][u], sr[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double v = f * sr[q];
+          wl[l + q * bd] = v;
+          acc = fma(wk[l + q * bd], v, acc);
+        }
+      }
+      for (; l < nloc; l += bd) {
+        const int64_t r = r0 + l;
+        double sr = 0.0;
+        for (int k = A.irp[r], ke = A.irp[r + 1]; k < ke; ++k) sr = fma(A.val[k], __ldg(x + A.ja[k]), sr);
+        const double v = f * sr;
+        wl[l] = v;
+        acc = fma(wk[l], v, acc);
+      }
+    } else {
+      for (int l = threadIdx.x; l < nloc; l += bd) {
+        const double v = w[l];
+        wl[l] = v;
+        acc = fma(wk[l], v, acc);
+      }
     }
     block_sum_store_512(acc, vals, red, &part[b]);
   }
@@ -1102,12 +1157,16 @@ static int ensure_workspace(psfun_krylov* meth, int64_t n, int nl, int phiorder)
 }
 
 // Blocks of the group that shares the matrix products of a dense f(H) whose
-// products have order m: one block while its 256 threads need one round of
-// 4-row strips, else about 128 strips per block, at most 16.
+// products have order m.  A product of order m is m^2 / 32 warp instructions
+// per step of its inner sum, and an SM sub-partition retires one FP64 warp
+// instruction per 64 clocks: below order 20 one block does it faster than a
+// group can hand it out (a post and a wait cost about 3000 clocks), above it
+// 128 entries per block (one warp per sub-partition) spread the products
+// over up to 128 SMs.
 static int dense_group_blocks(int m) {
-  const long T = (long)((m + 3) / 4) * m;
-  if (T <= (long)kDenseThreads) return 1;
-  return (int)std::min<long>(16, (T + 127) / 128);
+  if (m < 20) return 1;
+  const long T = (long)m * m;
+  return (int)std::max<long>(1, std::min<long>(128, (T + 127) / 128));
 }
 
 // Blocks of the group for a dense f(H) of order m: the product-based
@@ -1314,6 +1373,11 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   const int gm = mgs_grid();
   int mgs_chunk = 0;
   const int gms = arnoldi ? mgs_sm_plan(n, &mgs_chunk) : 0;
+  // The Arnoldi SpMV inside the MGS kernel (rows of the block, one thread per
+  // row) when every row is short: a GB300 SM retires two FP64 FMAs per clock,
+  // so spreading the SpMV's FMAs over the MGS kernel's threads of every SM
+  // costs no more than the tiled kernel, without the write and re-read of w.
+  const bool fuse_spmv = gms > 0 && !sai && a->max_row <= 64;
   const int tridiag = arnoldi ? 0 : 1;
   const size_t small_doubles = meth->small.bytes / sizeof(double);
 
@@ -1346,7 +1410,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
           set_last_error("SAIARNOLDI: inner CG failed");
           return PSFUN_ERR_FROM_SUBROUTINE_NON;
         }
-      } else {
+      } else if (!fuse_spmv) {
         prof_begin(PROF_AR_SPMV, s);
         k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
         prof_end(PROF_AR_SPMV, s);
@@ -1354,7 +1418,10 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       prof_begin(PROF_AR_MGS, s);
       if (gms > 0) {
         unsigned bar_base = (unsigned)((int64_t)(i - 1) * i / 2 - 1);  // barriers of steps 2..i-1
-        void* args[] = {(void*)&st, (void*)&i, (void*)&mgs_chunk, (void*)&bar_base};
+        int fuse = fuse_spmv ? 1 : 0;
+        double sc = scaling;
+        void* args[] = {(void*)&st, (void*)&i, (void*)&mgs_chunk, (void*)&bar_base, (void*)&A, (void*)&sc,
+                        (void*)&fuse};
         const size_t smem = kMgsSmFixed + sizeof(double) * (size_t)mgs_chunk;
         PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs_sm, dim3(gms), dim3(kMgsSmThreads), args, smem, s));
       } else {
@@ -1362,7 +1429,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
         PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_mgs, dim3(gm), dim3(kMgsThreads), args, 0, s));
       }
       prof_end(PROF_AR_MGS, s);
-      count_launch(sai ? 1 : 2);
+      count_launch((sai || fuse_spmv) ? 1 : 2);
     } else {
       prof_begin(PROF_LZ_SPMV, s);
       PSF_TRY(launch_lz_persist(st, A, i, i + 1, s));
