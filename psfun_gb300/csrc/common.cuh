@@ -113,6 +113,29 @@ PSF_DEVINL void block_sum_store_512(double v, double* vals, double* red, double*
   if (threadIdx.x == 0) *out = (red[0] + red[1]) + (red[2] + red[3]);
 }
 
+// Two sums at once (blockDim.x == 512), each in the order of
+// block_sum_store_512: warps 0..3 reduce v1 through vals, warps 4..7 reduce
+// v2 through vals2 (each SM sub-partition holds one warp of each), thread 0
+// stores both.  With out2 null only v1 is reduced.
+PSF_DEVINL void block_sum2_store_512(double v1, double v2, double* vals, double* vals2, double* red, double* out1,
+                                     double* out2) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  vals[threadIdx.x] = v1;
+  if (out2) vals2[threadIdx.x] = v2;
+  __syncthreads();
+  if (wid < (out2 ? 8 : 4)) {
+    const double* p = ((wid < 4) ? vals : vals2) + 128 * (wid & 3) + lane;
+    double t = ((p[0] + p[32]) + p[64]) + p[96];
+    t = warp_sum(t);
+    if (lane == 0) red[wid] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *out1 = (red[0] + red[1]) + (red[2] + red[3]);
+    if (out2) *out2 = (red[4] + red[5]) + (red[6] + red[7]);
+  }
+}
+
 // Thread 0 stores the maximum of the block's values to *out (blockDim.x == 512),
 // the counterpart of block_sum_store_512.
 PSF_DEVINL void block_max_store_512(double v, double* vals, double* red, double* out) {
@@ -168,6 +191,34 @@ PSF_DEVINL double partials_sum_to0(const volatile double* p, int count, double* 
     tot = ((t[0] + t[4]) + (t[2] + t[6])) + ((t[1] + t[5]) + (t[3] + t[7]));
   }
   return tot;
+}
+
+// partials_sum_to0 of p1[0..count) and, with two, of p2[0..count) (count <=
+// 256, blockDim.x >= 512): warps 0..7 take p1's chunks, warps 8..15 p2's.
+// Only thread 0 gets the totals.
+PSF_DEVINL void partials_sum2_to0(const volatile double* p1, const volatile double* p2, int count, bool two,
+                                  double* red, double* t1, double* t2) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nch = (count + 31) >> 5;
+  const int w = wid & 7;
+  if (w < nch && (wid < 8 || two)) {
+    const volatile double* p = (wid < 8) ? p1 : p2;
+    double v = (32 * w + lane < count) ? p[32 * w + lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0) red[wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = (q < nch) ? red[q] : 0.0;
+    *t1 = ((t[0] + t[4]) + (t[2] + t[6])) + ((t[1] + t[5]) + (t[3] + t[7]));
+    if (two) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) t[q] = (q < nch) ? red[8 + q] : 0.0;
+      *t2 = ((t[0] + t[4]) + (t[2] + t[6])) + ((t[1] + t[5]) + (t[3] + t[7]));
+    }
+  }
 }
 
 // Sum of `count` partials in a fixed order by one block (all threads get it).

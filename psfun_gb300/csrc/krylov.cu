@@ -490,23 +490,111 @@ __global__ void __launch_bounds__(kMgsThreads) k_ar_mgs(KState st, int i) {
   }
 }
 
-// The same modified Gram-Schmidt with the block's rows of w held in shared
-// memory for the whole step (used when they fit, n <= ~4.3M rows on 152 SMs):
-// per sweep only W_k and W_{k+1} stream from HBM, and w never leaves the SM
-// until it is written back at the end.  512 threads; the grid barriers count
-// on a counter that grows across the steps of a solve (bar_base = barriers
-// run by the earlier steps), per-block partials are reduced through shared
-// memory and the scalars of a sweep are formed by thread 0.
+// Gram-Schmidt of slot i against slots 1..i-1 with the block's rows of w
+// held in shared memory for the whole step (used when they fit, n <= ~4.3M
+// rows on 152 SMs): w never leaves the SM until it is written back at the
+// end.  512 threads.
+//
+// The basis vectors are taken two at a time: one sweep over the rows
+// subtracts h(k) v_k and h(k+1) v_{k+1}, in that order, and forms the dots of
+// the result with the next two vectors, and one grid barrier ends the sweep.
+// Within a pair h(k+1) = v_{k+1} . w is taken before the v_k update (as in
+// classical Gram-Schmidt); across pairs the order is that of modified
+// Gram-Schmidt (psfun_d_arnoldi.f90:210-214).  The two coefficients differ
+// from the one-at-a-time ones by h(k) (v_{k+1} . v_k), a rounding-level
+// difference for a basis orthogonal to working precision, and the FP64 work
+// per row is the same (two FMAs per basis vector), so halving the sweeps
+// halves the barriers, partial reductions and sweep start-ups, which take a
+// third of the time of a sweep when the FP64 pipe bounds the rest.
+//
+// The grid barriers count on a counter that grows across the steps of a
+// solve (bar_base = barriers run by the earlier steps, mgs_barriers_before),
+// per-block partials are reduced through shared memory and the scalars of a
+// sweep are formed by thread 0.  With fuse the block also forms its rows of
+// w = scaling s_{i-1} A W_{i-1} (the SpMV of psfun_d_arnoldi.f90:202, each
+// row's entries summed in order as k_ar_spmv does), which saves that launch
+// and the write and re-read of w.
 constexpr int kMgsSmThreads = 512;
-constexpr size_t kMgsSmFixed = sizeof(double) * (kMgsSmThreads + 32 + 8);
+constexpr size_t kMgsSmFixed = sizeof(double) * (2 * kMgsSmThreads + 32 + 8);
+
+// Barriers run by the paired sweeps of steps 2..i-1: step j runs one after
+// forming w and one per pair of its j - 1 basis vectors.
+inline unsigned mgs_barriers_before(int i) {
+  int64_t t = 0;
+  for (int j = 2; j < i; ++j) t += 1 + j / 2;
+  return (unsigned)t;
+}
+
+// One paired sweep over the block's rows of w: w -= c1 v_k (and c2 v_{k+1}
+// with TWO), then the dots of the result with the next vectors (NEXT = 1 or
+// 2) or its squared norm (NEXT = 0) into acc1, acc2.  Rows go in groups per
+// thread (four, or two when four vectors stream); the next group's loads are
+// issued before this group's arithmetic.  Rows are accumulated in order, so
+// the sums are reproducible.
+template <bool TWO, int NEXT>
+PSF_DEVINL void mgs_pair_sweep(double* __restrict__ wl, int nloc, int bd, double c1, double c2,
+                               const double* __restrict__ vk, const double* __restrict__ vk1,
+                               const double* __restrict__ vn1, const double* __restrict__ vn2, double& acc1,
+                               double& acc2) {
+  auto row = [&](int r, double a, double a1, double n1, double n2) {
+    double v = fma(-c1, a, wl[r]);
+    if (TWO) v = fma(-c2, a1, v);
+    wl[r] = v;
+    if (NEXT == 0) acc1 = fma(v, v, acc1);
+    if (NEXT >= 1) acc1 = fma(n1, v, acc1);
+    if (NEXT == 2) acc2 = fma(n2, v, acc2);
+  };
+  // rows per group: the group's loads and the next group's stay in registers
+  constexpr int kStreams = 1 + (TWO ? 1 : 0) + NEXT;
+  constexpr int RG = (kStreams <= 2) ? 4 : 2;
+  int l = threadIdx.x;
+  if (l + (RG - 1) * bd < nloc) {
+    double a[RG], a1[RG], n1[RG], n2[RG];
+#pragma unroll
+    for (int q = 0; q < RG; ++q) {
+      a[q] = vk[l + q * bd];
+      a1[q] = TWO ? vk1[l + q * bd] : 0.0;
+      n1[q] = (NEXT >= 1) ? vn1[l + q * bd] : 0.0;
+      n2[q] = (NEXT == 2) ? vn2[l + q * bd] : 0.0;
+    }
+    for (;;) {
+      const int ln = l + RG * bd;
+      const bool more = ln + (RG - 1) * bd < nloc;
+      double b[RG], b1[RG], m1[RG], m2[RG];
+      if (more) {
+#pragma unroll
+        for (int q = 0; q < RG; ++q) {
+          b[q] = vk[ln + q * bd];
+          b1[q] = TWO ? vk1[ln + q * bd] : 0.0;
+          m1[q] = (NEXT >= 1) ? vn1[ln + q * bd] : 0.0;
+          m2[q] = (NEXT == 2) ? vn2[ln + q * bd] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RG; ++q) row(l + q * bd, a[q], a1[q], n1[q], n2[q]);
+      l = ln;
+      if (!more) break;
+#pragma unroll
+      for (int q = 0; q < RG; ++q) {
+        a[q] = b[q];
+        a1[q] = b1[q];
+        n1[q] = m1[q];
+        n2[q] = m2[q];
+      }
+    }
+  }
+  for (; l < nloc; l += bd)
+    row(l, vk[l], TWO ? vk1[l] : 0.0, (NEXT >= 1) ? vn1[l] : 0.0, (NEXT == 2) ? vn2[l] : 0.0);
+}
 
 __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base,
                                                                CsrDev A, double scaling, int fuse) {
   extern __shared__ __align__(16) double mgs_sm[];
-  double* vals = mgs_sm;               // kMgsSmThreads
-  double* red = vals + kMgsSmThreads;  // 32
-  double* scal = red + 32;             // 8
-  double* wl = scal + 8;               // chunk
+  double* vals = mgs_sm;                // kMgsSmThreads
+  double* vals2 = vals + kMgsSmThreads;  // kMgsSmThreads
+  double* red = vals2 + kMgsSmThreads;   // 32
+  double* scal = red + 32;              // 8
+  double* wl = scal + 8;                // chunk
   KCtrl* c = st.ctrl;
   if (c->done) return;
   if (c->breakdown) {  // the previous step found h(i-1,i-2) == 0 (istop = 2)
@@ -516,18 +604,18 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
   const int G = gridDim.x;
   const int b = blockIdx.x;
   const int bd = blockDim.x;
+  const int nv = i - 1;  // basis vectors to orthogonalise against
   const int64_t r0 = (int64_t)b * chunk;
   const int nloc = (int)max((int64_t)0, min(r0 + chunk, st.n) - r0);
   double* __restrict__ w = WAT(st, i) + r0;
-  double* part = st.partials;
+  double* part = st.partials;  // two buffers of 2 G partials
   unsigned nb = bar_base;
-  {  // the rows of w (loaded, or with fuse their SpMV formed here); dot with v_1
-    const double* __restrict__ wk = WAT(st, 1) + r0;
-    double acc = 0.0;
+  {  // the rows of w (loaded, or with fuse formed here); dots with v_1, v_2
+    const double* __restrict__ v1 = WAT(st, 1) + r0;
+    const double* __restrict__ v2 = WAT(st, nv >= 2 ? 2 : 1) + r0;
+    const bool two = nv >= 2;
+    double acc1 = 0.0, acc2 = 0.0;
     if (fuse) {
-      // w = scaling s_{i-1} A W_{i-1} (psfun_d_arnoldi.f90:202), each row's
-      // entries summed in order as k_ar_spmv does; saves that launch and the
-      // write and read of w
       const double f = scaling * st.s[i - 1];
       const double* __restrict__ x = WAT(st, i - 1);
       int l = threadIdx.x;
@@ -544,19 +632,19 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
 #pragma unroll
         for (int q = 0; q < 4; ++q) len = max(len, ke[q] - kb[q]);
         double sr[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int t = 0; t < len; t += 4) {
-          double vv[4][4], xv[4][4];
+        for (int t = 0; t < len; t += 2) {
+          double vv[4][2], xv[4][2];
 #pragma unroll
           for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 2; ++u) {
               const int k = kb[q] + t + u;
               const bool on = k < ke[q];
               vv[q][u] = on ? A.val[k] : 0.0;
               xv[q][u] = on ? __ldg(x + A.ja[k]) : 0.0;
             }
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
+          for (int u = 0; u < 2; ++u)
 #pragma unroll
             for (int q = 0; q < 4; ++q)
               if (kb[q] + t + u < ke[q]) sr[q] = fma(vv[q][u], xv[q][u], sr[q]);
@@ -565,7 +653,8 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
         for (int q = 0; q < 4; ++q) {
           const double v = f * sr[q];
           wl[l + q * bd] = v;
-          acc = fma(wk[l + q * bd], v, acc);
+          acc1 = fma(v1[l + q * bd], v, acc1);
+          if (two) acc2 = fma(v2[l + q * bd], v, acc2);
         }
       }
       for (; l < nloc; l += bd) {
@@ -574,91 +663,61 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
         for (int k = A.irp[r], ke = A.irp[r + 1]; k < ke; ++k) sr = fma(A.val[k], __ldg(x + A.ja[k]), sr);
         const double v = f * sr;
         wl[l] = v;
-        acc = fma(wk[l], v, acc);
+        acc1 = fma(v1[l], v, acc1);
+        if (two) acc2 = fma(v2[l], v, acc2);
       }
     } else {
       for (int l = threadIdx.x; l < nloc; l += bd) {
         const double v = w[l];
         wl[l] = v;
-        acc = fma(wk[l], v, acc);
+        acc1 = fma(v1[l], v, acc1);
+        if (two) acc2 = fma(v2[l], v, acc2);
       }
     }
-    block_sum_store_512(acc, vals, red, &part[b]);
+    block_sum2_store_512(acc1, acc2, vals, vals2, red, &part[b], two ? &part[G + b] : nullptr);
   }
   if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
-  for (int k = 1; k <= i - 1; ++k) {
-    const double tot = partials_sum_to0(part + (size_t)((k - 1) & 1) * G, G, red);
+  int buf = 0;
+  for (int k = 1; k <= nv; k += 2) {
+    const bool two = k + 1 <= nv;
+    const int kn = k + 2;
+    const int next = (kn > nv) ? 0 : ((kn + 1 <= nv) ? 2 : 1);
+    const double* pin = part + (size_t)buf * 2 * G;
+    double t1 = 0.0, t2 = 0.0;
+    partials_sum2_to0(pin, pin + G, G, two, red, &t1, &t2);
     if (threadIdx.x == 0) {
-      const double h = st.s[k] * tot;  // h(k,i-1) = v_k . w
-      if (b == 0) HAT(st, k, i - 1) = h;
-      scal[0] = h * st.s[k];
+      const double h1 = st.s[k] * t1;  // h(k,i-1) = v_k . w
+      if (b == 0) HAT(st, k, i - 1) = h1;
+      scal[0] = h1 * st.s[k];
+      if (two) {
+        const double h2 = st.s[k + 1] * t2;
+        if (b == 0) HAT(st, k + 1, i - 1) = h2;
+        scal[1] = h2 * st.s[k + 1];
+      }
     }
     __syncthreads();
-    const double cc = scal[0];
-    const double* __restrict__ wk = WAT(st, k) + r0;
-    double acc = 0.0;
-    int l = threadIdx.x;
-    if (k + 1 <= i - 1) {  // update with v_k fused with the dot of v_{k+1}
-      const double* __restrict__ wn = WAT(st, k + 1) + r0;
-      // the next group's loads are issued before this group's arithmetic
-      if (l + 3 * bd < nloc) {
-        double a[4], nx[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          a[q] = wk[l + q * bd];
-          nx[q] = wn[l + q * bd];
-        }
-        for (;;) {
-          const int ln = l + 4 * bd;
-          const bool more = ln + 3 * bd < nloc;
-          double a2[4], nx2[4];
-          if (more) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              a2[q] = wk[ln + q * bd];
-              nx2[q] = wn[ln + q * bd];
-            }
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const double v = fma(-cc, a[q], wl[l + q * bd]);
-            wl[l + q * bd] = v;
-            acc = fma(nx[q], v, acc);
-          }
-          l = ln;
-          if (!more) break;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) { a[q] = a2[q]; nx[q] = nx2[q]; }
-        }
-      }
-      for (; l < nloc; l += bd) {
-        const double v = fma(-cc, wk[l], wl[l]);
-        wl[l] = v;
-        acc = fma(wn[l], v, acc);
-      }
-    } else {  // last update fused with the norm
-      for (; l + 3 * bd < nloc; l += 4 * bd) {
-        double a[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a[q] = wk[l + q * bd];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const double v = fma(-cc, a[q], wl[l + q * bd]);
-          wl[l + q * bd] = v;
-          acc = fma(v, v, acc);
-        }
-      }
-      for (; l < nloc; l += bd) {
-        const double v = fma(-cc, wk[l], wl[l]);
-        wl[l] = v;
-        acc = fma(v, v, acc);
-      }
+    const double c1 = scal[0], c2 = two ? scal[1] : 0.0;
+    const double* __restrict__ vk = WAT(st, k) + r0;
+    const double* __restrict__ vk1 = two ? WAT(st, k + 1) + r0 : nullptr;
+    const double* __restrict__ vn1 = (next >= 1) ? WAT(st, kn) + r0 : nullptr;
+    const double* __restrict__ vn2 = (next == 2) ? WAT(st, kn + 1) + r0 : nullptr;
+    double acc1 = 0.0, acc2 = 0.0;
+    if (two) {
+      if (next == 2) mgs_pair_sweep<true, 2>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
+      else if (next == 1) mgs_pair_sweep<true, 1>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
+      else mgs_pair_sweep<true, 0>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
+    } else {
+      if (next == 2) mgs_pair_sweep<false, 2>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
+      else if (next == 1) mgs_pair_sweep<false, 1>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
+      else mgs_pair_sweep<false, 0>(wl, nloc, bd, c1, c2, vk, vk1, vn1, vn2, acc1, acc2);
     }
-    block_sum_store_512(acc, vals, red, &part[(size_t)(k & 1) * G + b]);
+    buf ^= 1;
+    double* pout = part + (size_t)buf * 2 * G;
+    block_sum2_store_512(acc1, acc2, vals, vals2, red, &pout[b], (next == 2) ? &pout[G + b] : nullptr);
     if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
   }
   for (int l = threadIdx.x; l < nloc; l += bd) w[l] = wl[l];
-  const double tot = partials_sum_to0(part + (size_t)((i - 1) & 1) * G, G, red);
+  const double tot = partials_sum_to0(part + (size_t)buf * 2 * G, G, red);
   if (b == 0 && threadIdx.x == 0) {
     const double beta = sqrt(tot);
     HAT(st, i, i - 1) = beta;
@@ -1417,7 +1476,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       }
       prof_begin(PROF_AR_MGS, s);
       if (gms > 0) {
-        unsigned bar_base = (unsigned)((int64_t)(i - 1) * i / 2 - 1);  // barriers of steps 2..i-1
+        unsigned bar_base = mgs_barriers_before(i);
         int fuse = fuse_spmv ? 1 : 0;
         double sc = scaling;
         void* args[] = {(void*)&st, (void*)&i, (void*)&mgs_chunk, (void*)&bar_base, (void*)&A, (void*)&sc,
