@@ -593,7 +593,7 @@ int psfun_gpu_serial_apply(psfun_serial* fun, int n, const double* a, int lda, d
   psf::NvtxRange nvtx_range("psfun_gpu_serial_apply");
   if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   if (n < 1 || lda < n) return PSFUN_ERR_FROM_SUBROUTINE;
-  DevBuf da, dx, dy;
+  static DevBuf da, dx, dy;  // kept between calls, grown as needed
   PSF_TRY(da.ensure(sizeof(double) * (size_t)n * n));
   PSF_TRY(dx.ensure(sizeof(double) * n));
   PSF_TRY(dy.ensure(sizeof(double) * n));
@@ -609,9 +609,6 @@ int psfun_gpu_serial_apply(psfun_serial* fun, int n, const double* a, int lda, d
         cudaStreamSynchronize(s) != cudaSuccess)
       rc = PSFUN_ERR_CUDA;
   }
-  da.release();
-  dx.release();
-  dy.release();
   return rc;
 }
 
@@ -632,7 +629,7 @@ int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, co
   if (!fun || !a || !x || !y) return PSFUN_ERR_INVALID_VECT_STATE;
   const int64_t n = a->n;
   if (n < 1 || n > 8192) return PSFUN_ERR_FROM_SUBROUTINE;
-  DevBuf da, dx, dy;
+  static DevBuf da, dx, dy;  // kept between calls, grown as needed
   PSF_TRY(da.ensure(sizeof(double) * (size_t)n * n));
   PSF_TRY(dx.ensure(sizeof(double) * n));
   PSF_TRY(dy.ensure(sizeof(double) * n));
@@ -648,9 +645,6 @@ int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, co
         cudaStreamSynchronize(s) != cudaSuccess)
       rc = PSFUN_ERR_CUDA;
   }
-  da.release();
-  dx.release();
-  dy.release();
   return rc;
 }
 

@@ -676,7 +676,18 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
     }
     block_sum2_store_512(acc1, acc2, vals, vals2, red, &part[b], two ? &part[G + b] : nullptr);
   }
+  // With concurrent istop = 1 estimates an estimate that converged (or
+  // failed) asks the steps still queued to stop: block 0 reads the request
+  // before the first barrier and every block reads its reading after it.
+  // The launches after a stop see done (set here, on the launching stream)
+  // and return before their first barrier, so no launch waits on a barrier
+  // count that a stopped one did not reach.
+  if (b == 0 && threadIdx.x == 0) c->stop_dec = *(volatile int*)&c->stop_req;
   if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
+  if (*(volatile int*)&c->stop_dec) {
+    if (b == 0 && threadIdx.x == 0) c->done = 1;
+    return;
+  }
   int buf = 0;
   for (int k = 1; k <= nv; k += 2) {
     const bool two = k + 1 <= nv;
@@ -747,6 +758,7 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
       st.errd_all[i] = errden;
       if (r < eps) {
         atomicMin(&c->conv_first, i);
+        *(volatile int*)&c->stop_req = 1;  // the steps still queued stop at their first barrier
         if (st.host_flag) st.host_flag[0] = 1;
       }
       return;
@@ -796,7 +808,11 @@ __device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps
     if (threadIdx.x == 0) {
       atomicOr(&c->err, rc);
       c->info = PSFUN_ERR_FROM_SUBROUTINE_NON;
-      c->done = 1;
+      // a concurrent estimate runs beside the steps' kernels, whose blocks
+      // must all take the same decision: it asks them to stop through
+      // stop_req (read once per launch by block 0), never through done
+      if (st.errn_all) *(volatile int*)&c->stop_req = 1;
+      else c->done = 1;
       if (st.host_flag) st.host_flag[0] = 1;
     }
     return;
@@ -1772,11 +1788,11 @@ int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, 
   if (!parse_fun(fun, &fp)) return PSFUN_ERR_FROM_SUBROUTINE;
   cudaStream_t s = stream();
   const size_t fs = fh_scratch_doubles(n, fp.phiorder) + 4 * (size_t)n * n + 8 * (size_t)n;
-  DevBuf scr;
+  static DevBuf scr;  // kept between calls, grown as needed
   PSF_TRY(scr.ensure(sizeof(double) * fs + 64));
   int rc = PSFUN_SUCCESS;
   if (fp.fname == FN_USERF) {
-    if (!fun->f_ptr) { scr.release(); return PSFUN_ERR_FROM_SUBROUTINE; }
+    if (!fun->f_ptr) return PSFUN_ERR_FROM_SUBROUTINE;
     rc = userf_apply(fun->f_ptr, fun->scaling, n, a_dev, lda, x_dev, y_dev, scr.as<double>());
   } else {
     int* dstat = reinterpret_cast<int*>(scr.as<char>() + sizeof(double) * fs);
@@ -1803,7 +1819,6 @@ int serial_apply_device(psfun_serial* fun, int n, const double* a_dev, int lda, 
       rc = PSFUN_ERR_FROM_SUBROUTINE;
     }
   }
-  scr.release();
   return rc;
 }
 
