@@ -138,8 +138,8 @@ int psfun_gpu_serial_apply_sparse(psfun_serial* fun, psfun_csr* a, double* y, co
 /* No counterpart in the reference.  y = f(scaling*a) x as psfun_gpu_serial_apply,
  * with device pointers a (lda), x, y, for callers that must not allocate device
  * memory: its scratch is one static 1 MiB __device__ array per device, held
- * until the process exits, instead of a cudaMalloc/cudaFree pair per call
- * (cudaFree waits for the whole device).  Accepts n <= 64 and, for PHI,
+ * until the process exits, instead of the device buffers that
+ * psfun_gpu_serial_apply allocates on first use.  Accepts n <= 64 and, for PHI,
  * phiorder <= 8 (the other functions ignore PHIORDER); larger sizes and USERF
  * return 111 with a message in psfun_gpu_last_error.  The first call on a
  * device looks up the array's address; make that first call before any stream
