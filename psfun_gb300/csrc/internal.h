@@ -81,7 +81,8 @@ struct KCtrl {
   int stop_req;   // the monitor asks the steps to stop
   int stop_dec;   // CTA 0's reading of stop_req, taken before a grid barrier
   int bd_step;    // step at which a Lanczos breakdown was found (0: none)
-  int conv_first; // concurrent Arnoldi estimates: the first converged iteration (INT_MAX: none)
+  int conv_first; // concurrent estimates: the first converged iteration (INT_MAX: none)
+  int est_last;   // concurrent estimates: the last iteration estimated
   alignas(128) double beta0;  // rs(1) = ||x||
   double errnum;
   double errden;

@@ -73,7 +73,7 @@ __global__ void k_reset(KState st, size_t small_doubles) {
     KCtrl* c = st.ctrl;
     c->done = c->conv = c->breakdown = c->itx = c->yk_len = c->nterms = c->err = c->info = 0;
     c->bar_count = c->bar_gen = c->red_counter = c->red_counter2 = 0u;
-    c->pub = c->stop_req = c->stop_dec = c->bd_step = 0;
+    c->pub = c->stop_req = c->stop_dec = c->bd_step = c->est_last = 0;
     c->conv_first = 0x7fffffff;
     c->beta0 = c->errnum = c->c1 = c->c2 = c->derr = 0.0;
     c->errden = 1.0;
@@ -227,22 +227,35 @@ struct EpiLzDot {
   }
 };
 
-// Monitor CTA of a persistent launch (the last block of the grid, outside
-// the grid barriers): it follows the steps as CTA 0 publishes their T entries
-// and asks them to stop (ms_monitor_cta: the shifted residuals of a
-// multi-shift solve; est_monitor_cta: the a posteriori estimate of istop = 1).
+// Monitor CTAs of a persistent launch (the last blocks of the grid, outside
+// the grid barriers): they follow the steps as CTA 0 publishes their T
+// entries and ask them to stop (ms_monitor_cta: the shifted residuals of a
+// multi-shift solve, one block; est_monitor_cta: the a posteriori estimates of
+// istop = 1, kEstMonitors blocks taking the iterations in turn).
 enum : int { LZ_PLAIN = 0, LZ_MON_SHIFTS = 1, LZ_MON_ESTIMATE = 2 };
+constexpr int kEstMonitors = 4;
+template <int MODE>
+constexpr int lz_monitors() {
+  return MODE == LZ_PLAIN ? 0 : (MODE == LZ_MON_SHIFTS ? 1 : kEstMonitors);
+}
 struct LzMonitor {
   MsParams mp;   // LZ_MON_SHIFTS
   FunParams fp;  // LZ_MON_ESTIMATE: f and its variant (scaling 1)
   double eps;
   int tridiag;
+  // LZ_MON_ESTIMATE: per iteration i its yk at yk_all + i * ldy (the error
+  // words in KState::errn_all/errd_all), per monitor r its dense scratch at
+  // scr + r * scr_stride
+  double* yk_all;
+  int ldy;
+  double* scr;
+  int64_t scr_stride;
 };
 __device__ __noinline__ void ms_monitor_cta(KState& st, const MsParams& mp, int i_begin, int i_end);
-__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end);
+__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end, int r);
 
-// MODE LZ_PLAIN: the grid is the compute CTAs.  Otherwise the grid has one
-// more block, the monitor.  The steps read the monitor's stop request through
+// MODE LZ_PLAIN: the grid is the compute CTAs.  Otherwise the grid has
+// lz_monitors<MODE>() more blocks, the monitors.  The steps read a monitor's stop request through
 // CTA 0: its thread 0 copies stop_req into stop_dec before arriving at the
 // first grid barrier of a step, and every CTA reads stop_dec after that
 // barrier, so all of them leave at the same step.  Steps run past the one at
@@ -263,10 +276,10 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
     }
     return;
   }
-  const int G = gridDim.x - (kMon ? 1 : 0), bid = blockIdx.x;
-  if (kMon && bid == G) {
+  const int G = gridDim.x - lz_monitors<MODE>(), bid = blockIdx.x;
+  if (kMon && bid >= G) {
     if (MODE == LZ_MON_SHIFTS) ms_monitor_cta(st, mon.mp, i_begin, i_end);
-    else est_monitor_cta(st, mon, i_begin, i_end);
+    else est_monitor_cta(st, mon, i_begin, i_end, bid - G);
     return;
   }
   lz_smem_init(sm);
@@ -847,6 +860,29 @@ __device__ int monitor_wait_pub(KCtrl* c, int want) {
   return p;
 }
 
+// For the estimate monitors, which take the iterations in turn: as
+// monitor_wait_pub, but returns -2 (without an error) once step `want` will
+// not be published because the steps stop before it: an estimate of an
+// earlier iteration converged or failed, or a breakdown ended the steps
+// before `want`.
+__device__ int monitor_wait_pub_or_end(KCtrl* c, int want) {
+  const unsigned long long t0 = globaltimer_ns();
+  int p;
+  while ((p = *(volatile int*)&c->pub) < want) {
+    if (*(volatile int*)&c->err != 0) return -1;
+    if (*(volatile int*)&c->conv_first <= want || *(volatile int*)&c->info != 0) return -2;
+    const int bd = *(volatile int*)&c->bd_step;
+    if (bd != 0 && bd < want) return -2;
+    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+      atomicOr(&c->err, DEVERR_TIMEOUT);
+      return -1;
+    }
+    __nanosleep(64);
+  }
+  __threadfence();
+  return p;
+}
+
 // Shifted residuals of the steps as they are published (each step's LDL^T
 // update of every shift depends on the previous one): per shift the LDL^T
 // pivot d and phi = last entry of (xi I + sign T_i)^{-1} e1, relative
@@ -943,36 +979,40 @@ __device__ __noinline__ void ms_monitor_cta(KState& st, const MsParams& mp, int 
   }
 }
 
-// The a posteriori estimate of istop = 1 (estimate_body) for the
-// iterations i = 2 .. i_end-1 of a solve, beside the steps: estimate i waits
-// for step i-1 to be published.  A breakdown found at the end of step i-1
-// ends the estimates there (psfun_d_lanczos.f90:225-230); on convergence the
-// estimate records itx and yk (estimate_tail) and asks the steps to stop.
-// One block: the dense evaluation runs without a helper group.
-__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end) {
+// The a posteriori estimates of istop = 1 (estimate_body) for the
+// iterations i = 2 .. i_end-1 of a solve, beside the steps: monitor r of
+// kEstMonitors takes the iterations first + r, first + r + kEstMonitors, ...,
+// and estimate i waits for step i-1 to be published.  Each estimate writes
+// its own words (yk slot, error numerator and denominator: the concurrent
+// form of estimate_tail); one that converges records its iteration with
+// atomicMin on conv_first and asks the steps to stop, and the first
+// converged iteration is taken after the launch (k_par_select), as the
+// serial order would have stopped there.  A breakdown found at the end of
+// step i-1 ends the estimates there (psfun_d_lanczos.f90:225-230).  One
+// block per estimate: the dense evaluation runs without a helper group.
+__device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, int i_begin, int i_end, int r) {
   __shared__ DenseSmem dsm;
   __shared__ int s_pub;
   KCtrl* c = st.ctrl;
   dense_group_begin(dsm, nullptr);
+  KState ste = st;
+  ste.fscratch = mon.scr + (size_t)r * mon.scr_stride;
   int pub = i_begin - 1;
-  for (int i = max(2, i_begin + 1); i < i_end; ++i) {
+  for (int i = max(2, i_begin + 1) + r; i < i_end; i += kEstMonitors) {
     if (pub < i - 1) {
-      if (threadIdx.x == 0) s_pub = monitor_wait_pub(c, i - 1);
+      if (threadIdx.x == 0) s_pub = monitor_wait_pub_or_end(c, i - 1);
       __syncthreads();
       pub = s_pub;
       __syncthreads();
       if (pub < 0) return;
     }
-    if (*(volatile int*)&c->bd_step == i - 1) return;  // 0: no breakdown (i - 1 >= 1)
-    estimate_body(st, mon.fp, i, mon.eps, mon.tridiag, dsm, false);
+    const int bd = *(volatile int*)&c->bd_step;
+    if (bd != 0 && bd <= i - 1) return;  // 0: no breakdown (i - 1 >= 1)
+    ste.yk = mon.yk_all + (size_t)i * mon.ldy;
+    estimate_body(ste, mon.fp, i, mon.eps, mon.tridiag, dsm, false);
     __syncthreads();
-    if (*(volatile int*)&c->done) {  // converged (or failed): stop the steps
-      if (threadIdx.x == 0) {
-        __threadfence();
-        *(volatile int*)&c->stop_req = 1;
-      }
-      return;
-    }
+    if (threadIdx.x == 0) atomicMax(&c->est_last, i);
+    if (*(volatile int*)&c->info != 0 || *(volatile int*)&c->conv_first <= i) return;
   }
 }
 
@@ -1097,6 +1137,7 @@ __global__ void k_par_select(KState st, const double* yk_all, int ldy, int i_las
   KCtrl* c = st.ctrl;
   const int j = c->conv_first;
   if (c->beta0 == 0.0 || c->info != 0) return;
+  if (i_last < 0) i_last = c->est_last;  // the monitors' last estimate
   if (j != 0x7fffffff) {
     const int m = j - 1;
     for (int l = threadIdx.x; l < m; l += blockDim.x) st.yk[l] = yk_all[(size_t)j * ldy + l];
@@ -1298,10 +1339,10 @@ static int persist_grid() {
 template <int MODE>
 static int launch_lz_persist_mode(KState& st, const CsrDev& A, int i_begin, int i_end, const LzMonitor& mon,
                                   cudaStream_t s) {
-  const int extra = (MODE == LZ_PLAIN) ? 0 : 1;
+  const int extra = lz_monitors<MODE>();
   int G = persist_grid<MODE>() - extra;
   if (G < 1) {
-    set_last_error("persistent Lanczos: no room for the monitor block");
+    set_last_error("persistent Lanczos: no room for the monitor blocks");
     return PSFUN_ERR_CUDA;
   }
   int tpc = (A.ntiles + G - 1) / G;
@@ -1333,9 +1374,11 @@ static int grid_for(int64_t items, int threads, int per_sm) {
 // Grid and rows per block of k_ar_mgs_sm for n rows, or 0 when the rows of a
 // block do not fit in shared memory.
 static int mgs_sm_plan(int64_t n, int* chunk) {
-  // at least 2048 rows per block: a small basis needs few blocks, and each
-  // sweep's grid barrier costs less with fewer arrivals
-  const int G = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (n + 2047) / 2048));
+  // at least 512 rows per block: a paired sweep costs each block 4 FMAs per
+  // row (512 rows: 64 FP64 warp instructions over the SM's four
+  // sub-partitions, about 1 us), so below that the grid barrier (more costly
+  // with more arrivals) outweighs the FP64 time that another block saves
+  const int G = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (n + 511) / 512));
   int64_t ch = (n + G - 1) / G;
   ch = (ch + 1) & ~(int64_t)1;
   const size_t bytes = kMgsSmFixed + sizeof(double) * (size_t)ch;
@@ -1533,15 +1576,46 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   };
 
   // istop = 1 Lanczos whose estimate runs on one block: every step and every
-  // estimate in one persistent launch (the estimate on its monitor block)
-  const bool lz_mon = istop == 1 && !arnoldi && !sai && !userf && dense_blocks(fpk, nl + 1, true) == 1;
+  // estimate in one persistent launch (the estimate on its monitor block,
+  // beside the steps, so its latency hides behind them: a product-based f
+  // qualifies while its products of order m fill one round of a block's
+  // 256 threads in 4-row strips, m (m + 3) / 4 <= 256, i.e. m <= 31)
+  const int m_mon = nl + 1 + (fpk.fname == FN_PHI ? fpk.phiorder + 1 : 0);
+  const bool lz_mon = istop == 1 && !arnoldi && !sai && !userf &&
+                      (dense_blocks(fpk, nl + 1, true) == 1 || (long)((m_mon + 3) / 4) * m_mon <= kDenseThreads);
+  // the monitors' words: yk per iteration, error numerator and denominator
+  // per iteration, a dense scratch per monitor (allocated here, before any
+  // capture; 256-byte aligned regions for the complex variants' 16-byte pairs)
+  double* lz_yk_all = nullptr;
+  double* lz_scr = nullptr;
+  int64_t lz_scr_stride = 0;
+  if (lz_mon) {
+    auto al32 = [](size_t d) { return (d + 31) & ~(size_t)31; };
+    const size_t ldy = (size_t)nl + 1;
+    lz_scr_stride = (int64_t)al32(fh_scratch_doubles(nl + 1, fp.phiorder) + 64);
+    const size_t o_errn = al32((ldy + 1) * ldy), o_errd = o_errn + al32(ldy + 2), o_scr = o_errd + al32(ldy + 2);
+    PSF_TRY(meth->par.ensure(sizeof(double) * (o_scr + (size_t)kEstMonitors * lz_scr_stride + 64)));
+    double* pb = meth->par.as<double>();
+    lz_yk_all = pb;
+    st.errn_all = pb + o_errn;
+    st.errd_all = pb + o_errd;
+    lz_scr = pb + o_scr;
+  }
   auto launch_lz_estimating = [&]() -> int {
     LzMonitor mon;
     memset(&mon, 0, sizeof mon);
     mon.fp = fpk;
     mon.eps = eps;
     mon.tridiag = 1;
-    return launch_lz_persist_mode<LZ_MON_ESTIMATE>(st, A, 1, nl + 1, mon, s);
+    mon.yk_all = lz_yk_all;
+    mon.ldy = nl + 1;
+    mon.scr = lz_scr;
+    mon.scr_stride = lz_scr_stride;
+    PSF_TRY(launch_lz_persist_mode<LZ_MON_ESTIMATE>(st, A, 1, nl + 1, mon, s));
+    k_par_select<<<1, kDenseThreads, 0, s>>>(st, lz_yk_all, nl + 1, -1);
+    count_launch();
+    PSF_CUDA(cudaGetLastError());
+    return PSFUN_SUCCESS;
   };
   if ((istop == 2 || lz_mon) && !userf && !prof_enabled() && !sai) {
     // fixed-length solve: one CUDA graph, captured once per launch key
@@ -1550,11 +1624,11 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     struct Key {
       const void* a; const void* x; void* y; const void* V; int64_t n; int nl, arnoldi, keeplast, gs, gv, gm;
       FunParams fp; double scaling;
-      const void *irp, *ja, *val, *tiles;
+      const void *irp, *ja, *val, *tiles, *par;
       int istop; double eps;
     } key;
     memset(&key, 0, sizeof key);
-    key.istop = istop; key.eps = eps;
+    key.istop = istop; key.eps = eps; key.par = lz_mon ? meth->par.ptr : nullptr;
     key.irp = A.irp; key.ja = A.ja; key.val = A.val; key.tiles = A.tile_desc;
     key.a = a; key.x = x; key.y = y; key.V = st.V; key.n = n; key.nl = nl; key.arnoldi = arnoldi;
     key.keeplast = meth->keeplast; key.gs = gs; key.gv = gv; key.gm = gm; key.fp = fpk; key.scaling = scaling;
@@ -2182,60 +2256,112 @@ __global__ void k_adj_R(AdjShifts sh, int mg, int mx, const double* solg, const 
 // y = sum_p coef[p] W_p (p < m)
 __global__ void __launch_bounds__(kVecThreads) k_lincomb(const double* V, int64_t ldv, int64_t n, const double* coef,
                                                          int m, double* y) {
+  // the terms are summed in order; four loads are issued ahead of their FMAs
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double acc = 0.0;
-    for (int p = 0; p < m; ++p) acc = fma(coef[p], V[(size_t)p * ldv + r], acc);
+    int p = 0;
+    for (; p + 4 <= m; p += 4) {
+      const double a0 = V[(size_t)p * ldv + r], a1 = V[(size_t)(p + 1) * ldv + r];
+      const double a2 = V[(size_t)(p + 2) * ldv + r], a3 = V[(size_t)(p + 3) * ldv + r];
+      acc = fma(coef[p], a0, acc);
+      acc = fma(coef[p + 1], a1, acc);
+      acc = fma(coef[p + 2], a2, acc);
+      acc = fma(coef[p + 3], a3, acc);
+    }
+    for (; p < m; ++p) acc = fma(coef[p], V[(size_t)p * ldv + r], acc);
     y[r] = acc;
   }
 }
 
-constexpr int kAdjChunk = 16;
+// Columns of R' per pass, held in registers: the m_x columns in equal chunks
+// of at most 16 (so no FMA is spent on padding columns).
+static int adj_chunk(int mx) {
+  const int nch = (mx + 15) / 16;
+  return (mx + nch - 1) / nch;
+}
 
-// P[q][i] = sum_p Wg[p][i] R'[p][q], q in chunks of 16 held in registers
+// P[q][i] = sum_p Wg[p][i] R'[p][q], q in chunks of C held in registers
+template <int C>
 __global__ void __launch_bounds__(kVecThreads) k_adj_P(const double* Wg, int64_t ldg, int mg, const double* R, int mx,
                                                        int64_t n, double* P, int64_t ldp) {
-  extern __shared__ double Rs[];  // mg x kAdjChunk
-  for (int q0 = 0; q0 < mx; q0 += kAdjChunk) {
-    const int qn = min(kAdjChunk, mx - q0);
+  extern __shared__ double Rs[];  // mg x C
+  for (int q0 = 0; q0 < mx; q0 += C) {
+    const int qn = min(C, mx - q0);
     __syncthreads();
-    for (int e = threadIdx.x; e < mg * kAdjChunk; e += blockDim.x) {
-      const int p = e / kAdjChunk, qq = e - p * kAdjChunk;
+    for (int e = threadIdx.x; e < mg * C; e += blockDim.x) {
+      const int p = e / C, qq = e - p * C;
       Rs[e] = (qq < qn) ? R[(size_t)p * mx + q0 + qq] : 0.0;
     }
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-      double acc[kAdjChunk];
+      double acc[C];
 #pragma unroll
-      for (int qq = 0; qq < kAdjChunk; ++qq) acc[qq] = 0.0;
+      for (int qq = 0; qq < C; ++qq) acc[qq] = 0.0;
       for (int p = 0; p < mg; ++p) {
         const double w = Wg[(size_t)p * ldg + i];
 #pragma unroll
-        for (int qq = 0; qq < kAdjChunk; ++qq) acc[qq] = fma(w, Rs[p * kAdjChunk + qq], acc[qq]);
+        for (int qq = 0; qq < C; ++qq) acc[qq] = fma(w, Rs[p * C + qq], acc[qq]);
       }
       for (int qq = 0; qq < qn; ++qq) P[(size_t)(q0 + qq) * ldp + i] = acc[qq];
     }
   }
 }
 
-// grad[k] = sum_q P[q][i] Wx[q][ja[k]] for every stored entry k of row i
+// grad[k] = sum_q P[q][i] Wx[q][ja[k]] for every stored entry k of row i;
+// a chunk's C gathers of an entry are issued before its FMAs
+template <int C>
 __global__ void __launch_bounds__(kVecThreads) k_adj_sddmm(CsrDev A, const double* P, int64_t ldp, const double* Wx,
                                                            int64_t ldx, int mx, double* grad) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.n; i += (int64_t)gridDim.x * blockDim.x) {
     const int kb = A.irp[i], ke = A.irp[i + 1];
-    for (int q0 = 0; q0 < mx; q0 += kAdjChunk) {
-      const int qn = min(kAdjChunk, mx - q0);
-      double pi[kAdjChunk];
+    for (int q0 = 0; q0 < mx; q0 += C) {
+      const int qn = min(C, mx - q0);
+      double pi[C];
 #pragma unroll
-      for (int qq = 0; qq < kAdjChunk; ++qq) pi[qq] = (qq < qn) ? P[(size_t)(q0 + qq) * ldp + i] : 0.0;
+      for (int qq = 0; qq < C; ++qq) pi[qq] = (qq < qn) ? P[(size_t)(q0 + qq) * ldp + i] : 0.0;
       for (int k = kb; k < ke; ++k) {
         const int j = A.ja[k];
+        double xv[C];
+#pragma unroll
+        for (int qq = 0; qq < C; ++qq) xv[qq] = (qq < qn) ? __ldg(Wx + (size_t)(q0 + qq) * ldx + j) : 0.0;
         double acc = (q0 == 0) ? 0.0 : grad[k];
-        for (int qq = 0; qq < qn; ++qq) acc = fma(pi[qq], __ldg(Wx + (size_t)(q0 + qq) * ldx + j), acc);
+#pragma unroll
+        for (int qq = 0; qq < C; ++qq)
+          if (qq < qn) acc = fma(pi[qq], xv[qq], acc);
         grad[k] = acc;
       }
     }
   }
 }
+
+// P = W_g R' (adj_P) and the sampled product on A's pattern (adj_sddmm), with
+// the chunk size of adj_chunk(mx): one instantiation per size 1..16.
+#define PSF_ADJ_DISPATCH(call)                                                                   \
+  switch (adj_chunk(mx)) {                                                                       \
+    case 1: call(1); break;   case 2: call(2); break;   case 3: call(3); break;                  \
+    case 4: call(4); break;   case 5: call(5); break;   case 6: call(6); break;                  \
+    case 7: call(7); break;   case 8: call(8); break;   case 9: call(9); break;                  \
+    case 10: call(10); break; case 11: call(11); break; case 12: call(12); break;                \
+    case 13: call(13); break; case 14: call(14); break; case 15: call(15); break;                \
+    default: call(16); break;                                                                    \
+  }
+
+static void adj_P(const double* Wg, int64_t ldg, int mg, const double* R, int mx, int64_t n, double* P, int64_t ldp,
+                  cudaStream_t s) {
+  const int g = grid_for(n, kVecThreads, 4);
+#define PSF_ADJ_P(c) k_adj_P<c><<<g, kVecThreads, sizeof(double) * mg * (c), s>>>(Wg, ldg, mg, R, mx, n, P, ldp)
+  PSF_ADJ_DISPATCH(PSF_ADJ_P)
+#undef PSF_ADJ_P
+}
+
+static void adj_sddmm(const CsrDev& A, const double* P, int64_t ldp, const double* Wx, int64_t ldx, int mx,
+                      double* grad, cudaStream_t s) {
+  const int g = grid_for(A.n, kVecThreads, 4);
+#define PSF_ADJ_S(c) k_adj_sddmm<c><<<g, kVecThreads, 0, s>>>(A, P, ldp, Wx, ldx, mx, grad)
+  PSF_ADJ_DISPATCH(PSF_ADJ_S)
+#undef PSF_ADJ_S
+}
+#undef PSF_ADJ_DISPATCH
 
 // out = g . v (two-pass, deterministic)
 __global__ void __launch_bounds__(kVecThreads) k_dot_partial(const double* a, const double* b, int64_t n, double* part) {
@@ -2395,8 +2521,7 @@ static int expm_adjoint_arnoldi(psfun_csr* a, double t, const double* x, const d
     k_adj_vanloan_R<<<std::max(1, std::min(1024, (mg * mx + 255) / 256)), 256, 0, s>>>(
         E, M, mg, mx, t, wg->ctrl.as<KCtrl>(), cx_save, small_of(wg) + (size_t)ldh * ldh, sx_save, R);
     const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
-    k_adj_P<<<gv, kVecThreads, sizeof(double) * mg * kAdjChunk, s>>>(wg->V.as<double>(), wg->ldv, mg, R, mx, n, P,
-                                                                       ld);
+    adj_P(wg->V.as<double>(), wg->ldv, mg, R, mx, n, P, ld, s);
     count_launch(2);
     const double* Wx = arx->V.as<double>();
     int64_t ldx = arx->ldv;
@@ -2410,7 +2535,7 @@ static int expm_adjoint_arnoldi(psfun_csr* a, double t, const double* x, const d
       Wx = arx->V.as<double>();
       ldx = arx->ldv;
     }
-    k_adj_sddmm<<<gv, kVecThreads, 0, s>>>(a->dev(), P, ld, Wx, ldx, mx, grad_vals);
+    adj_sddmm(a->dev(), P, ld, Wx, ldx, mx, grad_vals, s);
     count_launch();
     int hs = -1;
     PSF_CUDA(cudaMemcpyAsync(&hs, stat.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -2482,7 +2607,7 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
   const int mx = rx.m;
   if (mx < 1) return PSFUN_ERR_FROM_SUBROUTINE_NON;
   k_adj_solve<<<1, 32, 0, s>>>(rx.st, sh, mx, solx, band, coefy, sx);
-  k_lincomb<<<gv, kVecThreads, 0, s>>>(rx.st.V, rx.st.ldv, n, coefy, mx, ytmp);
+  k_lincomb<<<grid_for(n, kVecThreads, 4), kVecThreads, 0, s>>>(rx.st.V, rx.st.ldv, n, coefy, mx, ytmp);
   count_launch(2);
   if (!grad_x && !grad_t && !grad_vals) {  // forward only
     KCtrl hx;
@@ -2501,14 +2626,13 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
   k_adj_solve<<<1, 32, 0, s>>>(rg.st, sh, mg, solg, band, coefg, sg);
   count_launch();
   if (grad_x) {
-    k_lincomb<<<gv, kVecThreads, 0, s>>>(rg.st.V, rg.st.ldv, n, coefg, mg, grad_x);
+    k_lincomb<<<grid_for(n, kVecThreads, 4), kVecThreads, 0, s>>>(rg.st.V, rg.st.ldv, n, coefg, mg, grad_x);
     count_launch();
   }
   if (grad_vals) {
     k_adj_R<<<std::max(1, (mg * mx + 255) / 256), 256, 0, s>>>(sh, mg, mx, solg, solx, sg, sx, R);
     PSF_TRY(pbuf.ensure(sizeof(double) * (size_t)mx * ld));
-    k_adj_P<<<gv, kVecThreads, sizeof(double) * mg * kAdjChunk, s>>>(rg.st.V, rg.st.ldv, mg, R, mx, n,
-                                                                       pbuf.as<double>(), ld);
+    adj_P(rg.st.V, rg.st.ldv, mg, R, mx, n, pbuf.as<double>(), ld, s);
     count_launch(2);
     const double* Wx = rx.st.V;
     int64_t ldx = rx.st.ldv;
@@ -2522,7 +2646,7 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
       Wx = rx2.st.V;
       ldx = rx2.st.ldv;
     }
-    k_adj_sddmm<<<gv, kVecThreads, 0, s>>>(a->dev(), pbuf.as<double>(), ld, Wx, ldx, mx, grad_vals);
+    adj_sddmm(a->dev(), pbuf.as<double>(), ld, Wx, ldx, mx, grad_vals, s);
     count_launch();
   }
   if (grad_t) {
