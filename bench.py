@@ -275,11 +275,20 @@ def bench_arnoldi_phi(torch, pg, peak_gbs: float, reps: int = 3):
     y_exact = exact.convdiff_phi1(2048, x, p.params["t"])
     rel = float(np.linalg.norm(yd.cpu().numpy() - y_exact) / np.linalg.norm(y_exact))
     del a, xd, yd
+    # The FP64 roof: per step with j basis vectors the SpMV (nnz FMAs) and the
+    # Gram-Schmidt (two FMAs per row per vector and the norm), then the
+    # recombination; against 2 DFMA per clock per SM at the maximum SM clock.
+    dfma = sum(nnz + (2 * j + 1) * n for j in range(1, m)) + m * n
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    fp64_peak = 2.0 * sms * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
     return {"workload": "2-D convection-diffusion 2048^2 (n=4,194,304, nnz=20,963,328), y=phi_1(-1e-3 A)x, "
                         "Arnoldi m=60 (istop 2)",
             "ms_per_solve": 1e3 * dt, "solves_per_s": 1.0 / dt, "algorithmic_bytes_per_solve": nbytes,
             "achieved_GBs": nbytes / dt / 1e9, "frac_of_hbm_peak": nbytes / dt / 1e9 / peak_gbs,
-            "rel_err_m60_vs_exact": rel}
+            "algorithmic_dfma_per_solve": dfma, "achieved_gdfma_s": dfma / dt / 1e9,
+            "fp64_peak_gdfma_s": fp64_peak / 1e9, "frac_of_fp64_peak": dfma / dt / fp64_peak,
+            "fp64_floor_ms": 1e3 * dfma / fp64_peak, "rel_err_m60_vs_exact": rel}
 
 
 def bench_multishift(torch, pg, peak_gbs: float, reps: int = 3):
