@@ -283,3 +283,34 @@ def test_pinned_host_vectors_in_place(lib, kname, variant, istop):
     # in place: y is x
     r2 = meth.apply(fun, a, xp.numpy(), 1e-10, itmax=60, istop=istop, y=xp.numpy())
     assert r2.info == 0 and np.array_equal(xp.numpy(), ref.y)
+
+
+@pytest.mark.parametrize("variant", ["CHBSYM", "GENPADE"])
+def test_lanczos_istop1_estimate_monitors(lib, orc, variant):
+    """istop = 1 Lanczos in one launch, its a posteriori estimates on four
+    monitor blocks that take the iterations in turn: every combination of a
+    short Krylov dimension (the monitors with no iteration, or one) and an
+    eps that converges at each early iteration matches the oracle's serial
+    loop (same iteration count and estimate, y within 1e-10), and the breakdown
+    case stops the estimates where psfun_d_lanczos.f90:225-230 does."""
+    A = -0.5 * matrices.laplacian_2d(20)
+    x = matrices.unit(np.random.default_rng(21).standard_normal(A.shape[0]))
+    for itmax in (2, 3, 4, 5, 6, 9, 14):
+        for eps in (1e-1, 1e-3, 1e-6, 1e-9, 1e-13):
+            g = run_gpu("LANCZOS", "EXP", variant, 1.0, A, x, eps, itmax=itmax, istop=1)
+            o = run_orc(orc, "LANCZOS", "EXP", variant, 1.0, A, x, eps, itmax=itmax, istop=1)
+            # (itmax 2 without convergence leaves a null projected matrix:
+            # 4011 from both)
+            assert g.info == o["info"], (itmax, eps, g.info, o["info"])
+            if o["info"] != 0:
+                continue
+            assert g.iter == o["iter"], (itmax, eps, g.iter, o["iter"])
+            # the estimate divides by yk's last entry, which rounding moves
+            # relative to its own small size
+            assert abs(g.err - o["err"]) <= 1e-3 * abs(o["err"]) + 1e-15, (itmax, eps, g.err, o["err"])
+            assert rel(g.y, o["y"]) <= TOL, (itmax, eps)
+    from test_oracle_krylov import lanczos_breakdown_case
+    B, xb = lanczos_breakdown_case()
+    g = run_gpu("LANCZOS", "EXP", variant, 1.0, B, xb, 1e-14, itmax=10, istop=1)
+    o = run_orc(orc, "LANCZOS", "EXP", variant, 1.0, B, xb, 1e-14, itmax=10, istop=1)
+    assert g.info == o["info"] == 0 and g.iter == o["iter"] and rel(g.y, o["y"]) <= TOL
