@@ -314,3 +314,25 @@ def test_lanczos_istop1_estimate_monitors(lib, orc, variant):
     g = run_gpu("LANCZOS", "EXP", variant, 1.0, B, xb, 1e-14, itmax=10, istop=1)
     o = run_orc(orc, "LANCZOS", "EXP", variant, 1.0, B, xb, 1e-14, itmax=10, istop=1)
     assert g.info == o["info"] == 0 and g.iter == o["iter"] and rel(g.y, o["y"]) <= TOL
+
+
+def test_arnoldi_istop1_concurrent_estimates_stop(lib, orc):
+    """istop = 1 Arnoldi: the estimates run beside the steps and the first
+    converged one stops the steps still queued (at their first grid barrier,
+    all blocks alike).  Krylov dimensions 2..12 and eps from 1e-1 to 1e-12 on
+    a nonsymmetric operator match the oracle's serial loop (same iteration
+    count, y within 1e-10), and a solve after an early stop is unaffected."""
+    A = -1e-3 * matrices.convdiff_2d(24)
+    x = matrices.unit(np.random.default_rng(22).standard_normal(A.shape[0]))
+    for itmax in (2, 3, 5, 8, 12):
+        for eps in (1e-1, 1e-4, 1e-8, 1e-12):
+            g = run_gpu("ARNOLDI", "EXP", "GENPADE", 1.0, A, x, eps, itmax=itmax, istop=1)
+            o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", 1.0, A, x, eps, itmax=itmax, istop=1)
+            assert g.info == o["info"], (itmax, eps, g.info, o["info"])
+            if o["info"] != 0:
+                continue
+            assert g.iter == o["iter"], (itmax, eps, g.iter, o["iter"])
+            assert rel(g.y, o["y"]) <= TOL, (itmax, eps)
+    g = run_gpu("ARNOLDI", "EXP", "GENPADE", 1.0, A, x, 1e-12, itmax=40, istop=2)
+    o = run_orc(orc, "ARNOLDI", "EXP", "GENPADE", 1.0, A, x, 1e-12, itmax=40, istop=2)
+    assert g.info == 0 and g.iter == o["iter"] and rel(g.y, o["y"]) <= TOL
