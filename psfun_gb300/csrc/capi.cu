@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "persist.cuh"
 
 namespace psf {
 
@@ -476,13 +477,24 @@ int csr_transpose(psfun_csr* a, psfun_csr** out) {
   return PSFUN_SUCCESS;
 }
 
+// y = alpha A x + beta y through the warp-specialised tile pipeline of the
+// persistent kernels (persist.cuh): one block per SM over a contiguous range
+// of tiles, the last warp staging up to four tiles ahead by TMA.
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_axpby(CsrDev A, const double* x, double alpha, double beta,
-                                                             double* y, int* err) {
-  PSF_SPMV_SMEM();
-  spmv_smem_init(sm);
+                                                             double* y, int* err, int tiles_per_cta) {
+  extern __shared__ __align__(128) unsigned char lz_smem_raw[];
+  LzSmem& sm = *reinterpret_cast<LzSmem*>(lz_smem_raw);
+  const int t0 = min(A.ntiles, (int)blockIdx.x * tiles_per_cta);
+  const int t1 = min(A.ntiles, t0 + tiles_per_cta);
+  if (t0 >= t1) return;
+  lz_smem_init(sm);
+  const bool stream = A.stream != 0;
+  PipeCounters pc{0u, 0u};
+  if (threadIdx.x == kConsumerWarps * 32) {
+    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued, stream)) atomicOr(err, DEVERR_TIMEOUT);
+  }
   EpiAxpby epi{alpha, beta, y};
-  spmv_tiles(A, x, epi, sm, err);
-  spmv_sched_done(A);
+  pipe_spmv(A, x, t0, t1, sm, epi, err, pc, false, stream);
 }
 
 int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double* y) {
@@ -491,12 +503,10 @@ int spmv_device(psfun_csr* a, double alpha, const double* x, double beta, double
   cudaStream_t s = stream();
   PSF_CUDA(cudaMemsetAsync(errbuf.ptr, 0, sizeof(int), s));
   if (a->ntiles > 0) {
-    static bool attr = false;
-    if (!attr) { spmv_smem_attr(k_spmv_axpby); attr = true; }
-    int g = a->ntiles;
-    const int cap = sm_count() * 4;
-    if (g > cap) g = cap;
-    k_spmv_axpby<<<g, kSpmvThreads, kSpmvSmemBytes, s>>>(a->dev(), x, alpha, beta, y, errbuf.as<int>());
+    static const int gmax = persist_grid_for(k_spmv_axpby);
+    const int tpc = std::max(1, (a->ntiles + gmax - 1) / gmax);
+    const int g = std::max(1, (a->ntiles + tpc - 1) / tpc);
+    k_spmv_axpby<<<g, kSpmvThreads, kLzSmemBytes, s>>>(a->dev(), x, alpha, beta, y, errbuf.as<int>(), tpc);
     count_launch();
     PSF_CUDA(cudaGetLastError());
   }

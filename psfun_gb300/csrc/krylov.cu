@@ -107,90 +107,6 @@ __global__ void __launch_bounds__(kVecThreads) k_init(KState st, const double* _
   });
 }
 
-// Lanczos: u = A W_i and alpha_i = v_i . A v_i = s_i^2 (W_i . u)
-// (psfun_d_lanczos.f90:198-204, :239-246).  u stays unscaled; s_i is folded
-// into alpha and into the update coefficients.
-__global__ void __launch_bounds__(kSpmvThreads) k_lz_spmv(KState st, CsrDev A, int i) {
-  PSF_SPMV_SMEM();
-  KCtrl* c = st.ctrl;
-  if (c->done) return;
-  if (c->breakdown) {  // |beta_i| < 1e-16 found by the previous update: exit at the top of iteration i
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      c->done = 1;
-      if (st.host_flag) st.host_flag[0] = 1;
-    }
-    return;
-  }
-  spmv_smem_init(sm);
-  const double sc = st.s[i];
-  const double* wi = WAT(st, i);
-  EpiDot epi{st.u, wi, 0.0};
-  spmv_tiles(A, wi, epi, sm, &c->err);
-  spmv_sched_done(A);
-  const double acc = block_sum(epi.acc, sm.red);
-  last_block_reduce(acc, st.partials, &c->red_counter, sm.red, [&](double tot) {
-    const double alpha = sc * sc * tot;
-    HAT(st, i, i) = alpha;
-    // w = s_i (u - alpha W_i - (beta_i s_{i-1} / s_i) W_{i-1})
-    c->c1 = alpha;
-    c->c2 = (i >= 2) ? HAT(st, i - 1, i) * st.s[i - 1] / sc : 0.0;
-    if (i >= 2) c->itx = i - 1;
-  });
-}
-
-// Lanczos: w = A v_i - alpha_i v_i - beta_i v_{i-1} = s_i w' with
-// w' = u - alpha_i W_i - (beta_i s_{i-1}/s_i) W_{i-1}; stored as
-// W_{i+1} = 2^k w', 2^k the power of two nearest below s_i, so the stored
-// vectors keep norms of order ||A|| (the power-of-two scaling is exact and
-// costs no FP64 instruction).  beta_{i+1} = ||w|| = s_i ||w'||,
-// s_{i+1} = 1 / (2^k ||w'||).  (psfun_d_lanczos.f90:212, :221-230, :254-266)
-__global__ void __launch_bounds__(kVecThreads, 4) k_lz_update(KState st, int i) {
-  __shared__ double red[32];
-  KCtrl* c = st.ctrl;
-  if (c->done) return;
-  const double c1 = c->c1, c2 = c->c2;
-  const int k2 = ilog2_normal(st.s[i]);
-  const double* __restrict__ u = st.u;
-  const double* __restrict__ wi = WAT(st, i);
-  const double* __restrict__ wm = (i >= 2) ? WAT(st, i - 1) : wi;
-  double* __restrict__ wo = WAT(st, i + 1);
-  double acc = 0.0;
-  const int64_t npair = st.n >> 1;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npair; p += stride) {
-    const double2 uu = reinterpret_cast<const double2*>(u)[p];
-    const double2 a = reinterpret_cast<const double2*>(wi)[p];
-    const double2 b = reinterpret_cast<const double2*>(wm)[p];
-    const double w0 = fma(-c2, b.x, fma(-c1, a.x, uu.x));
-    const double w1 = fma(-c2, b.y, fma(-c1, a.y, uu.y));
-    acc = fma(w0, w0, acc);
-    acc = fma(w1, w1, acc);
-    double2 w;
-    w.x = scale_pow2(w0, k2);
-    w.y = scale_pow2(w1, k2);
-    reinterpret_cast<double2*>(wo)[p] = w;
-  }
-  if ((st.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    const int64_t r = st.n - 1;
-    const double w = fma(-c2, wm[r], fma(-c1, wi[r], u[r]));
-    wo[r] = scale_pow2(w, k2);
-    acc = fma(w, w, acc);
-  }
-  acc = block_sum(acc, red);
-  last_block_reduce(acc, st.partials, &c->red_counter, red, [&](double tot) {
-    const double wn = sqrt(tot);
-    const double b = st.s[i] * wn;
-    HAT(st, i, i + 1) = b;
-    HAT(st, i + 1, i) = b;
-    st.s[i + 1] = 1.0 / ldexp(wn, k2);
-    if (i + 1 <= st.nl && fabs(b) < 1e-16) {  // checked at the top of iteration i+1
-      c->breakdown = 1;
-      c->itx = i;
-    }
-    if (st.host_flag) st.host_flag[1] = i;
-  });
-}
-
 // ---------------------------------------------------------------------------
 // Persistent Lanczos: steps [i_begin, i_end) in one cooperative launch.
 // Each CTA owns a contiguous range of row tiles (static schedule: the tile
@@ -429,15 +345,27 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
   if (bid == 0 && threadIdx.x == 0) st.s[i_end] = 1.0 / ldexp(wn_prev, k2_prev);
 }
 
-// Arnoldi: w = scaling * A v_{i-1} into slot i   (psfun_d_arnoldi.f90:202)
-__global__ void __launch_bounds__(kSpmvThreads) k_ar_spmv(KState st, CsrDev A, int i, double scaling) {
-  PSF_SPMV_SMEM();
+// Arnoldi: w = scaling * A v_{i-1} into slot i through the warp-specialised
+// tile pipeline of the persistent kernels (persist.cuh): one block per SM
+// over a contiguous range of tiles, the last warp staging up to four tiles
+// ahead by TMA while fifteen warps form one row per thread.
+__global__ void __launch_bounds__(kSpmvThreads) k_ar_spmv_pipe(KState st, CsrDev A, int i, double scaling,
+                                                               int tiles_per_cta) {
+  extern __shared__ __align__(128) unsigned char lz_smem_raw[];
+  LzSmem& sm = *reinterpret_cast<LzSmem*>(lz_smem_raw);
   KCtrl* c = st.ctrl;
   if (c->done || c->breakdown) return;
-  spmv_smem_init(sm);
+  const int t0 = min(A.ntiles, (int)blockIdx.x * tiles_per_cta);
+  const int t1 = min(A.ntiles, t0 + tiles_per_cta);
+  if (t0 >= t1) return;
+  lz_smem_init(sm);
+  const bool stream = A.stream != 0;
+  PipeCounters pc{0u, 0u};
+  if (threadIdx.x == kConsumerWarps * 32) {
+    if (!pipe_produce(A, t0, t0 + min(kLzStages, t1 - t0), sm, pc.issued, stream)) atomicOr(&c->err, DEVERR_TIMEOUT);
+  }
   EpiAxpby epi{scaling * st.s[i - 1], 0.0, WAT(st, i)};
-  spmv_tiles(A, WAT(st, i - 1), epi, sm, &c->err);
-  spmv_sched_done(A);
+  pipe_spmv(A, WAT(st, i - 1), t0, t1, sm, epi, &c->err, pc, false, stream);
 }
 
 // Arnoldi: modified Gram-Schmidt of slot i against slots 1..i-1, one pass over
@@ -525,7 +453,7 @@ __global__ void __launch_bounds__(kMgsThreads) k_ar_mgs(KState st, int i) {
 // per-block partials are reduced through shared memory and the scalars of a
 // sweep are formed by thread 0.  With fuse the block also forms its rows of
 // w = scaling s_{i-1} A W_{i-1} (the SpMV of psfun_d_arnoldi.f90:202, each
-// row's entries summed in order as k_ar_spmv does), which saves that launch
+// row's entries summed in order as the tiled SpMV does), which saves that launch
 // and the write and re-read of w.
 constexpr int kMgsSmThreads = 512;
 constexpr size_t kMgsSmFixed = sizeof(double) * (2 * kMgsSmThreads + 32 + 8);
@@ -1312,8 +1240,6 @@ static int launch_dense(const void* kern, int G, DenseGroup* grp, DenseGroup** g
 static void spmv_kernel_attrs() {
   static bool done = false;
   if (done) return;
-  spmv_smem_attr(k_lz_spmv);
-  spmv_smem_attr(k_ar_spmv);
   cudaFuncSetAttribute(k_lz_persist<LZ_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
   cudaFuncSetAttribute(k_lz_persist<LZ_MON_SHIFTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLzSmemBytes);
   cudaFuncSetAttribute(k_lz_persist<LZ_MON_ESTIMATE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1491,11 +1417,17 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   const int gm = mgs_grid();
   int mgs_chunk = 0;
   const int gms = arnoldi ? mgs_sm_plan(n, &mgs_chunk) : 0;
-  // The Arnoldi SpMV inside the MGS kernel (rows of the block, one thread per
-  // row) when every row is short: a GB300 SM retires two FP64 FMAs per clock,
-  // so spreading the SpMV's FMAs over the MGS kernel's threads of every SM
-  // costs no more than the tiled kernel, without the write and re-read of w.
-  const bool fuse_spmv = gms > 0 && !sai && a->max_row <= 64;
+  // The Arnoldi SpMV: for fewer than 2^19 rows with short rows (<= 64
+  // entries) inside the Gram-Schmidt kernel (the block's rows, one thread per
+  // row; a small problem saves the launch and the write and re-read of w);
+  // otherwise the pipelined kernel (k_ar_spmv_pipe), whose TMA stages keep
+  // about 150 KB of matrix in flight per SM where the fused rows' dependent
+  // loads keep a few KB (2048^2 convection-diffusion, per step: 72 against
+  // 133 us).
+  const bool fuse_spmv = gms > 0 && !sai && a->max_row <= 64 && n < ((int64_t)1 << 19);
+  static const int ar_pipe_max = persist_grid_for(k_ar_spmv_pipe);
+  const int ar_pipe_tpc = std::max(1, (a->ntiles + ar_pipe_max - 1) / ar_pipe_max);
+  const int ar_pipe_grid = std::max(1, (a->ntiles + ar_pipe_tpc - 1) / ar_pipe_tpc);
   const int tridiag = arnoldi ? 0 : 1;
   const size_t small_doubles = meth->small.bytes / sizeof(double);
 
@@ -1530,7 +1462,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
         }
       } else if (!fuse_spmv) {
         prof_begin(PROF_AR_SPMV, s);
-        k_ar_spmv<<<gs, kSpmvThreads, kSpmvSmemBytes, s>>>(st, A, i, scaling);
+        k_ar_spmv_pipe<<<ar_pipe_grid, kSpmvThreads, kLzSmemBytes, s>>>(st, A, i, scaling, ar_pipe_tpc);
         prof_end(PROF_AR_SPMV, s);
       }
       prof_begin(PROF_AR_MGS, s);

@@ -6,13 +6,15 @@
 //
 // Schedule: the rows are cut on the host into tiles of at most kTileRows rows
 // and kTileNnz stored entries (a row longer than kTileNnz is a tile of its
-// own).  A persistent grid walks the tiles.  For a regular tile one thread
-// issues two TMA bulk copies (cp.async.bulk) that stage the tile's values and
-// column indices into shared memory behind an mbarrier; then each thread owns
-// one row and reads its entries from shared memory, gathering x through the
+// own).  For a regular tile one thread issues TMA bulk copies
+// (cp.async.bulk) that stage the tile's values, column indices and row
+// pointers into shared memory behind an mbarrier; then each thread owns one
+// row and reads its entries from shared memory, gathering x through the
 // read-only path.  Values and indices are therefore read from HBM exactly once,
 // in 16-byte-aligned bulk transfers, whatever the row lengths.  Long rows are
-// reduced cooperatively by the whole block straight from global memory.
+// reduced cooperatively straight from global memory.  The tile pipeline that
+// drives this (a producer warp staging four tiles ahead of fifteen consumer
+// warps) is in persist.cuh; the batched launch stages its tiles itself.
 #pragma once
 
 #include "common.cuh"
@@ -58,7 +60,7 @@ struct __align__(128) SpmvSmem {
   double red[kSpmvThreads / 32];
 };
 
-// Dynamic shared memory of a kernel that runs spmv_tiles (51 KB: above the
+// Dynamic shared memory of a kernel that stages tiles into SpmvSmem (51 KB: above the
 // 48 KB static limit, so kernels declare it with PSF_SPMV_SMEM and launch
 // with kSpmvSmemBytes after psf::spmv_smem_attr()).
 constexpr size_t kSpmvSmemBytes = sizeof(SpmvSmem);
@@ -71,7 +73,7 @@ inline void spmv_smem_attr(K kernel) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpmvSmemBytes);
 }
 
-// Once per kernel, before the first spmv_tiles call.
+// Once per kernel, before its first tile is staged.
 PSF_DEVINL void spmv_smem_init(SpmvSmem& sm, unsigned empty_count = 1) {
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -180,77 +182,6 @@ PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const
     }
   }
   return s;
-}
-
-// Walks tiles handed out by a device work counter (A.sched[0]) and calls
-// epi(row, sum) once per row, by exactly one thread.  Two tile buffers: the
-// next tile is staged by TMA while the current one is computed.  The caller
-// must end the kernel with spmv_sched_done().  Returns false if a bounded
-// wait timed out (*err is set).
-template <class Epi>
-PSF_DEVINL bool spmv_tiles(const CsrDev& A, const double* __restrict__ x, Epi& epi, SpmvSmem& sm, int* err) {
-  if (threadIdx.x == 0) sm.next_tile = (int)atomicAdd(&A.sched[0], 1u);
-  __syncthreads();
-  int t = sm.next_tile;
-  __syncthreads();  // everyone has read next_tile before thread 0 overwrites it
-  int b = 0;
-  bool staged = false;  // buffer b holds tile t
-  if (t < A.ntiles && threadIdx.x == 0) {
-    const TileInfo ti = tile_info(A, t);
-    if (ti.k1 - ti.k0 <= kTileNnz) spmv_issue(A, ti, sm, b);
-  }
-  while (t < A.ntiles) {
-    const TileInfo ti = tile_info(A, t);
-    const bool long_row = (ti.k1 - ti.k0) > kTileNnz;
-    staged = !long_row;
-    // claim and stage the next tile into the other buffer
-    if (threadIdx.x == 0) {
-      const int tn = (int)atomicAdd(&A.sched[0], 1u);
-      sm.next_tile = tn;
-      if (tn < A.ntiles) {
-        const TileInfo tj = tile_info(A, tn);
-        if (tj.k1 - tj.k0 <= kTileNnz) spmv_issue(A, tj, sm, b ^ 1);
-      }
-    }
-    if (long_row) {
-      // one long row: block-cooperative dot product from global memory
-      double s = 0.0;
-      for (int k = ti.k0 + threadIdx.x; k < ti.k1; k += blockDim.x) s = fma(A.val[k], __ldg(x + A.ja[k]), s);
-      s = block_sum(s, sm.red);
-      if (threadIdx.x == 0) epi(ti.r0, s);
-    } else {
-      const bool ok = mbar_wait(&sm.bar[b], sm.phase[b]);
-      if (__syncthreads_or(!ok)) {  // block-uniform decision
-        if (threadIdx.x == 0) atomicOr(err, DEVERR_TIMEOUT);
-        mbar_wait(&sm.bar[b], sm.phase[b]);
-        mbar_wait(&sm.bar[b ^ 1], sm.phase[b ^ 1]);
-        return false;
-      }
-      const SpmvTile& tb = sm.buf[b];
-      const int nr = ti.r1 - ti.r0;
-      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) epi(ti.r0 + lr, spmv_row(tb, ti, lr, x));
-    }
-    if (staged && threadIdx.x == 0) sm.phase[b] ^= 1u;
-    __syncthreads();  // buffer b is free again; next_tile visible
-    t = sm.next_tile;
-    b ^= 1;
-  }
-  return true;
-}
-
-// Every block calls this once at the end of a kernel that used spmv_tiles:
-// the last block to finish resets the work counter for the next launch.
-PSF_DEVINL void spmv_sched_done(const CsrDev& A) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(&A.sched[1], 1u);
-    if (prev == gridDim.x - 1) {
-      A.sched[0] = 0u;
-      A.sched[1] = 0u;
-      __threadfence();
-    }
-  }
 }
 
 // y = alpha*A*x + beta*y (psb_spmm); alpha may come from device memory.
