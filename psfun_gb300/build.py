@@ -70,7 +70,7 @@ def build(verbose: bool = False) -> Path:
         objs = list(ex.map(lambda s: _compile(s, verbose, fresh), SOURCES))
     if not fresh and LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
         return LIB
-    cmd = [nvcc(), "-shared", "-o", str(LIB)] + [str(o) for o in objs] + GENCODE + ["-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", str(LIB)] + [str(o) for o in objs] + GENCODE + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -240,7 +241,26 @@ int psfun_gpu_profile_read(int kernel, long long* launches, double* total_ms) {
   return PSFUN_SUCCESS;
 }
 
+}  // extern "C"
+
 // ---- CSR ------------------------------------------------------------------
+// f(begin, end) over [0, n) in contiguous parts on up to 16 host threads
+// (one part below 2^17 items).
+template <class F>
+static void host_parallel_for(int64_t n, F f) {
+  const int T = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  if (n < ((int64_t)1 << 17) || T == 1) {
+    f((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(T);
+  for (int t = 0; t < T; ++t) th.emplace_back([&, t] { f(n * t / T, n * (t + 1) / T); });
+  for (auto& x : th) x.join();
+}
+
+extern "C" {
+
 int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32_t* ja, const double* val,
                          int index_base, psfun_csr** out) {
   if (!out) return PSFUN_ERR_INVALID_ARGS_COMBINATION;
@@ -259,25 +279,37 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
   if (n == 0) {
     hirp[0] = 0;
   } else {
-    for (int64_t i = 0; i <= n; ++i) hirp[i] = irp[i] - index_base;
+    host_parallel_for(n + 1, [&](int64_t b, int64_t e) {
+      for (int64_t i = b; i < e; ++i) hirp[i] = irp[i] - index_base;
+    });
     if (hirp[0] != 0 || hirp[n] != nnz) {
       set_last_error("rowptr must start at the index base and end at nnz");
       return PSFUN_ERR_INVALID_MATRIX;
     }
-    for (int64_t i = 0; i < n; ++i)
-      if (hirp[i + 1] < hirp[i]) {
-        set_last_error("rowptr not monotone");
-        return PSFUN_ERR_INVALID_MATRIX;
-      }
+    std::atomic<int> bad{0};
+    host_parallel_for(n, [&](int64_t b, int64_t e) {
+      for (int64_t i = b; i < e; ++i)
+        if (hirp[i + 1] < hirp[i]) { bad.store(1); return; }
+    });
+    if (bad.load()) {
+      set_last_error("rowptr not monotone");
+      return PSFUN_ERR_INVALID_MATRIX;
+    }
   }
   std::vector<int32_t> hja(nnz);
-  for (int64_t k = 0; k < nnz; ++k) {
-    const int32_t c = ja[k] - index_base;
-    if (c < 0 || c >= n) {
+  {
+    std::atomic<int> bad{0};
+    host_parallel_for(nnz, [&](int64_t b, int64_t e) {
+      for (int64_t k = b; k < e; ++k) {
+        const int32_t c = ja[k] - index_base;
+        if (c < 0 || c >= n) { bad.store(1); return; }
+        hja[k] = c;
+      }
+    });
+    if (bad.load()) {
       set_last_error("column index out of range");
       return PSFUN_ERR_INVALID_MATRIX;
     }
-    hja[k] = c;
   }
   auto* a = new psfun_csr();
   a->n = n;
@@ -304,19 +336,29 @@ int psfun_gpu_csr_create(int64_t n, int64_t nnz, const int32_t* irp, const int32
     tdesc[t].y = hirp[tiles[t]];
     if (t + 1 < tiles.size()) a->max_tile_rows = std::max<int32_t>(a->max_tile_rows, tiles[t + 1] - tiles[t]);
   }
-  // norms and diagonal
-  double ninf = 0.0;
+  // norms and diagonal (per row; the maxima combined over the parts)
   a->h_diag.assign(n, 0.0);
-  for (int64_t i = 0; i < n; ++i) {
-    double s = 0.0;
-    a->max_row = std::max<int32_t>(a->max_row, hirp[i + 1] - hirp[i]);
-    for (int32_t k = hirp[i]; k < hirp[i + 1]; ++k) {
-      s += fabs(val[k]);
-      if (hja[k] == i) a->h_diag[i] += val[k];
+  std::mutex mx;
+  double ninf = 0.0;
+  int32_t max_row = 0;
+  host_parallel_for(n, [&](int64_t b, int64_t e) {
+    double ninf_p = 0.0;
+    int32_t max_row_p = 0;
+    for (int64_t i = b; i < e; ++i) {
+      double s = 0.0;
+      max_row_p = std::max<int32_t>(max_row_p, hirp[i + 1] - hirp[i]);
+      for (int32_t k = hirp[i]; k < hirp[i + 1]; ++k) {
+        s += fabs(val[k]);
+        if (hja[k] == i) a->h_diag[i] += val[k];
+      }
+      if (s > ninf_p) ninf_p = s;
     }
-    if (s > ninf) ninf = s;
-  }
+    std::lock_guard<std::mutex> lock(mx);
+    ninf = std::max(ninf, ninf_p);
+    max_row = std::max(max_row, max_row_p);
+  });
   a->norm_inf = ninf;
+  a->max_row = max_row;
   cudaStream_t s = stream();
   auto fail = [&](cudaError_t e) {
     (void)cudaGetLastError();

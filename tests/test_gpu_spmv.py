@@ -9,19 +9,29 @@ pytestmark = pytest.mark.gpu
 
 def int_matrix(n, density, seed, long_rows=()):
     rng = np.random.default_rng(seed)
-    A = sp.random(n, n, density=density, random_state=seed, format="lil")
+    if n <= 2000:
+        A = sp.random(n, n, density=density, random_state=seed, format="coo")
+        rows, cols = [A.row.astype(np.int64)], [A.col.astype(np.int64)]
+    else:  # coordinates drawn directly (duplicates merge)
+        k = int(density * n * n)
+        rows, cols = [rng.integers(0, n, size=k)], [rng.integers(0, n, size=k)]
     for r in long_rows:
-        cols = rng.choice(n, size=min(n, 5000), replace=False)
-        A[r, cols] = 1.0
-    A = A.tocsr()
+        c = rng.choice(n, size=min(n, 5000), replace=False)
+        rows.append(np.full(len(c), r, dtype=np.int64))
+        cols.append(c.astype(np.int64))
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    A = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(n, n))
     A.data = rng.integers(-3, 4, size=A.nnz).astype(np.float64)
     A.eliminate_zeros()
     A.sort_indices()
     return A
 
 
+# 600,000 rows: about 1,250 tiles, several per block of the pipeline (the
+# producer's four stages wrap around), with long rows among them
 @pytest.mark.parametrize("n,density,long_rows", [(1, 1.0, ()), (37, 0.2, ()), (5000, 0.002, ()),
-                                                  (20000, 0.0004, (3, 19999)), (6000, 0.0, ())])
+                                                  (20000, 0.0004, (3, 19999)), (6000, 0.0, ()),
+                                                  (600000, 8e-6, (0, 123457, 599999))])
 def test_spmv_bit_exact(lib, n, density, long_rows):
     import psfun_gb300 as pg
     A = int_matrix(n, density, n, long_rows)
