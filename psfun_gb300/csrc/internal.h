@@ -83,6 +83,7 @@ struct KCtrl {
   int bd_step;    // step at which a Lanczos breakdown was found (0: none)
   int conv_first; // concurrent estimates: the first converged iteration (INT_MAX: none)
   int est_last;   // concurrent estimates: the last iteration estimated
+  int steps_end;  // persistent Arnoldi: 1 + the last step published, once the steps have ended (0: running)
   alignas(128) double beta0;  // rs(1) = ||x||
   double errnum;
   double errden;

@@ -73,7 +73,7 @@ __global__ void k_reset(KState st, size_t small_doubles) {
     KCtrl* c = st.ctrl;
     c->done = c->conv = c->breakdown = c->itx = c->yk_len = c->nterms = c->err = c->info = 0;
     c->bar_count = c->bar_gen = c->red_counter = c->red_counter2 = 0u;
-    c->pub = c->stop_req = c->stop_dec = c->bd_step = c->est_last = 0;
+    c->pub = c->stop_req = c->stop_dec = c->bd_step = c->est_last = c->steps_end = 0;
     c->conv_first = 0x7fffffff;
     c->beta0 = c->errnum = c->c1 = c->c2 = c->derr = 0.0;
     c->errden = 1.0;
@@ -528,21 +528,23 @@ PSF_DEVINL void mgs_pair_sweep(double* __restrict__ wl, int nloc, int bd, double
     row(l, vk[l], TWO ? vk1[l] : 0.0, (NEXT >= 1) ? vn1[l] : 0.0, (NEXT == 2) ? vn2[l] : 0.0);
 }
 
-__global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base,
-                                                               CsrDev A, double scaling, int fuse) {
-  extern __shared__ __align__(16) double mgs_sm[];
+// One Arnoldi step i on the G blocks [0, G) of the launch (the body of
+// k_ar_mgs_sm and of each step of k_ar_persist); nb counts the grid barriers.
+// Returns 0 when the step ran, 1 when the solve had stopped or stops here
+// (every block alike), -1 when a bounded wait gave up.
+PSF_DEVINL int ar_step(KState& st, int i, int chunk, unsigned& nb, const CsrDev& A, double scaling, int fuse, int G,
+                       double* mgs_sm) {
   double* vals = mgs_sm;                // kMgsSmThreads
   double* vals2 = vals + kMgsSmThreads;  // kMgsSmThreads
   double* red = vals2 + kMgsSmThreads;   // 32
   double* scal = red + 32;              // 8
   double* wl = scal + 8;                // chunk
   KCtrl* c = st.ctrl;
-  if (c->done) return;
+  if (c->done) return 1;
   if (c->breakdown) {  // the previous step found h(i-1,i-2) == 0 (istop = 2)
     if (blockIdx.x == 0 && threadIdx.x == 0) c->done = 1;
-    return;
+    return 1;
   }
-  const int G = gridDim.x;
   const int b = blockIdx.x;
   const int bd = blockDim.x;
   const int nv = i - 1;  // basis vectors to orthogonalise against
@@ -550,7 +552,6 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
   const int nloc = (int)max((int64_t)0, min(r0 + chunk, st.n) - r0);
   double* __restrict__ w = WAT(st, i) + r0;
   double* part = st.partials;  // two buffers of 2 G partials
-  unsigned nb = bar_base;
   {  // the rows of w (loaded, or with fuse formed here); dots with v_1, v_2
     const double* __restrict__ v1 = WAT(st, 1) + r0;
     const double* __restrict__ v2 = WAT(st, nv >= 2 ? 2 : 1) + r0;
@@ -624,10 +625,10 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
   // and return before their first barrier, so no launch waits on a barrier
   // count that a stopped one did not reach.
   if (b == 0 && threadIdx.x == 0) c->stop_dec = *(volatile int*)&c->stop_req;
-  if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
+  if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return -1;
   if (*(volatile int*)&c->stop_dec) {
     if (b == 0 && threadIdx.x == 0) c->done = 1;
-    return;
+    return 1;
   }
   int buf = 0;
   for (int k = 1; k <= nv; k += 2) {
@@ -666,7 +667,7 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
     buf ^= 1;
     double* pout = part + (size_t)buf * 2 * G;
     block_sum2_store_512(acc1, acc2, vals, vals2, red, &pout[b], (next == 2) ? &pout[G + b] : nullptr);
-    if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return;
+    if (!grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) return -1;
   }
   for (int l = threadIdx.x; l < nloc; l += bd) w[l] = wl[l];
   const double tot = partials_sum_to0(part + (size_t)buf * 2 * G, G, red);
@@ -677,6 +678,48 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, i
     c->itx = i - 1;
     if (beta == 0.0) c->breakdown = 1;
     if (st.host_flag) st.host_flag[1] = i;
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(kMgsSmThreads) k_ar_mgs_sm(KState st, int i, int chunk, unsigned bar_base,
+                                                               CsrDev A, double scaling, int fuse) {
+  extern __shared__ __align__(16) double mgs_sm[];
+  unsigned nb = bar_base;
+  ar_step(st, i, chunk, nb, A, scaling, fuse, gridDim.x, mgs_sm);
+}
+
+// Arnoldi with istop = 1 on a small problem: every step in one cooperative
+// launch (ar_step with the fused SpMV on the first blocks, and one more grid
+// barrier per step so that the next step's SpMV reads the finished W_i and
+// s_i), the a posteriori estimates on the last kEstMonitors blocks as in the
+// Lanczos launch (est_monitor_cta).  Block 0 publishes step i as pub = i - 1
+// (the estimate of iteration i needs H(1:i, 1:i-1)) and, when the steps end,
+// steps_end = 1 + the last step published, so that no monitor waits for a
+// step that will not come.
+__global__ void __launch_bounds__(kMgsSmThreads) k_ar_persist(KState st, int chunk, CsrDev A, double scaling, int nl,
+                                                                LzMonitor mon) {
+  extern __shared__ __align__(16) double mgs_sm[];
+  KCtrl* c = st.ctrl;
+  const int G = gridDim.x - kEstMonitors, b = blockIdx.x;
+  if (b >= G) {
+    est_monitor_cta(st, mon, 1, nl + 1, b - G);
+    return;
+  }
+  unsigned nb = 0;
+  int last = 0;
+  for (int i = 2; i <= nl; ++i) {
+    if (ar_step(st, i, chunk, nb, A, scaling, 1, G, mgs_sm) != 0) break;
+    if (b == 0 && threadIdx.x == 0) {
+      __threadfence();
+      *(volatile int*)&c->pub = i - 1;
+    }
+    last = i - 1;
+    if (i < nl && !grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) break;
+  }
+  if (b == 0 && threadIdx.x == 0) {
+    __threadfence();
+    *(volatile int*)&c->steps_end = last + 1;
   }
 }
 
@@ -791,8 +834,8 @@ __device__ int monitor_wait_pub(KCtrl* c, int want) {
 // For the estimate monitors, which take the iterations in turn: as
 // monitor_wait_pub, but returns -2 (without an error) once step `want` will
 // not be published because the steps stop before it: an estimate of an
-// earlier iteration converged or failed, or a breakdown ended the steps
-// before `want`.
+// earlier iteration converged or failed, a breakdown ended the steps
+// before `want`, or the steps ended (steps_end) before publishing it.
 __device__ int monitor_wait_pub_or_end(KCtrl* c, int want) {
   const unsigned long long t0 = globaltimer_ns();
   int p;
@@ -801,6 +844,8 @@ __device__ int monitor_wait_pub_or_end(KCtrl* c, int want) {
     if (*(volatile int*)&c->conv_first <= want || *(volatile int*)&c->info != 0) return -2;
     const int bd = *(volatile int*)&c->bd_step;
     if (bd != 0 && bd < want) return -2;
+    const int se = *(volatile int*)&c->steps_end;
+    if (se != 0 && want > se - 1) return -2;
     if (globaltimer_ns() - t0 > kWaitLimitNs) {
       atomicOr(&c->err, DEVERR_TIMEOUT);
       return -1;
@@ -1515,13 +1560,30 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   const int m_mon = nl + 1 + (fpk.fname == FN_PHI ? fpk.phiorder + 1 : 0);
   const bool lz_mon = istop == 1 && !arnoldi && !sai && !userf &&
                       (dense_blocks(fpk, nl + 1, true) == 1 || (long)((m_mon + 3) / 4) * m_mon <= kDenseThreads);
+  // istop = 1 Arnoldi on a small problem (the SpMV fused into the step
+  // kernel, Krylov dimension <= 64): every step in one launch with the
+  // estimates on its monitor blocks (k_ar_persist), when the step blocks and
+  // the monitors fit on the GPU at once
+  bool ar_mon = false;
+  const size_t ar_smem = kMgsSmFixed + sizeof(double) * (size_t)mgs_chunk;
+  if (istop == 1 && arnoldi && !sai && !userf && fuse_spmv && nl <= 64) {
+    static size_t attr = 0;
+    if (attr < ar_smem &&
+        cudaFuncSetAttribute(k_ar_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ar_smem) == cudaSuccess)
+      attr = ar_smem;
+    int per = 0;
+    if (attr >= ar_smem &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ar_persist, kMgsSmThreads, ar_smem) == cudaSuccess)
+      ar_mon = per * sm_count() >= gms + kEstMonitors;
+    (void)cudaGetLastError();
+  }
   // the monitors' words: yk per iteration, error numerator and denominator
   // per iteration, a dense scratch per monitor (allocated here, before any
   // capture; 256-byte aligned regions for the complex variants' 16-byte pairs)
   double* lz_yk_all = nullptr;
   double* lz_scr = nullptr;
   int64_t lz_scr_stride = 0;
-  if (lz_mon) {
+  if (lz_mon || ar_mon) {
     auto al32 = [](size_t d) { return (d + 31) & ~(size_t)31; };
     const size_t ldy = (size_t)nl + 1;
     lz_scr_stride = (int64_t)al32(fh_scratch_doubles(nl + 1, fp.phiorder) + 64);
@@ -1549,7 +1611,27 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
     PSF_CUDA(cudaGetLastError());
     return PSFUN_SUCCESS;
   };
-  if ((istop == 2 || lz_mon) && !userf && !prof_enabled() && !sai) {
+  auto launch_ar_estimating = [&]() -> int {
+    LzMonitor mon;
+    memset(&mon, 0, sizeof mon);
+    mon.fp = fpk;
+    mon.eps = eps;
+    mon.tridiag = 0;
+    mon.yk_all = lz_yk_all;
+    mon.ldy = nl + 1;
+    mon.scr = lz_scr;
+    mon.scr_stride = lz_scr_stride;
+    int chunk = mgs_chunk, nl_ = nl;
+    double sc = scaling;
+    void* args[] = {(void*)&st, (void*)&chunk, (void*)&A, (void*)&sc, (void*)&nl_, (void*)&mon};
+    PSF_CUDA(cudaLaunchCooperativeKernel((void*)k_ar_persist, dim3(gms + kEstMonitors), dim3(kMgsSmThreads), args,
+                                         ar_smem, s));
+    k_par_select<<<1, kDenseThreads, 0, s>>>(st, lz_yk_all, nl + 1, -1);
+    count_launch(2);
+    PSF_CUDA(cudaGetLastError());
+    return PSFUN_SUCCESS;
+  };
+  if ((istop == 2 || lz_mon || ar_mon) && !userf && !prof_enabled() && !sai) {
     // fixed-length solve: one CUDA graph, captured once per launch key
     // the device arrays of the matrix are part of the key: a handle can be
     // destroyed and another created at the same address
@@ -1560,7 +1642,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       int istop; double eps;
     } key;
     memset(&key, 0, sizeof key);
-    key.istop = istop; key.eps = eps; key.par = lz_mon ? meth->par.ptr : nullptr;
+    key.istop = istop; key.eps = eps; key.par = (lz_mon || ar_mon) ? meth->par.ptr : nullptr;
     key.irp = A.irp; key.ja = A.ja; key.val = A.val; key.tiles = A.tile_desc;
     key.a = a; key.x = x; key.y = y; key.V = st.V; key.n = n; key.nl = nl; key.arnoldi = arnoldi;
     key.keeplast = meth->keeplast; key.gs = gs; key.gv = gv; key.gm = gm; key.fp = fpk; key.scaling = scaling;
@@ -1574,6 +1656,8 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
       int rc = enqueue_prologue(false);
       if (!arnoldi) {
         if (rc == PSFUN_SUCCESS) rc = lz_mon ? launch_lz_estimating() : launch_lz_persist(st, A, 1, nl + 1, s);
+      } else if (ar_mon) {
+        if (rc == PSFUN_SUCCESS) rc = launch_ar_estimating();
       } else {
         for (int i = 2; i <= nl && rc == PSFUN_SUCCESS; ++i) rc = enqueue_step(i);
       }
