@@ -59,7 +59,7 @@ struct BaArgs {
   double eps;
   FunParams fp;
   const int* blk_unit;  // unit of every block of the step kernel
-  double* part;         // 2 x gridDim.x partial sums
+  double* part;         // 4 x gridDim.x partial sums
   unsigned* bar;        // grid barrier counter, zeroed before every step
   int* err;
   int* step;            // the current step i
@@ -116,10 +116,13 @@ __global__ void __launch_bounds__(kBaThreads) k_ba_init(BaArgs B) {
   }
 }
 
-// Step i of every live unit: W_i = t s_{i-1} A W_{i-1}, then modified
-// Gram-Schmidt against W_1..W_{i-1} with one sweep per basis vector (the
-// update with v_k fused with the dot of v_{k+1}, the last update with the
-// norm), then h(i,i-1) and s_i.  Units that have stopped only keep the
+// Step i of every live unit: W_i = t s_{i-1} A W_{i-1} with the dots of
+// its rows with W_1 and W_2 formed as they are computed, then Gram-Schmidt
+// against W_1..W_{i-1} taking the basis vectors two at a time as the plain
+// Arnoldi kernel does (one sweep subtracts h(k) v_k and h(k+1) v_{k+1} and
+// forms the dots with v_{k+2} and v_{k+3}, or the norm; h(k+1) is taken from
+// w before the v_k update), then h(i,i-1) and s_i.  One grid barrier per
+// pair of vectors serves all units.  Units that have stopped only keep the
 // barriers.
 __global__ void __launch_bounds__(kBaThreads) k_ba_step(BaArgs B) {
   __shared__ double red[32];
@@ -132,61 +135,81 @@ __global__ void __launch_bounds__(kBaThreads) k_ba_step(BaArgs B) {
   int64_t r0, r1;
   ba_rows(U, b, &r0, &r1);
   const int ldh = B.ldh;
+  const int nv = i - 1;
   double* w = BW(U, i);
   unsigned nb = 0;
   auto gsync = [&]() { return grid_sync_to(B.bar, (++nb) * (unsigned)G, B.err); };
-  if (live) {  // SpMV of the unit's rows
-    const double f = U.t * U.s[i - 1];
-    const double* wp = BW(U, i - 1);
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-      double acc = 0.0;
-      for (int k = U.A.irp[r], ke = U.A.irp[r + 1]; k < ke; ++k) acc = fma(U.A.val[k], __ldg(wp + U.A.ja[k]), acc);
-      w[r] = f * acc;
-    }
-  }
-  if (!gsync()) return;
-  {  // dot with W_1
-    double acc = 0.0;
-    if (live) {
-      const double* w1 = BW(U, 1);
-      for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) acc = fma(w1[r], w[r], acc);
-    }
-    acc = block_sum(acc, red);
-    if (threadIdx.x == 0) B.part[b] = acc;
-  }
-  if (!gsync()) return;
-  for (int k = 1; k <= i - 1; ++k) {
-    const double tot = ba_unit_sum(B.part + (size_t)((k - 1) & 1) * G, U, red);
+  // partials: two buffers of two values per block (value q of buffer p at
+  // part[(2 p + q) G + b])
+  auto put2 = [&](int p, double a1, double a2, bool two) {
+    a1 = block_sum(a1, red);
+    if (two) a2 = block_sum(a2, red);
     if (threadIdx.x == 0) {
-      const double h = U.s[k] * tot;  // h(k,i-1) = v_k . w
-      if (live && b == U.b0) BH(U, ldh, k, i - 1) = h;
-      sc[0] = h * U.s[k];
+      B.part[(size_t)(2 * p) * G + b] = a1;
+      if (two) B.part[(size_t)(2 * p + 1) * G + b] = a2;
+    }
+  };
+  {  // SpMV of the unit's rows, with the dots of w with W_1 and W_2
+    double acc1 = 0.0, acc2 = 0.0;
+    if (live) {
+      const double f = U.t * U.s[i - 1];
+      const double* wp = BW(U, i - 1);
+      const double* w1 = BW(U, 1);
+      const double* w2 = BW(U, nv >= 2 ? 2 : 1);
+      for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        double acc = 0.0;
+        for (int k = U.A.irp[r], ke = U.A.irp[r + 1]; k < ke; ++k) acc = fma(U.A.val[k], __ldg(wp + U.A.ja[k]), acc);
+        const double v = f * acc;
+        w[r] = v;
+        acc1 = fma(w1[r], v, acc1);
+        if (nv >= 2) acc2 = fma(w2[r], v, acc2);
+      }
+    }
+    put2(0, acc1, acc2, nv >= 2);
+  }
+  if (!gsync()) return;
+  int buf = 0;
+  for (int k = 1; k <= nv; k += 2) {
+    const bool two = k + 1 <= nv;
+    const int kn = k + 2;
+    const int next = (kn > nv) ? 0 : ((kn + 1 <= nv) ? 2 : 1);
+    const double t1 = ba_unit_sum(B.part + (size_t)(2 * buf) * G, U, red);
+    const double t2 = two ? ba_unit_sum(B.part + (size_t)(2 * buf + 1) * G, U, red) : 0.0;
+    if (threadIdx.x == 0) {
+      const double h1 = U.s[k] * t1;  // h(k,i-1) = v_k . w
+      if (live && b == U.b0) BH(U, ldh, k, i - 1) = h1;
+      sc[0] = h1 * U.s[k];
+      if (two) {
+        const double h2 = U.s[k + 1] * t2;
+        if (live && b == U.b0) BH(U, ldh, k + 1, i - 1) = h2;
+        sc[1] = h2 * U.s[k + 1];
+      }
     }
     __syncthreads();
-    const double c = sc[0];
-    double acc = 0.0;
+    const double c1 = sc[0], c2 = two ? sc[1] : 0.0;
+    double acc1 = 0.0, acc2 = 0.0;
     if (live) {
       const double* wk = BW(U, k);
-      if (k + 1 <= i - 1) {
-        const double* wn = BW(U, k + 1);
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-          const double v = fma(-c, wk[r], w[r]);
-          w[r] = v;
-          acc = fma(wn[r], v, acc);
-        }
-      } else {
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-          const double v = fma(-c, wk[r], w[r]);
-          w[r] = v;
-          acc = fma(v, v, acc);
+      const double* wk1 = BW(U, two ? k + 1 : k);
+      const double* wn1 = BW(U, next >= 1 ? kn : k);
+      const double* wn2 = BW(U, next == 2 ? kn + 1 : k);
+      for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        double v = fma(-c1, wk[r], w[r]);
+        if (two) v = fma(-c2, wk1[r], v);
+        w[r] = v;
+        if (next == 0) {
+          acc1 = fma(v, v, acc1);
+        } else {
+          acc1 = fma(wn1[r], v, acc1);
+          if (next == 2) acc2 = fma(wn2[r], v, acc2);
         }
       }
     }
-    acc = block_sum(acc, red);
-    if (threadIdx.x == 0) B.part[(size_t)(k & 1) * G + b] = acc;
+    buf ^= 1;
+    put2(buf, acc1, acc2, next == 2);
     if (!gsync()) return;
   }
-  const double tot = ba_unit_sum(B.part + (size_t)((i - 1) & 1) * G, U, red);
+  const double tot = ba_unit_sum(B.part + (size_t)(2 * buf) * G, U, red);
   if (live && b == U.b0 && threadIdx.x == 0) {
     const double beta = sqrt(tot);
     BH(U, ldh, i, i - 1) = beta;
@@ -380,7 +403,7 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
     uo[u].scr = carve(fsz);
   }
   const size_t oUnits = carve((sizeof(BaUnit) * nu + 7) / 8);
-  const size_t oPart = carve(2 * (size_t)gmax + 8);
+  const size_t oPart = carve(4 * (size_t)gmax + 8);
   const size_t oMap = carve(((size_t)gmax + 1) / 2 + 1);
   const size_t oE1 = carve(nl + 2);
   const size_t oMisc = carve(8);
