@@ -130,20 +130,25 @@ PSF_DEVINL void cram_pole_tridiag(int m, double t, const double* alpha, const do
     const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
                      (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
     U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+    b[k] = zmk(inv, 0.0);  // the pivot's reciprocal, reused by the back substitution
     a0 = zsub(q1, zmul(l, a1));
     a1 = zsub(q2, zmul(l, a2));
     a2 = zmk(0.0, 0.0);
     bk = zsub(qb, zmul(l, bk));
     q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
   }
-  if (cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) { *bad = 1; return; }
+  {
+    const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+    if (na == 0.0) { *bad = 1; return; }
+    b[m - 1] = zmk(1.0 / na, 0.0);
+  }
   U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
   zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);  // solution at i+1, i+2
   zc u0 = U[4 * (m - 1)], u1 = U[4 * (m - 1) + 1], u2 = U[4 * (m - 1) + 2], ub = U[4 * (m - 1) + 3];
   for (int i = m - 1; i >= 0; --i) {
     const zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
     if (i > 0) { u0 = U[4 * (i - 1)]; u1 = U[4 * (i - 1) + 1]; u2 = U[4 * (i - 1) + 2]; ub = U[4 * (i - 1) + 3]; }
-    const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+    const double inv = cuCreal(b[i]);
     zc sv = zsub(vb, zmul(v1, x1));
     sv = zsub(sv, zmul(v2, x2));
     const zc xi = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
@@ -483,19 +488,24 @@ PSF_DEVINL void final_quad(const BInst& I, const BatchArgs& B) {
       const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
                        (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
       U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      z[k] = zmk(inv, 0.0);  // the pivot's reciprocal, reused by the back substitution
       a0 = zsub(q1, zmul(l, a1));
       a1 = zsub(q2, zmul(l, a2));
       a2 = zmk(0.0, 0.0);
       bk = zsub(qb, zmul(l, bk));
       q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
     }
-    if (!fail && cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) fail = 1;
+    if (!fail) {
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      if (na == 0.0) fail = 1;
+      else z[m - 1] = zmk(1.0 / na, 0.0);
+    }
     if (fail) { atomicOr(&bad[q], 1); continue; }
     U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
     zc x1 = zmk(0.0, 0.0), x2 = zmk(0.0, 0.0);
     for (int k = m - 1; k >= 0; --k) {
       const zc v0 = U[4 * k], v1 = U[4 * k + 1], v2 = U[4 * k + 2], vb = U[4 * k + 3];
-      const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+      const double inv = cuCreal(z[k]);
       zc sv = zsub(vb, zmul(v1, x1));
       sv = zsub(sv, zmul(v2, x2));
       const zc xk = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,

@@ -1012,6 +1012,7 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
       const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
                        (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
       U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      b[k] = zmk(inv, 0.0);  // the pivot's reciprocal, reused by the back substitution
       a0 = zsub(q1, zmul(l, a1));
       a1 = zsub(q2, zmul(l, a2));
       a2 = zmk(0.0, 0.0);
@@ -1021,6 +1022,7 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
     if (!bad) {
       const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
       if (na == 0.0) bad = 1;
+      else b[m - 1] = zmk(1.0 / na, 0.0);
       U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
     }
     if (!bad) {
@@ -1030,7 +1032,7 @@ PSF_DEVINL bool cta_cram_tridiag(int m, double t, const double* H, int ldh, cons
       for (int i = m - 1; i >= 0; --i) {
         zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
         if (i > 0) { u0 = U[4 * (i - 1)]; u1 = U[4 * (i - 1) + 1]; u2 = U[4 * (i - 1) + 2]; ub = U[4 * (i - 1) + 3]; }
-        const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+        const double inv = cuCreal(b[i]);
         zc sv = zsub(vb, zmul(v1, x1));
         sv = zsub(sv, zmul(v2, x2));
         const zc xi = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,

@@ -1980,6 +1980,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
       const zc l = zmk((cuCreal(q0) * cuCreal(a0) + cuCimag(q0) * cuCimag(a0)) * inv,
                        (cuCimag(q0) * cuCreal(a0) - cuCreal(q0) * cuCimag(a0)) * inv);
       U[4 * k] = a0; U[4 * k + 1] = a1; U[4 * k + 2] = a2; U[4 * k + 3] = bk;
+      b[k] = zmk(inv, 0.0);  // the pivot's reciprocal, reused by the back substitution
       a0 = zsub(q1, zmul(l, a1));
       a1 = zsub(q2, zmul(l, a2));
       a2 = zmk(0.0, 0.0);
@@ -1987,7 +1988,9 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
       q0 = n0; q1 = n1; q2 = n2; qb = zmk(0.0, 0.0);
     }
     if (!bad) {
-      if (cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0) == 0.0) bad = 1;
+      const double na = cuCreal(a0) * cuCreal(a0) + cuCimag(a0) * cuCimag(a0);
+      if (na == 0.0) bad = 1;
+      else b[m - 1] = zmk(1.0 / na, 0.0);
       U[4 * (m - 1)] = a0; U[4 * (m - 1) + 1] = a1; U[4 * (m - 1) + 2] = a2; U[4 * (m - 1) + 3] = bk;
     }
     if (!bad) {
@@ -1996,7 +1999,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_ms_final(KState st, MsParams 
       for (int k = m - 1; k >= 0; --k) {
         const zc v0 = u0, v1 = u1, v2 = u2, vb = ub;
         if (k > 0) { u0 = U[4 * (k - 1)]; u1 = U[4 * (k - 1) + 1]; u2 = U[4 * (k - 1) + 2]; ub = U[4 * (k - 1) + 3]; }
-        const double inv = 1.0 / (cuCreal(v0) * cuCreal(v0) + cuCimag(v0) * cuCimag(v0));
+        const double inv = cuCreal(b[k]);
         zc sv = zsub(vb, zmul(v1, x1));
         sv = zsub(sv, zmul(v2, x2));
         const zc xk = zmk((cuCreal(sv) * cuCreal(v0) + cuCimag(sv) * cuCimag(v0)) * inv,
@@ -2215,28 +2218,43 @@ __global__ void k_adj_solve(KState st, AdjShifts sh, int m, double* sol, double*
       du2[i] = zmk(0.0, 0.0);
       b[i] = zmk(i == 0 ? beta0 : 0.0, 0.0);
     }
+    // Pivots are compared by squared modulus and a complex division is one
+    // reciprocal of |p|^2 and products (the shifts and t T are of moderate
+    // size, far from the range where |p|^2 would over- or underflow): this
+    // is a sequential FP64 chain per shift, whose length is its cost.  The
+    // reciprocal of each final pivot is kept (in the used dl slot) for the
+    // back substitution.
+    auto n2 = [](zc a) { return fma(cuCreal(a), cuCreal(a), cuCimag(a) * cuCimag(a)); };
+    auto is0 = [](zc a) { return ((__double_as_longlong(cuCreal(a)) | __double_as_longlong(cuCimag(a))) << 1) == 0; };
+    auto mulc = [](zc a, zc b, double r) {  // a conj(b) r
+      return zmk(fma(cuCreal(a), cuCreal(b), cuCimag(a) * cuCimag(b)) * r,
+                 fma(cuCimag(a), cuCreal(b), -cuCreal(a) * cuCimag(b)) * r);
+    };
     int fail = 0;
     for (int i = 0; i < m - 1 && !fail; ++i) {
-      if (zabs(d[i]) < zabs(dl[i])) {
+      if (n2(d[i]) < n2(dl[i])) {
         zc tt;
         tt = d[i]; d[i] = dl[i]; dl[i] = tt;
         tt = du[i]; du[i] = d[i + 1]; d[i + 1] = tt;
         if (i + 1 < m - 1) { tt = du2[i]; du2[i] = du[i + 1]; du[i + 1] = tt; }
         tt = b[i]; b[i] = b[i + 1]; b[i + 1] = tt;
       }
-      if (zabs(d[i]) == 0.0) { fail = 1; break; }
-      const zc l = zdiv(dl[i], d[i]);
+      if (is0(d[i])) { fail = 1; break; }
+      const double r = 1.0 / n2(d[i]);
+      const zc l = mulc(dl[i], d[i], r);
+      dl[i] = zmk(r, 0.0);
       d[i + 1] = zsub(d[i + 1], zmul(l, du[i]));
       if (i + 1 < m - 1) du[i + 1] = zsub(du[i + 1], zmul(l, du2[i]));
       b[i + 1] = zsub(b[i + 1], zmul(l, b[i]));
     }
-    if (!fail && zabs(d[m - 1]) == 0.0) fail = 1;
+    if (!fail && is0(d[m - 1])) fail = 1;
     if (fail) { atomicOr(&bad, 1); continue; }
+    dl[m - 1] = zmk(1.0 / n2(d[m - 1]), 0.0);
     for (int i = m - 1; i >= 0; --i) {
       zc sv = b[i];
       if (i + 1 < m) sv = zsub(sv, zmul(du[i], b[i + 1]));
       if (i + 2 < m) sv = zsub(sv, zmul(du2[i], b[i + 2]));
-      b[i] = zdiv(sv, d[i]);
+      b[i] = mulc(sv, d[i], cuCreal(dl[i]));
     }
   }
   __syncthreads();
