@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(kBaThreads) k_ba_estimate(BaArgs B) {
   BaUnit& U = B.u[blockIdx.x];
   if (i > B.nl || U.done) return;
   dense_group_begin(sm, nullptr);
+  dense_use_dynamic_smem(sm);
   if (B.istop != 1) {
     if (i == B.nl && threadIdx.x == 0) U.done = 1;  // the loop ends after iteration nl
     return;
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(kBaThreads) k_ba_final(BaArgs B) {
   __shared__ DenseSmem sm;
   BaUnit& U = B.u[blockIdx.x];
   dense_group_begin(sm, nullptr);
+  dense_use_dynamic_smem(sm);
   if (U.info != 0) return;
   if (U.beta0 == 0.0) {
     if (threadIdx.x == 0) { U.nterms = 0; U.itx = 0; }
@@ -389,6 +391,18 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
     return o;
   };
   const size_t fsz = fh_scratch_doubles(nl + 1, fp.phiorder) + 64;
+  // a unit's dense evaluations keep their Pade work matrices in shared
+  // memory when those of the largest order fit
+  size_t dsmem = 0;
+  if (fh_uses_gemm(fp)) {
+    const size_t M = (size_t)nl + 1 + (fp.fname == FN_PHI ? (size_t)std::max(fp.phiorder, 1) : 0);
+    const size_t want = sizeof(double) * ((fp.fname == FN_PHI ? 6 : 5) * M * M + 64);
+    if (want <= (size_t)200 * 1024 &&
+        cudaFuncSetAttribute(k_ba_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) == cudaSuccess &&
+        cudaFuncSetAttribute(k_ba_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) == cudaSuccess)
+      dsmem = want;
+    (void)cudaGetLastError();
+  }
   struct Off { size_t V, H, s, rs, yk, coef, scr; };
   std::vector<Off> uo(nu);
   for (int u = 0; u < nu; ++u) {
@@ -492,7 +506,7 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
       cudaError_t e = cudaMemsetAsync(B.bar, 0, sizeof(unsigned), s);
       if (e == cudaSuccess)
         e = cudaLaunchCooperativeKernel((void*)k_ba_step, dim3(G), dim3(kBaThreads), args, 0, s);
-      if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_estimate, dim3(nu), dim3(kBaThreads), args, 0, s);
+      if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_estimate, dim3(nu), dim3(kBaThreads), args, dsmem, s);
       if (e == cudaSuccess) e = cudaLaunchKernel((void*)k_ba_next, dim3(1), dim3(256), args, 0, s);
       cudaError_t ec = cudaStreamEndCapture(s, &graph);
       if (e != cudaSuccess) {
@@ -540,7 +554,7 @@ int batch_arnoldi(psfun_krylov* meth, const FunParams& fp_in, int count, const p
     }
     {
       void* args[] = {(void*)&B};
-      PSF_CUDA(cudaLaunchKernel((void*)k_ba_final, dim3(nu), dim3(kBaThreads), args, 0, s));
+      PSF_CUDA(cudaLaunchKernel((void*)k_ba_final, dim3(nu), dim3(kBaThreads), args, dsmem, s));
       PSF_CUDA(cudaLaunchKernel((void*)k_ba_recombine, dim3(G), dim3(kBaThreads), args, 0, s));
       count_launch(2);
     }

@@ -92,6 +92,8 @@ struct DenseSmem {
   double coef[64];
   DenseGroup* grp;  // null: a single block does everything
   unsigned jobs;   // products posted so far (block 0, thread 0)
+  double* sws;     // the block's dynamic shared memory, for a single block's work matrices
+  unsigned sws_cap;  // its size in doubles (0: none)
 };
 
 // ---- real building blocks --------------------------------------------------
@@ -113,7 +115,34 @@ PSF_DEVINL void gemm_tasks(int m, double alpha, const double* A, int lda, const 
     const double* a = A + i;
     const double* b = B + (size_t)j * ldb;
     double c = 0.0;
-    for (int l = 0; l < m; ++l) c = fma(alpha * b[l], a[(size_t)l * lda], c);
+    int l = 0;
+    // eight terms' loads issued ahead of their FMAs (the sum stays in order);
+    // alpha == 1, the common case, costs no multiply (1 * b is exact)
+    if (alpha == 1.0) {
+      for (; l + 8 <= m; l += 8) {
+        double av[8], bv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          av[q] = a[(size_t)(l + q) * lda];
+          bv[q] = b[l + q];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c = fma(bv[q], av[q], c);
+      }
+      for (; l < m; ++l) c = fma(b[l], a[(size_t)l * lda], c);
+    } else {
+      for (; l + 8 <= m; l += 8) {
+        double av[8], bv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          av[q] = a[(size_t)(l + q) * lda];
+          bv[q] = b[l + q];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c = fma(alpha * bv[q], av[q], c);
+      }
+      for (; l < m; ++l) c = fma(alpha * b[l], a[(size_t)l * lda], c);
+    }
     C[i + (size_t)j * ldc] = c;
   }
 }
@@ -179,8 +208,9 @@ PSF_DEVINL void cta_gemm(DenseSmem& sm, int m, double alpha, const double* A, in
 }
 
 // Columns [c0, c1) of B := U^{-1} L^{-1} P B, with the factors that
-// cta_gesv leaves in A (unit L below the diagonal, U on and above it) and its
-// row exchanges piv[k].  The block's threads run over the entries of its
+// cta_lu_solve leaves in A (unit L below the diagonal, U on and above it;
+// the exchange of step k applied to columns k.. only) and its row exchanges
+// piv[k].  The block's threads run over the entries of its
 // columns, one barrier per elimination step: first the exchanges and the
 // forward elimination in the order of the factorisation, then the
 // column-oriented back substitution of the reference BLAS DTRSM (step k
@@ -291,6 +321,25 @@ PSF_DEVINL void dense_group_begin(DenseSmem& sm, DenseGroup* grp) {
   if (threadIdx.x == 0) {
     sm.grp = (gridDim.x > 1) ? grp : nullptr;
     sm.jobs = 0u;
+    sm.sws = nullptr;
+    sm.sws_cap = 0u;
+  }
+  __syncthreads();
+}
+
+// A block that evaluates f(H) alone may keep the work matrices of a small
+// evaluation in its dynamic shared memory (whatever the launch gave it): on
+// one SM every elimination step and product is a chain of dependent loads,
+// FMAs and barriers, and shared memory answers in tens of cycles where L2
+// takes hundreds.  Call after dense_group_begin; a group's helper blocks
+// read block 0's operands from global memory, so a group keeps them there.
+PSF_DEVINL void dense_use_dynamic_smem(DenseSmem& sm) {
+  extern __shared__ __align__(16) double psf_dense_dyn[];
+  if (threadIdx.x == 0 && !sm.grp) {
+    unsigned bytes;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(bytes));
+    sm.sws = psf_dense_dyn;
+    sm.sws_cap = bytes / 8u;
   }
   __syncthreads();
 }
@@ -457,58 +506,169 @@ PSF_DEVINL bool cta_gesv(int m, int nrhs, double* A, int lda, double* B, int ldb
   return true;
 }
 
-// Solve A X = B like cta_gesv (DGESV semantics), for the Pade step: the
-// factorisation of A alone by block 0, with the multipliers of a column
-// formed by one reciprocal of its pivot as LAPACK DGETF2 does, the pivot
-// rows into ws (int) and the reciprocals of U's diagonal into ws + m
-// (2 m doubles in all); then the substitutions (lu_solve_cols) for all the
-// right-hand sides by this block or, with a group, shared over its blocks.
+// Pivot of column c (rows c..m-1) from the values a warp holds, row
+// c + lane + 32 q in v[q]: the first row of largest magnitude (IDAMAX), the
+// magnitudes compared as the bit patterns of |v|, which order finite
+// doubles as their magnitudes (a NaN ranks below every number).  Then the
+// column's exchange and its multipliers, v times the reciprocal of the
+// pivot as LAPACK DGETF2 forms them, stored in col; the pivot row and the
+// reciprocal go to piv[c], rdiag[c] and the step slot sm.iv[2 + (c & 1)]
+// (-1 on an exactly zero pivot).  Lanes of one warp, all 32.
+PSF_DEVINL void lu_pivot_column(int m, int c, double* col, const double (&v)[4], int* piv, double* rdiag,
+                                DenseSmem& sm) {
+  const int lane = threadIdx.x & 31;
+  long long best = -1;
+  int bi = c;
+  double bv = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = c + lane + 32 * q;
+    if (i < m) {
+      long long key = __double_as_longlong(v[q]) & 0x7fffffffffffffffLL;
+      if (key > 0x7ff0000000000000LL) key = -1;
+      if (key > best) { best = key; bi = i; bv = v[q]; }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bv = ov; }
+  }
+  const double acc = __shfl_sync(0xffffffffu, v[0], 0);  // a(c, c) before the exchange
+  if (best == 0) {
+    if (lane == 0) sm.iv[2 + (c & 1)] = -1;
+    return;
+  }
+  if (best < 0) bv = acc;  // a column of NaN: no exchange, the NaN carried on
+  const double rp = __drcp_rn(bv);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = c + lane + 32 * q;
+    if (i < m) col[i] = (i == c) ? bv : ((i == bi) ? acc : v[q]) * rp;
+  }
+  if (lane == 0) {
+    piv[c] = bi;
+    rdiag[c] = rp;
+    sm.iv[2 + (c & 1)] = bi;
+  }
+}
+
+// LU factorisation with partial pivoting of A (m x m, m <= 128): the
+// row exchanges of step k applied to columns k.. only, so that L's columns
+// keep the rows they had when formed and the substitutions interleave the
+// exchanges with the forward elimination (lu_solve_cols).  At step k every
+// warp takes its share of the trailing columns (the exchange and the
+// rank-1 update, its rows in registers); warp 0 takes column k + 1 first and
+// on the values still in its registers finds the next pivot, forms its
+// reciprocal and the next multipliers while the other warps finish the step:
+// one block barrier per step, the pivot slots alternating between steps.
+PSF_DEVINL bool cta_lu_factor_small(int m, double* A, int lda, int* piv, double* rdiag, DenseSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (warp == 0) {
+    double v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = lane + 32 * q;
+      v[q] = (i < m) ? A[i] : 0.0;
+    }
+    lu_pivot_column(m, 0, A, v, piv, rdiag, sm);
+  }
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    const int p = sm.iv[2 + (k & 1)];
+    if (p < 0) { __syncthreads(); return false; }
+    if (k + 1 == m) break;
+    const double* lk = A + (size_t)k * lda;
+    double l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = k + 1 + lane + 32 * q;
+      l[q] = (i < m) ? lk[i] : 0.0;
+    }
+    for (int j = k + 1 + warp; j < m; j += nw) {
+      double* col = A + (size_t)j * lda;
+      const double akj = col[k], apj = col[p];
+      __syncwarp();
+      double v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = k + 1 + lane + 32 * q;
+        if (i < m) {
+          v[q] = fma(-l[q], apj, (i == p) ? akj : col[i]);
+          col[i] = v[q];
+        } else {
+          v[q] = 0.0;
+        }
+      }
+      if (lane == 0) col[k] = apj;
+      if (j == k + 1) {
+        __syncwarp();
+        lu_pivot_column(m, k + 1, col, v, piv, rdiag, sm);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Solve A X = B (DGESV semantics), for the Pade step: the factorisation of
+// A alone by block 0, the multipliers of a column formed by one reciprocal
+// of its pivot as LAPACK DGETF2 does, the pivot rows into ws (int) and the
+// reciprocals of U's diagonal into ws + m (2 m doubles in all); then the
+// substitutions (lu_solve_cols) for all the right-hand sides by this block
+// or, with a group, shared over its blocks.  The row exchanges of step k
+// reach columns k.. of A only (the order lu_solve_cols applies them in).
 // Returns false on an exactly zero pivot.
 PSF_DEVINL bool cta_lu_solve(int m, int nrhs, double* A, int lda, double* B, int ldb, double* ws, DenseSmem& sm) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   int* piv = reinterpret_cast<int*>(ws);
   double* rdiag = ws + m;
   if (m < 1) { __syncthreads(); return true; }
-  // The reciprocal of each pivot is formed by lane 0 of warp 0 as soon as the
-  // pivot is found, while the other warps finish the step's update: an FP64
-  // division is a chain of about ten dependent FP64 instructions.
-  if (threadIdx.x < 32) {
-    warp_pivot(m, 0, A, lda, sm);
-    if (threadIdx.x == 0) sm.dv[3] = 1.0 / sm.dv[1];
-  }
-  __syncthreads();
-  for (int k = 0; k < m; ++k) {
-    const int p = sm.iv[0];
-    const double piv_v = sm.dv[1], akk = sm.dv[2], rp = sm.dv[3];
-    if (sm.iv[1]) { __syncthreads(); return false; }
-    if (threadIdx.x == 0) piv[k] = p;
-    if (p != k) {
-      for (int j = threadIdx.x; j < m; j += blockDim.x) {
-        if (j == k) continue;
-        double* a = A + (size_t)j * lda;
-        const double t = a[k]; a[k] = a[p]; a[p] = t;
-      }
-      if (threadIdx.x == 0) A[k + (size_t)k * lda] = piv_v;
-    }
-    double* lk = A + (size_t)k * lda;
-    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) lk[i] = ((i == p) ? akk : lk[i]) * rp;
-    __syncthreads();
-    for (int j = k + 1 + warp; j < m; j += nw) {
-      double* col = A + (size_t)j * lda;
-      const double akj = col[k];
-      for (int i = k + 1 + lane; i < m; i += 32) col[i] = fma(-lk[i], akj, col[i]);
-      if (j == k + 1) {  // warp 0: the pivot of the next step and its reciprocal
-        __syncwarp();
-        warp_pivot(m, k + 1, A, lda, sm);
-        __syncwarp();
-        if (lane == 0) sm.dv[3] = 1.0 / sm.dv[1];
-      }
+  if (m <= 128) {
+    if (!cta_lu_factor_small(m, A, lda, piv, rdiag, sm)) return false;
+  } else {
+    // The reciprocal of each pivot is formed by lane 0 of warp 0 as soon as
+    // the pivot is found, while the other warps finish the step's update.
+    if (threadIdx.x < 32) {
+      warp_pivot(m, 0, A, lda, sm);
+      if (threadIdx.x == 0) sm.dv[3] = 1.0 / sm.dv[1];
     }
     __syncthreads();
+    for (int k = 0; k < m; ++k) {
+      const int p = sm.iv[0];
+      const double piv_v = sm.dv[1], akk = sm.dv[2], rp = sm.dv[3];
+      if (sm.iv[1]) { __syncthreads(); return false; }
+      if (threadIdx.x == 0) piv[k] = p;
+      if (p != k) {
+        for (int j = k + 1 + threadIdx.x; j < m; j += blockDim.x) {
+          double* a = A + (size_t)j * lda;
+          const double t = a[k]; a[k] = a[p]; a[p] = t;
+        }
+        if (threadIdx.x == 0) A[k + (size_t)k * lda] = piv_v;
+      }
+      double* lk = A + (size_t)k * lda;
+      for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) lk[i] = ((i == p) ? akk : lk[i]) * rp;
+      __syncthreads();
+      for (int j = k + 1 + warp; j < m; j += nw) {
+        double* col = A + (size_t)j * lda;
+        const double akj = col[k];
+        for (int i = k + 1 + lane; i < m; i += 32) col[i] = fma(-lk[i], akj, col[i]);
+        if (j == k + 1) {  // warp 0: the pivot of the next step and its reciprocal
+          __syncwarp();
+          warp_pivot(m, k + 1, A, lda, sm);
+          __syncwarp();
+          if (lane == 0) sm.dv[3] = 1.0 / sm.dv[1];
+        }
+      }
+      __syncthreads();
+    }
+    for (int k = threadIdx.x; k < m; k += blockDim.x) rdiag[k] = 1.0 / A[k + (size_t)k * lda];
+    __syncthreads();
   }
-  for (int k = threadIdx.x; k < m; k += blockDim.x) rdiag[k] = 1.0 / A[k + (size_t)k * lda];
-  __syncthreads();
-  if (!sm.grp || nrhs < 2 * (int)gridDim.x) {
+  if (!sm.grp) {
     lu_solve_cols(m, A, lda, piv, rdiag, B, ldb, 0, nrhs);
     return true;
   }
@@ -1140,6 +1300,12 @@ PSF_DEVINL int fh_apply_cta(const FunParams& fp, int m, const double* H, int ldh
                             double* scratch, bool tridiag, DenseSmem& sm) {
   if (m < 1) return DEVERR_BADSIZE;
   const size_t mm = (size_t)m * m;
+  {  // the Pade variants' work matrices in shared memory when they fit
+    const size_t M = (size_t)m + (fp.fname == FN_PHI ? (size_t)max(fp.phiorder, 1) : 0);
+    const size_t need = (fp.fname == FN_PHI) ? 6 * M * M + 64 : 5 * mm + 64;
+    const bool pade = (fp.fname == FN_EXP && fp.variant == VAR_GENPADE) || fp.fname == FN_PHI;
+    if (pade && !sm.grp && sm.sws && need <= sm.sws_cap) scratch = sm.sws;
+  }
   if (fp.fname == FN_EXP) {
     switch (fp.variant) {
       case VAR_GENPADE: {

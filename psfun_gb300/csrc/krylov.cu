@@ -769,7 +769,8 @@ __device__ void estimate_tail(KState& st, int i, double eps, double* red) {
     return;                                  \
   }                                          \
   __shared__ DenseSmem sm;                   \
-  dense_group_begin(sm, grp)
+  dense_group_begin(sm, grp);                \
+  dense_use_dynamic_smem(sm)
 
 __device__ void estimate_body(KState& st, const FunParams& fp, int i, double eps, int tridiag, DenseSmem& sm,
                               bool breakdown_ends = true) {
@@ -968,6 +969,7 @@ __device__ __noinline__ void est_monitor_cta(KState& st, const LzMonitor& mon, i
   __shared__ int s_pub;
   KCtrl* c = st.ctrl;
   dense_group_begin(dsm, nullptr);
+  dense_use_dynamic_smem(dsm);  // the launch's dynamic shared memory, unused by a monitor block
   KState ste = st;
   ste.fscratch = mon.scr + (size_t)r * mon.scr_stride;
   int pub = i_begin - 1;
@@ -1267,8 +1269,14 @@ static int dense_blocks(const FunParams& fp, int m, bool tridiag) {
   return 1;
 }
 
+// Dynamic shared memory of a single-block dense evaluation (with the
+// kernel's static shared memory within the 48 KB that needs no opt-in): the
+// Pade variants' work matrices up to order 31 (phi's augmented order 29).
+constexpr size_t kDenseDynSmem = 40 * 1024;
+
 // A dense kernel (its last parameter the DenseGroup*, set in args) as a group
-// of G co-resident blocks, or as one block with no group.
+// of G co-resident blocks, or as one block with no group (given shared
+// memory for its work matrices).
 static int launch_dense(const void* kern, int G, DenseGroup* grp, DenseGroup** grp_arg, void** args, cudaStream_t s) {
   if (G > 1) {
     *grp_arg = grp;
@@ -1276,7 +1284,7 @@ static int launch_dense(const void* kern, int G, DenseGroup* grp, DenseGroup** g
     PSF_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(kDenseThreads), args, 0, s));
   } else {
     *grp_arg = nullptr;
-    PSF_CUDA(cudaLaunchKernel(kern, dim3(1), dim3(kDenseThreads), args, 0, s));
+    PSF_CUDA(cudaLaunchKernel(kern, dim3(1), dim3(kDenseThreads), args, kDenseDynSmem, s));
   }
   count_launch();
   return PSFUN_SUCCESS;
@@ -1565,17 +1573,31 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   // estimates on its monitor blocks (k_ar_persist), when the step blocks and
   // the monitors fit on the GPU at once
   bool ar_mon = false;
-  const size_t ar_smem = kMgsSmFixed + sizeof(double) * (size_t)mgs_chunk;
+  size_t ar_smem = kMgsSmFixed + sizeof(double) * (size_t)mgs_chunk;
   if (istop == 1 && arnoldi && !sai && !userf && fuse_spmv && nl <= 64) {
-    static size_t attr = 0;
-    if (attr < ar_smem &&
-        cudaFuncSetAttribute(k_ar_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ar_smem) == cudaSuccess)
-      attr = ar_smem;
-    int per = 0;
-    if (attr >= ar_smem &&
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ar_persist, kMgsSmThreads, ar_smem) == cudaSuccess)
-      ar_mon = per * sm_count() >= gms + kEstMonitors;
-    (void)cudaGetLastError();
+    auto co_resident = [&](size_t bytes) {
+      static size_t attr = 0;
+      if (attr < bytes &&
+          cudaFuncSetAttribute(k_ar_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+        attr = bytes;
+      int per = 0;
+      const bool ok = attr >= bytes &&
+                      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ar_persist, kMgsSmThreads, bytes) ==
+                          cudaSuccess &&
+                      per * sm_count() >= gms + kEstMonitors;
+      (void)cudaGetLastError();
+      return ok;
+    };
+    // room for a monitor's Pade work matrices of the largest order (its
+    // dense evaluations in shared memory), when the blocks still fit at once
+    const size_t M = (size_t)nl + 1 + (fpk.fname == FN_PHI ? (size_t)max(fpk.phiorder, 1) : 0);
+    const size_t mon_smem = sizeof(double) * ((fpk.fname == FN_PHI ? 6 : 5) * M * M + 64);
+    if (fh_uses_gemm(fpk) && mon_smem > ar_smem && mon_smem <= (size_t)200 * 1024 && co_resident(mon_smem)) {
+      ar_smem = mon_smem;
+      ar_mon = true;
+    } else {
+      ar_mon = co_resident(ar_smem);
+    }
   }
   // the monitors' words: yk per iteration, error numerator and denominator
   // per iteration, a dense scratch per monitor (allocated here, before any
