@@ -609,6 +609,53 @@ def run_reference(args):
     return 0
 
 
+def bench_skewed(torch, pg, peak_gbs: float, n: int = 1 << 22, reps: int = 20):
+    """y = A x (psb_spmm) through the device C-ABI call on a matrix with
+    power-law row lengths (alpha 1.5, 4..4000 entries per row, seed 5) and on
+    one of the same n and nnz with equal-length rows, uniformly random
+    columns in both: algorithmic B_spmv = 12 nnz + 4 (n + 1) + 16 n per
+    call over its CUDA-event time (matrix ~0.6 GB, above L2)."""
+    import scipy.sparse as sp
+    from psfun_gb300 import matrices
+    out = {"workload": f"SpMV y = A x, n = {n}, power-law row lengths (alpha 1.5, 4..4000) "
+                       "against equal row lengths, same n and nnz"}
+    As = matrices.skewed_rows(n)
+    nnz = As.nnz
+    rng = np.random.default_rng(6)
+    k = nnz // n
+    lens = np.full(n, k, dtype=np.int64)
+    lens[: nnz - k * n] += 1
+    ip = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(lens, out=ip[1:])
+    Au = sp.csr_matrix((rng.standard_normal(nnz), rng.integers(0, n, size=nnz), ip), shape=(n, n))
+    Au.sum_duplicates()
+    Au.sort_indices()
+    x = rng.standard_normal(n)
+    xd = torch.tensor(x, device="cuda")
+    for name, A in (("skewed", As), ("uniform", Au)):
+        a = pg.CsrMatrix.from_scipy(A)
+        yd = torch.zeros_like(xd)
+        for _ in range(3):
+            a.spmv(xd, y=yd)
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            a.spmv(xd, y=yd)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        b = 12 * A.nnz + 4 * (n + 1) + 16 * n
+        y_ref = A @ x
+        lens_a = np.diff(A.indptr)
+        out[name] = {"nnz": int(A.nnz), "max_row": int(lens_a.max()), "rows_over_32": int((lens_a > 32).sum()),
+                     "ms": ms, "gbs": b / ms / 1e6, "frac_of_hbm": b / ms / 1e6 / peak_gbs,
+                     "rel_diff_vs_scipy": float(np.linalg.norm(yd.cpu().numpy() - y_ref) / np.linalg.norm(y_ref))}
+        a.close()
+    return out
+
+
 def run_only(name: str, scale: float = 1.0) -> int:
     """One secondary workload on cuda:0, its result as one JSON line (`scale`
     shrinks the 64-instance batch of "batched" for profiling captures)."""
@@ -628,7 +675,8 @@ def run_only(name: str, scale: float = 1.0) -> int:
           "quad_batch": lambda: bench_quad_batch(torch, pg),
           "serial": lambda: bench_serial(torch, pg),
           "sai": lambda: bench_sai(torch, pg),
-          "laplace2d": lambda: bench_laplace2d(torch, pg)}[name]
+          "laplace2d": lambda: bench_laplace2d(torch, pg),
+          "skewed": lambda: bench_skewed(torch, pg, peak)}[name]
     print(json.dumps({name: fn()}), flush=True)
     return 0
 
@@ -644,7 +692,7 @@ def main():
     ap.add_argument("--n1", type=int, default=N1, help="grid side (128 = the benchmark workload; smaller only "
                                                         "for profiling captures)")
     ap.add_argument("--only", choices=["arnoldi_phi1", "multishift", "adjoint", "cg", "batched", "batched_arnoldi",
-                                       "quad_batch", "serial", "sai", "laplace2d"],
+                                       "quad_batch", "serial", "sai", "laplace2d", "skewed"],
                     help="run one secondary workload alone and print its result (for profiling captures)")
     ap.add_argument("--scale", type=float, default=1.0, help="with --only batched: instance sizes x scale "
                                                              "(smaller only for profiling captures)")

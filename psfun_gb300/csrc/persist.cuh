@@ -111,7 +111,7 @@ PSF_DEVINL bool pipe_spmv(const CsrDev& A, const double* __restrict__ x, int t0,
     } else {
       const SpmvTile& tb = sm.buf[b];
       const int nr = ti.r1 - ti.r0;
-      for (int lr = ctid; lr < nr; lr += kConsumerWarps * 32) epi(ti.r0 + lr, spmv_row(tb, ti, lr, x));
+      for (int base = ctid & ~31; base < nr; base += kConsumerWarps * 32) spmv_rows32(tb, ti, base, x, epi);
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&sm.empty[b]);

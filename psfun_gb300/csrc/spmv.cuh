@@ -155,17 +155,17 @@ PSF_DEVINL double spmv_batch(const SpmvTile& tb, int k, int cnt, int dj, const d
 }
 
 // Row sum of a staged tile: up to 8 gathers are issued before their FMAs.
-// Each batch is sized to the longest remaining row of the warp, chosen by a
-// warp-uniform switch: a predicated-off FP64 instruction still occupies the
-// FP64 pipe for the whole warp, so with 7 entries per row a fixed batch of 8
-// would cost one wasted FMA per row.  Entries are summed in order, so the
-// result does not depend on the batching.
-PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x) {
+// Each batch is sized to the longest remaining row among the lanes that sum
+// a row (wmax, warp-uniform), chosen by a warp-uniform switch: a
+// predicated-off FP64 instruction still occupies the FP64 pipe for the whole
+// warp, so with 7 entries per row a fixed batch of 8 would cost one wasted
+// FMA per row.  Entries are summed in order, so the result does not depend
+// on the batching.
+PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x, int wmax) {
   const int dj = ti.kv0 - ti.kj0;  // ja index = val index + dj
   const int di = ti.r0 - ti.ki0;
   const int kb = tb.irp[lr + di] - ti.kv0;
   const int ke = tb.irp[lr + di + 1] - ti.kv0;
-  const int wmax = __reduce_max_sync(__activemask(), ke - kb);
   double s = 0.0;
   for (int kk = 0; kk < wmax; kk += 8) {
     const int k = kb + kk;
@@ -182,6 +182,75 @@ PSF_DEVINL double spmv_row(const SpmvTile& tb, const TileInfo& ti, int lr, const
     }
   }
   return s;
+}
+
+// Row lr of a staged tile summed by the whole warp: lane l takes entries
+// l, l + 32, ... (four gathers in flight), then a butterfly sum; every lane
+// returns the total.
+PSF_DEVINL double spmv_row_warp(const SpmvTile& tb, const TileInfo& ti, int lr, const double* __restrict__ x) {
+  const int lane = threadIdx.x & 31;
+  const int dj = ti.kv0 - ti.kj0;
+  const int di = ti.r0 - ti.ki0;
+  const int kb = tb.irp[lr + di] - ti.kv0;
+  const int ke = tb.irp[lr + di + 1] - ti.kv0;
+  double s = 0.0;
+  for (int k0 = kb; k0 < ke; k0 += 128) {
+    double xv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + lane + 32 * q;
+      xv[q] = (k < ke) ? __ldg(x + tb.ja[k + dj]) : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + lane + 32 * q;
+      if (k0 + 32 * q < ke) s = fma((k < ke) ? tb.val[k] : 0.0, xv[q], s);
+    }
+  }
+  return warp_sum(s);
+}
+
+// The rows [base, base + 32) of a staged tile, one per lane of the calling
+// warp (lane l: row base + l), with the rows that are much longer than the
+// warp's others summed by the whole warp instead (row splitting for skewed
+// row lengths).  The split is chosen by counting FP64 warp instructions:
+// one row per lane costs the longest row's length, a row given to the warp
+// ceil(len / 32) + 5 (its FMAs and the butterfly); the threshold t is the
+// power of two from 32 up that minimises max(len <= t) + sum(len > t of
+// ceil(len / 32) + 5), or none when no t beats the plain schedule.  All
+// integer work on the warp's lengths; a warp whose rows are all at most 32
+// long takes the plain schedule at the cost of one reduction.  epi(r, sum)
+// is called once per row, by the row's lane.
+template <class Epi>
+PSF_DEVINL void spmv_rows32(const SpmvTile& tb, const TileInfo& ti, int base, const double* __restrict__ x, Epi& epi) {
+  const int lane = threadIdx.x & 31;
+  const int nr = ti.r1 - ti.r0;
+  const int lr = base + lane;
+  const bool valid = lr < nr;
+  const int di = ti.r0 - ti.ki0;
+  const int len = valid ? tb.irp[lr + di + 1] - tb.irp[lr + di] : 0;
+  const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)len);
+  int t = lmax, wshort = lmax;
+  if (lmax > 32) {
+    int best = lmax;
+    for (int c = 32; c < lmax; c <<= 1) {
+      const int smax = (int)__reduce_max_sync(0xffffffffu, (unsigned)(len <= c ? len : 0));
+      const int lcost = (int)__reduce_add_sync(0xffffffffu, (unsigned)(len > c ? (len + 31) / 32 + 5 : 0));
+      if (smax + lcost < best) {
+        best = smax + lcost;
+        t = c;
+        wshort = smax;
+      }
+    }
+  }
+  if (valid && len <= t) epi(ti.r0 + lr, spmv_row(tb, ti, lr, x, wshort));
+  unsigned longs = __ballot_sync(0xffffffffu, valid && len > t);
+  while (longs) {
+    const int j = __ffs(longs) - 1;
+    longs &= longs - 1;
+    const double s = spmv_row_warp(tb, ti, base + j, x);
+    if (lane == j) epi(ti.r0 + base + j, s);
+  }
 }
 
 // y = alpha*A*x + beta*y (psb_spmm); alpha may come from device memory.

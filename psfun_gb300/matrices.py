@@ -14,6 +14,8 @@ The benchmark problems are synthetic and seeded (numpy default_rng):
                       HHT rule with N = 24 and the analytic spectrum bounds
   uneven_batch        64 uneven instances (seed 3), 4 right-hand sides each
   grid_graph_adjoint  512^2 grid-graph Laplacian with lognormal(0,0.7) conductivities (seed 4)
+  skewed_rows         power-law row lengths (alpha 1.5, 4..4000 entries; seed 5) for the SpMV's
+                      row splitting
 """
 from __future__ import annotations
 
@@ -232,6 +234,31 @@ def uneven_spd_batch(count: int = 64, nrhs: int = 4):
         X = rng.standard_normal((nrhs, A.shape[0]))
         out.append(Problem(kind, A, X, dict(bounds=bounds)))
     return out
+
+
+def skewed_rows(n: int, alpha: float = 1.5, seed: int = 5, lmin: int = 4, lmax: int = 4000,
+                integer: bool = False) -> sp.csr_matrix:
+    """n x n matrix with power-law row lengths: len = min(lmax, floor(lmin u^(-1/alpha))),
+    u ~ U(0,1], so P(len > L) = (lmin/L)^alpha (alpha 1.5: mean ~12, about 250
+    rows per million longer than 1000); columns uniform without repetition in
+    a row, values N(0,1) (or nonzero integers in [-3, 3], for exact sums)."""
+    rng = np.random.default_rng(seed)
+    u = 1.0 - rng.random(n)
+    lens = np.minimum(lmax, np.floor(lmin * u ** (-1.0 / alpha))).astype(np.int64)
+    lens = np.minimum(lens, n)
+    indptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(lens, out=indptr[1:])
+    nnz = int(indptr[-1])
+    cols = rng.integers(0, n, size=nnz)
+    A = sp.csr_matrix((np.ones(nnz), cols, indptr), shape=(n, n))
+    A.sum_duplicates()  # a repeated column in a row merges
+    A.sort_indices()
+    if integer:
+        v = rng.integers(1, 4, size=A.nnz) * rng.choice([-1.0, 1.0], size=A.nnz)
+        A.data = v.astype(np.float64)
+    else:
+        A.data = rng.standard_normal(A.nnz)
+    return A
 
 
 def grid_graph_adjoint(N: int = 512):

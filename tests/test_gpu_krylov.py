@@ -95,6 +95,23 @@ def test_lanczos_variants_vs_oracle(lib, orc, variant, istop):
     assert rel(g.y, o["y"]) <= TOL
 
 
+def test_lanczos_skewed_graph_vs_oracle(lib, orc):
+    # a graph Laplacian with power-law degrees: the persistent Lanczos' SpMV
+    # sums the high-degree rows across a warp, into its fused epilogue
+    B = abs(matrices.skewed_rows(30000, alpha=1.3, seed=26))
+    S = (B + B.T).tocsr()
+    d = np.asarray(S.sum(axis=1)).ravel()
+    L = (sp.diags(d + 0.1) - S).tocsr()
+    L.sort_indices()
+    A = (-(0.5 / d.max()) * L).tocsr()
+    x = matrices.unit(np.random.default_rng(27).standard_normal(A.shape[0]))
+    for istop in (1, 2):
+        g = run_gpu("LANCZOS", "EXP", "CHBSYM", 1.0, A, x, 1e-11, itmax=40, istop=istop)
+        o = run_orc(orc, "LANCZOS", "EXP", "CHBSYM", 1.0, A, x, 1e-11, itmax=40, istop=istop)
+        assert g.info == 0 and o["info"] == 0 and g.iter == o["iter"]
+        assert rel(g.y, o["y"]) <= TOL
+
+
 def test_lanczos_ignores_scaling(lib, orc):
     """Lanczos drops fun%scaling (psfun_d_lanczos.f90:172-173,198): f(A)x is returned."""
     A = -matrices.laplacian_2d(16)

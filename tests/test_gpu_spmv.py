@@ -44,6 +44,32 @@ def test_spmv_bit_exact(lib, n, density, long_rows):
     assert np.array_equal(y2, 2.0 * (A @ x) - 3.0 * y0)
 
 
+# power-law row lengths: rows far longer than their warp-mates are summed by
+# the whole warp (every split threshold from 32 to 2048 taken somewhere)
+@pytest.mark.parametrize("n,alpha,seed", [(3000, 1.1, 21), (200000, 1.5, 22), (50000, 0.8, 23)])
+def test_spmv_skewed_rows_bit_exact(lib, n, alpha, seed):
+    import psfun_gb300 as pg
+    from psfun_gb300 import matrices
+    A = matrices.skewed_rows(n, alpha=alpha, seed=seed, integer=True)
+    x = np.random.default_rng(seed).integers(-5, 6, size=n).astype(np.float64)
+    a = pg.CsrMatrix.from_scipy(A)
+    assert np.array_equal(a.spmv(x), A @ x)
+    y0 = np.random.default_rng(seed + 1).integers(-5, 6, size=n).astype(np.float64)
+    assert np.array_equal(a.spmv(x, alpha=2.0, beta=-3.0, y=y0), 2.0 * (A @ x) - 3.0 * y0)
+
+
+def test_spmv_skewed_rows_float_matches_oracle(lib, orc):
+    import psfun_gb300 as pg
+    from psfun_gb300 import matrices
+    A = matrices.skewed_rows(40000, alpha=1.2, seed=24)
+    x = np.random.default_rng(25).standard_normal(A.shape[0])
+    y = pg.CsrMatrix.from_scipy(A).spmv(x, alpha=0.9)
+    ref = orc.spmv(orc.Csr.from_scipy(A), x, alpha=0.9)
+    # a warp-summed row adds its entries in another order: rounding only
+    scale = 0.9 * (abs(A) @ np.abs(x))
+    assert np.all(np.abs(y - ref) <= 1e-13 * scale + 1e-300)
+
+
 def test_spmv_one_based_input(lib):
     import psfun_gb300 as pg
     A = int_matrix(3000, 0.003, 7)
