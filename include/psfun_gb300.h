@@ -158,9 +158,13 @@ int psfun_gpu_serial_apply_device_static(psfun_serial* fun, int n, const double*
 int psfun_gpu_krylov_create(psfun_krylov** out);
 int psfun_gpu_krylov_destroy(psfun_krylov* meth);
 /* set(what, val): KNAME (:179-197); ITMAX, ITRACE, ISTOPC, IRST (:199-223).
- * Extension key (no counterpart in the reference): KEEPLAST = 1 makes the
+ * Extension keys (no counterpart in the reference): KEEPLAST = 1 makes the
  * final assembly use every coefficient of f(H) e1 instead of dropping the
- * last one as the reference does (psfun_d_arnoldi.f90:325-328). */
+ * last one as the reference does (psfun_d_arnoldi.f90:325-328); BATCHMAP
+ * fixes the SpMM mapping of psfun_gpu_d_krylov_batch (0 one thread per row,
+ * 1 nrhs threads per row, 2 one row per lane with the rows far longer than
+ * the warp's others summed by the whole warp) instead of the autotuner's
+ * choice (-1, the default); any other value returns 111. */
 int psfun_gpu_krylov_set_string(psfun_krylov* meth, const char* what, const char* val);
 int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val);
 /* The shift-and-invert method's parameters, which the reference keeps in the

@@ -209,8 +209,9 @@ class PsfunDKrylov:
 
     def set(self, what: str, val) -> int:
         """set(what, val): KNAME, KMETHD, PREC ('NONE' / 'DIAG') as strings;
-        ITMAX, ITRACE, ISTOPC, IRST, KEEPLAST as integers; TAU (the public
-        component meth%tau of the reference) as a real."""
+        ITMAX, ITRACE, ISTOPC, IRST, KEEPLAST, BATCHMAP (the batched Lanczos'
+        SpMM mapping, -1 = autotuned) as integers; TAU (the public component
+        meth%tau of the reference) as a real."""
         if isinstance(val, str):
             info = _lib().psfun_gpu_krylov_set_string(self.handle, what.encode(), val.encode())
             if info == 0 and what.strip().upper() == "KNAME":

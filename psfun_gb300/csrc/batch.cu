@@ -34,6 +34,7 @@ namespace psf {
 
 constexpr int kBatchMaxRhs = 4;
 constexpr int kBatchThreads = kSpmvThreads;
+constexpr int kBatchMappings = 3;  // SpMM mappings the autotuner chooses from
 
 // per-pair scalar arrays, each nl + 2 long
 enum { PA_ALPHA = 0, PA_BETA, PA_S, PA_RS, PA_YK, PA_COEF, PA_N };
@@ -193,6 +194,65 @@ PSF_DEVINL bool block_fT(const BInst& I, int nl, int m, unsigned mask) {
 // ---- phases ------------------------------------------------------------------
 enum { PH_INIT = 0, PH_SPMM = 1, PH_UPDATE = 2, PH_RECOMB = 3 };
 
+// One row of a staged tile against the R right-hand sides of W (row-major,
+// R per row), entries [kb, ke) of the buffer in order, four entries' gathers
+// in flight before their FMAs.
+template <int R>
+PSF_DEVINL void batch_row_thread(const SpmvTile& tb, int kb, int ke, int dj, const double* __restrict__ wi,
+                                 double (&s)[R]) {
+#pragma unroll
+  for (int q = 0; q < R; ++q) s[q] = 0.0;
+  int k = kb;
+  for (; k + 4 <= ke; k += 4) {
+    double a[4], xv[4][R];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      a[e] = tb.val[k + e];
+      const double* xr = wi + (size_t)tb.ja[k + e + dj] * R;
+      if (R == 4) {
+        const double2 x01 = __ldg(reinterpret_cast<const double2*>(xr));
+        const double2 x23 = __ldg(reinterpret_cast<const double2*>(xr) + 1);
+        xv[e][0] = x01.x;
+        xv[e][1 % R] = x01.y;
+        xv[e][2 % R] = x23.x;
+        xv[e][3 % R] = x23.y;
+      } else {
+#pragma unroll
+        for (int q = 0; q < R; ++q) xv[e][q] = __ldg(xr + q);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) s[q] = fma(a[e], xv[e][q], s[q]);
+    }
+  }
+  for (; k < ke; ++k) {
+    const double a = tb.val[k];
+    const double* xr = wi + (size_t)tb.ja[k + dj] * R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
+  }
+}
+
+// The same row summed by the whole warp: lane l takes entries l, l + 32, ...,
+// then one butterfly per right-hand side; every lane gets the R totals.
+template <int R>
+PSF_DEVINL void batch_row_warp(const SpmvTile& tb, int kb, int ke, int dj, const double* __restrict__ wi,
+                               double (&s)[R]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < R; ++q) s[q] = 0.0;
+  for (int k = kb + lane; k < ke; k += 32) {
+    const double a = tb.val[k];
+    const double* xr = wi + (size_t)tb.ja[k + dj] * R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) s[q] = warp_sum(s[q]);
+}
+
 // Row-level work of one tile for phase `ph`; returns the R partial sums.
 template <int R>
 PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs& B, SpmvSmem& sm, double* accR,
@@ -247,47 +307,50 @@ PSF_DEVINL void tile_work(const BInst& I, int ph, int i, int lt, const BatchArgs
     const int dj = ti.kv0 - ti.kj0, di = ti.r0 - ti.ki0;
     if (I.mapping == 0) {  // one thread per row, R accumulators
       for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-        const int kb = tb.irp[lr + di] - ti.kv0, ke = tb.irp[lr + di + 1] - ti.kv0;
         double s[R];
-#pragma unroll
-        for (int q = 0; q < R; ++q) s[q] = 0.0;
-        // four entries' gathers in flight before their FMAs (entry order kept)
-        int k = kb;
-        for (; k + 4 <= ke; k += 4) {
-          double a[4], xv[4][R];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            a[e] = tb.val[k + e];
-            const double* xr = wi + (size_t)tb.ja[k + e + dj] * R;
-            if (R == 4) {
-              const double2 x01 = __ldg(reinterpret_cast<const double2*>(xr));
-              const double2 x23 = __ldg(reinterpret_cast<const double2*>(xr) + 1);
-              xv[e][0] = x01.x;
-              xv[e][1 % R] = x01.y;
-              xv[e][2 % R] = x23.x;
-              xv[e][3 % R] = x23.y;
-            } else {
-#pragma unroll
-              for (int q = 0; q < R; ++q) xv[e][q] = __ldg(xr + q);
-            }
-          }
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-#pragma unroll
-            for (int q = 0; q < R; ++q) s[q] = fma(a[e], xv[e][q], s[q]);
-          }
-        }
-        for (; k < ke; ++k) {
-          const double a = tb.val[k];
-          const double* xr = wi + (size_t)tb.ja[k + dj] * R;
-#pragma unroll
-          for (int q = 0; q < R; ++q) s[q] = fma(a, __ldg(xr + q), s[q]);
-        }
+        batch_row_thread<R>(tb, tb.irp[lr + di] - ti.kv0, tb.irp[lr + di + 1] - ti.kv0, dj, wi, s);
         const int r = ti.r0 + lr;
 #pragma unroll
         for (int q = 0; q < R; ++q) {
           I.u[(size_t)r * R + q] = s[q];
           accR[q] = fma(s[q], wi[(size_t)r * R + q], accR[q]);
+        }
+      }
+    } else if (I.mapping == 2) {
+      // one row per lane, R accumulators, and the rows far longer than the
+      // warp's others summed by the whole warp (spmv.cuh::warp_row_split)
+      const int lane = threadIdx.x & 31;
+      for (int base = threadIdx.x & ~31; base < nr; base += blockDim.x) {
+        const int lr = base + lane;
+        const bool valid = lr < nr;
+        const int kb = valid ? tb.irp[lr + di] - ti.kv0 : 0, ke = valid ? tb.irp[lr + di + 1] - ti.kv0 : 0;
+        int wshort;
+        const int t = warp_row_split(ke - kb, wshort);
+        if (valid && ke - kb <= t) {
+          double s[R];
+          batch_row_thread<R>(tb, kb, ke, dj, wi, s);
+          const int r = ti.r0 + lr;
+#pragma unroll
+          for (int q = 0; q < R; ++q) {
+            I.u[(size_t)r * R + q] = s[q];
+            accR[q] = fma(s[q], wi[(size_t)r * R + q], accR[q]);
+          }
+        }
+        unsigned longs = __ballot_sync(0xffffffffu, valid && ke - kb > t);
+        while (longs) {
+          const int j = __ffs(longs) - 1;
+          longs &= longs - 1;
+          const int lj = base + j;
+          double s[R];
+          batch_row_warp<R>(tb, tb.irp[lj + di] - ti.kv0, tb.irp[lj + di + 1] - ti.kv0, dj, wi, s);
+          if (lane == j) {
+            const int r = ti.r0 + lj;
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+              I.u[(size_t)r * R + q] = s[q];
+              accR[q] = fma(s[q], wi[(size_t)r * R + q], accR[q]);
+            }
+          }
         }
       }
     } else {  // R threads per row, one right-hand side each
@@ -951,9 +1014,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) k_batch(BatchArgs B) {
 }
 
 // ---- autotuner ----------------------------------------------------------------
-// The SpMM mapping (one thread per row with R accumulators, or R threads per
-// row) is chosen per size bucket by timing a standalone run of the same tile
-// code on the bucket's first instance; the choice is cached per (bucket, R).
+// The SpMM mapping (0: one thread per row with R accumulators; 1: R threads
+// per row; 2: one row per lane with the rows far longer than the warp's
+// others summed by the whole warp) is chosen per size bucket by timing a
+// standalone run of the same tile code on the bucket's first instance; the
+// choice is cached per (bucket, R).
 template <int R>
 __global__ void __launch_bounds__(kBatchThreads) k_batch_spmm_probe(BatchArgs B, int k) {
   PSF_SPMV_SMEM();
@@ -1002,7 +1067,7 @@ static int autotune(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, cudaS
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int map = 0; map < 2; ++map) {
+    for (int map = 0; map < kBatchMappings; ++map) {
       hinst[k].mapping = map;
       PSF_CUDA(cudaMemcpyAsync(dinst + k, &hinst[k], sizeof(BInst), cudaMemcpyHostToDevice, s));
       const int g = std::max(1, std::min(hinst[k].ntiles, sm_count() * 2));
@@ -1040,9 +1105,14 @@ static void batch_attrs() {
 }
 
 template <int R>
-static int batch_launch(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, cudaStream_t s, int tune) {
+static int batch_launch(BatchArgs& B, std::vector<BInst>& hinst, BInst* dinst, cudaStream_t s, int mapping) {
   batch_attrs<R>();
-  if (tune) PSF_TRY(autotune<R>(B, hinst, dinst, s));
+  if (mapping < 0) {
+    PSF_TRY(autotune<R>(B, hinst, dinst, s));
+  } else {  // one mapping for every instance, as the caller asked
+    for (auto& I : hinst) I.mapping = mapping;
+    PSF_CUDA(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BInst) * hinst.size(), cudaMemcpyHostToDevice, s));
+  }
   int per = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch<R>, kBatchThreads, kSpmvSmemBytes);
   if (per < 1) per = 1;
@@ -1074,8 +1144,8 @@ struct BatchDesc {
   double eta, sign;
 };
 
-static int batch_run(DevBuf* wsbuf, int keeplast, int count, const std::vector<BatchDesc>& items, int R, double eps,
-                     int itmax, int istop, int* iters, double* errs, int* infos) {
+static int batch_run(DevBuf* wsbuf, int keeplast, int mapping, int count, const std::vector<BatchDesc>& items, int R,
+                     double eps, int itmax, int istop, int* iters, double* errs, int* infos) {
   const int nl = itmax;
   cudaStream_t s = stream();
   // workspace: one allocation, carved per instance
@@ -1170,10 +1240,10 @@ static int batch_run(DevBuf* wsbuf, int keeplast, int count, const std::vector<B
   PSF_CUDA(cudaMemcpyAsync(B.active, &active, sizeof active, cudaMemcpyHostToDevice, s));
   int rc;
   switch (R) {
-    case 1: rc = batch_launch<1>(B, hinst, dinst, s, 1); break;
-    case 2: rc = batch_launch<2>(B, hinst, dinst, s, 1); break;
-    case 3: rc = batch_launch<3>(B, hinst, dinst, s, 1); break;
-    default: rc = batch_launch<4>(B, hinst, dinst, s, 1); break;
+    case 1: rc = batch_launch<1>(B, hinst, dinst, s, mapping); break;
+    case 2: rc = batch_launch<2>(B, hinst, dinst, s, mapping); break;
+    case 3: rc = batch_launch<3>(B, hinst, dinst, s, mapping); break;
+    default: rc = batch_launch<4>(B, hinst, dinst, s, mapping); break;
   }
   if (rc != PSFUN_SUCCESS) return rc;
   int herr = 0;
@@ -1256,7 +1326,8 @@ extern "C" int psfun_gpu_d_krylov_batch(psfun_krylov* meth, psfun_serial* fun, i
   std::vector<psf::BatchDesc> desc(count);
   for (int k = 0; k < count; ++k)
     desc[k] = psf::BatchDesc{items[k].a, items[k].x, items[k].y, items[k].scaling, 0, nullptr, nullptr, 0.0, 0.0};
-  return psf::batch_run(&meth->scratch, meth->keeplast, count, desc, R, eps, itmax, istop, iters, errs, infos);
+  return psf::batch_run(&meth->scratch, meth->keeplast, meth->batchmap, count, desc, R, eps, itmax, istop, iters, errs,
+                        infos);
 }
 
 extern "C" int psfun_gpu_z_quadrature_batch(int count, const psfun_quad_item* items, double eps, int itmax,
@@ -1279,5 +1350,5 @@ extern "C" int psfun_gpu_z_quadrature_batch(int count, const psfun_quad_item* it
     desc[k] = psf::BatchDesc{q.a, q.x, q.y, 1.0, q.N, q.xi, q.c, q.eta, q.sign};
   }
   static psf::DevBuf ws;  // workspace of the quadrature batches
-  return psf::batch_run(&ws, 0, count, desc, R, eps, itmax, 1, iters, errs, infos);
+  return psf::batch_run(&ws, 0, -1, count, desc, R, eps, itmax, 1, iters, errs, infos);
 }

@@ -772,6 +772,7 @@ int psfun_gpu_krylov_set_integer(psfun_krylov* meth, const char* what, int val) 
   else if (k == "ISTOPC") meth->istopc = val;
   else if (k == "IRST") meth->irst = val;
   else if (k == "KEEPLAST") meth->keeplast = val;
+  else if (k == "BATCHMAP" && val >= -1 && val <= 2) meth->batchmap = val;
   else return PSFUN_ERR_INVALID_ARGS_COMBINATION;
   return PSFUN_SUCCESS;
 }

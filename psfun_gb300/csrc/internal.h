@@ -147,6 +147,7 @@ struct psfun_krylov {
   double tau = 0.0;
   int itmax = 200, itrace = 0, istopc = 1, irst = 10;
   int keeplast = 0;
+  int batchmap = -1;  // SpMM mapping of the batched Lanczos: -1 chosen by the autotuner, 0..2 fixed
   int prec = 0;  // inner-solve preconditioner of SAIARNOLDI: 0 NONE, 1 DIAG
   // cached workspace (never per call)
   psf::DevBuf V, u, small, scratch, partials, ctrl, xy;

@@ -221,16 +221,14 @@ PSF_DEVINL double spmv_row_warp(const SpmvTile& tb, const TileInfo& ti, int lr, 
 // integer work on the warp's lengths; a warp whose rows are all at most 32
 // long takes the plain schedule at the cost of one reduction.  epi(r, sum)
 // is called once per row, by the row's lane.
-template <class Epi>
-PSF_DEVINL void spmv_rows32(const SpmvTile& tb, const TileInfo& ti, int base, const double* __restrict__ x, Epi& epi) {
-  const int lane = threadIdx.x & 31;
-  const int nr = ti.r1 - ti.r0;
-  const int lr = base + lane;
-  const bool valid = lr < nr;
-  const int di = ti.r0 - ti.ki0;
-  const int len = valid ? tb.irp[lr + di + 1] - tb.irp[lr + di] : 0;
-  const int lmax = __reduce_max_sync(0xffffffffu, (unsigned)len);
-  int t = lmax, wshort = lmax;
+// The split of a warp's 32 rows (this lane's row has len entries, 0 past
+// the tile): returns the threshold t (rows longer than t go to the whole
+// warp) and in wshort the longest row kept by its lane.  Warp-uniform; all
+// 32 lanes must call it.
+PSF_DEVINL int warp_row_split(int len, int& wshort) {
+  const int lmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)len);
+  int t = lmax;
+  wshort = lmax;
   if (lmax > 32) {
     int best = lmax;
     for (int c = 32; c < lmax; c <<= 1) {
@@ -243,6 +241,19 @@ PSF_DEVINL void spmv_rows32(const SpmvTile& tb, const TileInfo& ti, int base, co
       }
     }
   }
+  return t;
+}
+
+template <class Epi>
+PSF_DEVINL void spmv_rows32(const SpmvTile& tb, const TileInfo& ti, int base, const double* __restrict__ x, Epi& epi) {
+  const int lane = threadIdx.x & 31;
+  const int nr = ti.r1 - ti.r0;
+  const int lr = base + lane;
+  const bool valid = lr < nr;
+  const int di = ti.r0 - ti.ki0;
+  const int len = valid ? tb.irp[lr + di + 1] - tb.irp[lr + di] : 0;
+  int wshort;
+  const int t = warp_row_split(len, wshort);
   if (valid && len <= t) epi(ti.r0 + lr, spmv_row(tb, ti, lr, x, wshort));
   unsigned longs = __ballot_sync(0xffffffffu, valid && len > t);
   while (longs) {

@@ -80,6 +80,52 @@ def test_batch_matches_plain(lib, orc, istop, R):
             assert np.linalg.norm(Y[q] - o["y"]) <= tol * np.linalg.norm(o["y"]), (k, q, tol)
 
 
+def skewed_laplacian(n, seed):
+    """Graph Laplacian (+ 0.1 I) of a power-law degree graph, scaled to
+    spectral radius <= 1: rows of 2..~8000 entries."""
+    import scipy.sparse as sp
+    B = abs(matrices.skewed_rows(n, alpha=1.3, seed=seed))
+    S = (B + B.T).tocsr()
+    d = np.asarray(S.sum(axis=1)).ravel()
+    L = (sp.diags(d + 0.1) - S).tocsr()
+    L.sort_indices()
+    return (-(0.5 / d.max()) * L).tocsr()
+
+
+@pytest.mark.parametrize("mapping", [-1, 0, 1, 2])
+def test_batch_mappings_skewed_rows(lib, orc, mapping):
+    # every SpMM mapping of the batch (and the autotuner's pick) on instances
+    # with power-law row lengths beside regular ones, against the plain calls
+    torch = pytest.importorskip("torch")
+    import psfun_gb300 as pg
+    eps, itmax, R = 1e-8, 30, 2
+    rng = np.random.default_rng(40)
+    mats = [skewed_laplacian(n, 41 + k) for k, n in enumerate((3000, 20000, 70000))]
+    mats.append(-0.2 * matrices.laplacian_2d(50))
+    items, handles = [], []
+    for A in mats:
+        X = rng.standard_normal((R, A.shape[0]))
+        items.append((A, X))
+        handles.append((pg.CsrMatrix.from_scipy(A), torch.tensor(X, device="cuda"),
+                        torch.zeros((R, A.shape[0]), dtype=torch.float64, device="cuda"), 1.0))
+    fun = pg.PsfunDSerial()
+    fun.set("FNAME", "EXP")
+    fun.set("VARIANT", "CHBSYM")
+    meth = pg.PsfunDKrylov()
+    meth.set("KNAME", "LANCZOS")
+    assert meth.set("BATCHMAP", mapping) == 0
+    info, infos, iters, errs = pg.krylov_batch(meth, fun, handles, eps, itmax=itmax, istop=1)
+    torch.cuda.synchronize()
+    assert info == 0 and not infos.any()
+    for k, ((A, X), (_, _, Yd, _)) in enumerate(zip(items, handles)):
+        Y = Yd.cpu().numpy()
+        for q in range(R):
+            r = plain(A, X[q], 1.0, eps, itmax, 1)
+            assert r.info == 0 and iters[k, q] == r.iter, (k, q)
+            assert np.linalg.norm(Y[q] - r.y) <= 1e-10 * np.linalg.norm(r.y), (k, q)
+    assert meth.set("BATCHMAP", 3) == 111 and meth.set("BATCHMAP", -2) == 111
+
+
 def test_batch_zero_rhs_and_errors(lib):
     torch = pytest.importorskip("torch")
     import psfun_gb300 as pg
