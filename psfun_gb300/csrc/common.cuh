@@ -292,13 +292,21 @@ PSF_DEVINL bool grid_barrier(unsigned int* count, volatile unsigned int* gen, in
 // completes when the counter reaches target = k * gridDim.x.  Compared with
 // grid_barrier, no generation word is read before arriving and the arrival is
 // a fire-and-forget reduction, which takes two L2 round trips off the release
-// path.  Memory ordering as in grid_barrier: the block barrier and the fence
-// before the arrival publish the block's writes; the acquire load and the
-// fence after the wait make the other blocks' writes visible.
+// path.  Memory ordering in the PTX model: the block barrier orders the
+// block's writes before thread 0's arrival, a reduction with release
+// semantics (cumulative, so it publishes what the block barrier ordered
+// before it); thread 0's acquire load that sees the target synchronises with
+// every arrival (the arrivals are read-modify-writes, each heading a release
+// sequence that the later ones continue), and the block barrier after the
+// wait extends that to the block's threads.  No separate fences.
 PSF_DEVINL unsigned ld_acquire_gpu(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+PSF_DEVINL void red_release_gpu_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 PSF_DEVINL bool grid_sync_to(unsigned int* count, unsigned int target, int* err) {
@@ -306,8 +314,7 @@ PSF_DEVINL bool grid_sync_to(unsigned int* count, unsigned int target, int* err)
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    __threadfence();
-    atomicAdd(count, 1u);
+    red_release_gpu_add(count, 1u);
     const unsigned long long t0 = globaltimer_ns();
     while (ld_acquire_gpu(count) < target) {
       if (*(volatile int*)err != 0) { ok = 0; break; }
@@ -318,7 +325,6 @@ PSF_DEVINL bool grid_sync_to(unsigned int* count, unsigned int target, int* err)
       }
       __nanosleep(32);
     }
-    __threadfence();
   }
   __syncthreads();
   return ok != 0;
