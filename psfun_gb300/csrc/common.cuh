@@ -309,6 +309,13 @@ PSF_DEVINL void red_release_gpu_add(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// A progress word published with release semantics (the thread's earlier
+// writes, and those a block barrier ordered before it, become visible to a
+// reader that sees the value and then fences).
+PSF_DEVINL void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 PSF_DEVINL bool grid_sync_to(unsigned int* count, unsigned int target, int* err) {
   __shared__ int ok;
   __syncthreads();

@@ -320,8 +320,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_lz_persist(KState st, CsrDev A
               c->breakdown = 1;
               c->itx = i;
             }
-            __threadfence();
-            *(volatile int*)&c->pub = i;
+            st_release_gpu(&c->pub, i);
           }
         }
       }
@@ -710,17 +709,11 @@ __global__ void __launch_bounds__(kMgsSmThreads) k_ar_persist(KState st, int chu
   int last = 0;
   for (int i = 2; i <= nl; ++i) {
     if (ar_step(st, i, chunk, nb, A, scaling, 1, G, mgs_sm) != 0) break;
-    if (b == 0 && threadIdx.x == 0) {
-      __threadfence();
-      *(volatile int*)&c->pub = i - 1;
-    }
+    if (b == 0 && threadIdx.x == 0) st_release_gpu(&c->pub, i - 1);
     last = i - 1;
     if (i < nl && !grid_sync_to(&c->bar_count, (++nb) * (unsigned)G, &c->err)) break;
   }
-  if (b == 0 && threadIdx.x == 0) {
-    __threadfence();
-    *(volatile int*)&c->steps_end = last + 1;
-  }
+  if (b == 0 && threadIdx.x == 0) st_release_gpu(&c->steps_end, last + 1);
 }
 
 // A posteriori estimate of iteration i (psfun_d_arnoldi.f90:222-276,
@@ -1350,6 +1343,16 @@ static int grid_for(int64_t items, int threads, int per_sm) {
   return (int)g;
 }
 
+// Grid of the vector kernels (k_init, k_recombine, ...) over n rows: eight
+// rows per thread on large n, but never fewer blocks than one row per thread
+// would fill on one wave of the GPU (a small n, e.g. 10,000 rows, would
+// otherwise run on 5 blocks, each thread its rows' FP64 chains one after
+// another).
+static int vec_grid(int64_t n) {
+  return grid_for(std::max<int64_t>(n / 8 + 1, std::min<int64_t>(n, (int64_t)sm_count() * kVecThreads)), kVecThreads,
+                  4);
+}
+
 // Grid and rows per block of k_ar_mgs_sm for n rows, or 0 when the rows of a
 // block do not fit in shared memory.
 static int mgs_sm_plan(int64_t n, int* chunk) {
@@ -1466,7 +1469,7 @@ int krylov_apply_device(psfun_krylov* meth, psfun_serial* fun, psfun_csr* a, dou
   const CsrDev A = a->dev();
   spmv_kernel_attrs();
   const int gs = grid_for((int64_t)a->ntiles * kSpmvThreads, kSpmvThreads, 4);
-  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  const int gv = vec_grid(n);
   const int gm = mgs_grid();
   int mgs_chunk = 0;
   const int gms = arnoldi ? mgs_sm_plan(n, &mgs_chunk) : 0;
@@ -2129,7 +2132,7 @@ static int shifted_lanczos(psfun_krylov* ws, DevBuf& msbuf, psfun_csr* a, const 
   st.host_flag = dflag;
   const CsrDev A = a->dev();
   spmv_kernel_attrs();
-  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  const int gv = vec_grid(n);
   k_init<<<gv, kVecThreads, 0, s>>>(st, b);
   count_launch();
   // Every Lanczos step in one persistent cooperative launch; its monitor
@@ -2179,7 +2182,7 @@ int quad_apply_device(psfun_csr* a, int N, const double* xi, const double* cw, d
   }
   run.mp.eta = eta;
   cudaStream_t s = stream();
-  const int gv = grid_for(a->n / 8 + 1, kVecThreads, 4);
+  const int gv = vec_grid(a->n);
   k_ms_final<<<1, kDenseThreads, 0, s>>>(run.st, run.mp);
   k_recombine<<<gv, kVecThreads, 0, s>>>(run.st, y);
   count_launch(2);
@@ -2537,7 +2540,7 @@ static int expm_adjoint_arnoldi(psfun_csr* a, double t, const double* x, const d
   PSF_CUDA(cudaMemcpyAsync(cx_save, arx->ctrl.ptr, sizeof(KCtrl), cudaMemcpyDeviceToDevice, s));
   if (grad_t) {  // dL/dt = g^T A y, before a recomputation reuses y's workspace
     PSF_TRY(spmv_device(a, 1.0, ytmp, 0.0, Ay));
-    const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+    const int gv = vec_grid(n);
     const int nb = std::min(gv, 4000);
     static DevBuf part;
     PSF_TRY(part.ensure(sizeof(double) * 4096));
@@ -2576,7 +2579,7 @@ static int expm_adjoint_arnoldi(psfun_csr* a, double t, const double* x, const d
     const double* E = scr.as<double>() + 4 * (size_t)M * M;
     k_adj_vanloan_R<<<std::max(1, std::min(1024, (mg * mx + 255) / 256)), 256, 0, s>>>(
         E, M, mg, mx, t, wg->ctrl.as<KCtrl>(), cx_save, small_of(wg) + (size_t)ldh * ldh, sx_save, R);
-    const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+    const int gv = vec_grid(n);
     adj_P(wg->V.as<double>(), wg->ldv, mg, R, mx, n, P, ld, s);
     count_launch(2);
     const double* Wx = arx->V.as<double>();
@@ -2652,7 +2655,7 @@ int expm_adjoint_device(psfun_csr* a, double t, const double* x, const double* g
   PSF_CUDA(cudaMemcpyAsync(dz, zc_h.data(), sizeof(double) * 2 * Nq, cudaMemcpyHostToDevice, s));
   PSF_CUDA(cudaMemcpyAsync(dc, cw_h.data(), sizeof(double) * 2 * Nq, cudaMemcpyHostToDevice, s));
   AdjShifts sh{Nq, dz, dc, t};
-  const int gv = grid_for(n / 8 + 1, kVecThreads, 4);
+  const int gv = vec_grid(n);
   PSF_TRY(tmpv.ensure(sizeof(double) * ld * 2));
   double* ytmp = y ? y : tmpv.as<double>();
   double* Ay = tmpv.as<double>() + ld;
