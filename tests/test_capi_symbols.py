@@ -46,6 +46,9 @@ def test_setters_without_gpu(lib):
     k = pg.PsfunDKrylov()
     assert k.set("kname", "LANCZOS") == 0 and k.set("itmax", 10) == 0 and k.set("BAD", 1) == 111
     assert k.set("ITMAX", "x") == 111
+    # the batched Lanczos' SpMM mapping: -1 (autotuned) or 0..2
+    assert all(k.set("BATCHMAP", v) == 0 for v in (-1, 0, 1, 2))
+    assert k.set("BATCHMAP", 3) == 111 and k.set("batchmap", -2) == 111
 
 
 def test_precinit_types_without_gpu(lib):
