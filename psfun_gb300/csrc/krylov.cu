@@ -467,55 +467,73 @@ inline unsigned mgs_barriers_before(int i) {
 
 // One paired sweep over the block's rows of w: w -= c1 v_k (and c2 v_{k+1}
 // with TWO), then the dots of the result with the next vectors (NEXT = 1 or
-// 2) or its squared norm (NEXT = 0) into acc1, acc2.  Rows go in groups per
-// thread (four, or two when four vectors stream); the next group's loads are
-// issued before this group's arithmetic.  Rows are accumulated in order, so
-// the sums are reproducible.
+// 2) or its squared norm (NEXT = 0) into acc1, acc2.  A thread takes two
+// adjacent rows at a time (16-byte loads and shared-memory accesses, half
+// the load/store instructions of one row per access: the sweep is FP64-bound
+// and the issue slots it frees go to the FMAs), pairs in groups per thread
+// (two, or one when four vectors stream), the next group's loads issued
+// before this group's arithmetic; an odd last row goes to thread 0.  Rows
+// are accumulated in a fixed order, so the sums are reproducible.  wl, and
+// the vectors at the block's first row, are 16-byte aligned (the block's
+// rows start at an even row of a basis whose leading dimension is a
+// multiple of 32).
 template <bool TWO, int NEXT>
 PSF_DEVINL void mgs_pair_sweep(double* __restrict__ wl, int nloc, int bd, double c1, double c2,
                                const double* __restrict__ vk, const double* __restrict__ vk1,
                                const double* __restrict__ vn1, const double* __restrict__ vn2, double& acc1,
                                double& acc2) {
-  auto row = [&](int r, double a, double a1, double n1, double n2) {
-    double v = fma(-c1, a, wl[r]);
+  auto one = [&](double w, double a, double a1, double n1, double n2) {
+    double v = fma(-c1, a, w);
     if (TWO) v = fma(-c2, a1, v);
-    wl[r] = v;
     if (NEXT == 0) acc1 = fma(v, v, acc1);
     if (NEXT >= 1) acc1 = fma(n1, v, acc1);
     if (NEXT == 2) acc2 = fma(n2, v, acc2);
+    return v;
   };
-  // rows per group: the group's loads and the next group's stay in registers
+  double2* __restrict__ w2 = reinterpret_cast<double2*>(wl);
+  const double2* __restrict__ k2 = reinterpret_cast<const double2*>(vk);
+  const double2* __restrict__ k12 = reinterpret_cast<const double2*>(vk1);
+  const double2* __restrict__ n12 = reinterpret_cast<const double2*>(vn1);
+  const double2* __restrict__ n22 = reinterpret_cast<const double2*>(vn2);
+  const double2 z2 = make_double2(0.0, 0.0);
+  auto pair = [&](int p, double2 a, double2 a1, double2 n1, double2 n2) {
+    const double2 w = w2[p];
+    const double vx = one(w.x, a.x, a1.x, n1.x, n2.x);
+    const double vy = one(w.y, a.y, a1.y, n1.y, n2.y);
+    w2[p] = make_double2(vx, vy);
+  };
   constexpr int kStreams = 1 + (TWO ? 1 : 0) + NEXT;
-  constexpr int RG = (kStreams <= 2) ? 4 : 2;
-  int l = threadIdx.x;
-  if (l + (RG - 1) * bd < nloc) {
-    double a[RG], a1[RG], n1[RG], n2[RG];
+  constexpr int PG = (kStreams <= 2) ? 2 : 1;  // pairs per group
+  const int np = nloc >> 1;
+  int p = threadIdx.x;
+  if (p + (PG - 1) * bd < np) {
+    double2 a[PG], a1[PG], n1[PG], n2[PG];
 #pragma unroll
-    for (int q = 0; q < RG; ++q) {
-      a[q] = vk[l + q * bd];
-      a1[q] = TWO ? vk1[l + q * bd] : 0.0;
-      n1[q] = (NEXT >= 1) ? vn1[l + q * bd] : 0.0;
-      n2[q] = (NEXT == 2) ? vn2[l + q * bd] : 0.0;
+    for (int q = 0; q < PG; ++q) {
+      a[q] = k2[p + q * bd];
+      a1[q] = TWO ? k12[p + q * bd] : z2;
+      n1[q] = (NEXT >= 1) ? n12[p + q * bd] : z2;
+      n2[q] = (NEXT == 2) ? n22[p + q * bd] : z2;
     }
     for (;;) {
-      const int ln = l + RG * bd;
-      const bool more = ln + (RG - 1) * bd < nloc;
-      double b[RG], b1[RG], m1[RG], m2[RG];
+      const int pn = p + PG * bd;
+      const bool more = pn + (PG - 1) * bd < np;
+      double2 b[PG], b1[PG], m1[PG], m2[PG];
       if (more) {
 #pragma unroll
-        for (int q = 0; q < RG; ++q) {
-          b[q] = vk[ln + q * bd];
-          b1[q] = TWO ? vk1[ln + q * bd] : 0.0;
-          m1[q] = (NEXT >= 1) ? vn1[ln + q * bd] : 0.0;
-          m2[q] = (NEXT == 2) ? vn2[ln + q * bd] : 0.0;
+        for (int q = 0; q < PG; ++q) {
+          b[q] = k2[pn + q * bd];
+          b1[q] = TWO ? k12[pn + q * bd] : z2;
+          m1[q] = (NEXT >= 1) ? n12[pn + q * bd] : z2;
+          m2[q] = (NEXT == 2) ? n22[pn + q * bd] : z2;
         }
       }
 #pragma unroll
-      for (int q = 0; q < RG; ++q) row(l + q * bd, a[q], a1[q], n1[q], n2[q]);
-      l = ln;
+      for (int q = 0; q < PG; ++q) pair(p + q * bd, a[q], a1[q], n1[q], n2[q]);
+      p = pn;
       if (!more) break;
 #pragma unroll
-      for (int q = 0; q < RG; ++q) {
+      for (int q = 0; q < PG; ++q) {
         a[q] = b[q];
         a1[q] = b1[q];
         n1[q] = m1[q];
@@ -523,8 +541,12 @@ PSF_DEVINL void mgs_pair_sweep(double* __restrict__ wl, int nloc, int bd, double
       }
     }
   }
-  for (; l < nloc; l += bd)
-    row(l, vk[l], TWO ? vk1[l] : 0.0, (NEXT >= 1) ? vn1[l] : 0.0, (NEXT == 2) ? vn2[l] : 0.0);
+  for (; p < np; p += bd)
+    pair(p, k2[p], TWO ? k12[p] : z2, (NEXT >= 1) ? n12[p] : z2, (NEXT == 2) ? n22[p] : z2);
+  if ((nloc & 1) && threadIdx.x == 0) {
+    const int r = nloc - 1;
+    wl[r] = one(wl[r], vk[r], TWO ? vk1[r] : 0.0, (NEXT >= 1) ? vn1[r] : 0.0, (NEXT == 2) ? vn2[r] : 0.0);
+  }
 }
 
 // One Arnoldi step i on the G blocks [0, G) of the launch (the body of
