@@ -10,9 +10,11 @@
 // (cp.async.bulk) that stage the tile's values, column indices and row
 // pointers into shared memory behind an mbarrier; then each thread owns one
 // row and reads its entries from shared memory, gathering x through the
-// read-only path.  Values and indices are therefore read from HBM exactly once,
-// in 16-byte-aligned bulk transfers, whatever the row lengths.  Long rows are
-// reduced cooperatively straight from global memory.  The tile pipeline that
+// read-only path; rows far longer than the other rows of their warp are
+// summed by the whole warp instead (spmv_rows32).  Values and indices are
+// therefore read from HBM exactly once, in 16-byte-aligned bulk transfers,
+// whatever the row lengths.  A row longer than a tile is reduced
+// cooperatively straight from global memory.  The tile pipeline that
 // drives this (a producer warp staging four tiles ahead of fifteen consumer
 // warps) is in persist.cuh; the batched launch stages its tiles itself.
 #pragma once
