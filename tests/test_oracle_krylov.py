@@ -176,3 +176,14 @@ def test_oracle_saiarnoldi_reference_quirks(orc):
     r2 = orc.saiarnoldi(orc.serial("EXP", "GENPADE", 1.0), orc.Csr.from_scipy(A), x, 1e-10, tau=0.0, istop=2,
                         itmax=40)
     assert r2["info"] == 0 and r2["iter"] == 39
+
+
+def test_oracle_spmv_on_power_law_rows(orc):
+    # the checker of the GPU row-splitting tests: exact on integer data,
+    # against scipy, whatever the row lengths
+    A = matrices.skewed_rows(30000, alpha=1.2, seed=31, integer=True)
+    x = np.random.default_rng(32).integers(-5, 6, size=A.shape[0]).astype(np.float64)
+    y0 = np.random.default_rng(33).integers(-5, 6, size=A.shape[0]).astype(np.float64)
+    oa = orc.Csr.from_scipy(A)
+    assert np.array_equal(orc.spmv(oa, x), A @ x)
+    assert np.array_equal(orc.spmv(oa, x, alpha=2.0, beta=-3.0, y=y0), 2.0 * (A @ x) - 3.0 * y0)
